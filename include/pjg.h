@@ -1,0 +1,222 @@
+/*
+ * pjg.h — C ABI of the GB300 template-matching library (libpjg.so).
+ *
+ * This is the boundary a host binding calls instead of the Jess C API that
+ * PyJess's Cython layer drives.  The reference consumes, per molecule and one
+ * candidate at a time:
+ *
+ *   Jess_create / Jess_addTemplate / Jess_free     include/jess/jess.pxd:18-21
+ *   Jess_query(J, M, t, s, reorder)                include/jess/jess.pxd:22
+ *   JessQuery_next / JessQuery_nextTemplate        include/jess/jess.pxd:24-25
+ *   JessQuery_template / JessQuery_atoms           include/jess/jess.pxd:26-27
+ *   JessQuery_superposition                        include/jess/jess.pxd:28
+ *   Superposition_rmsd / _rotation / _centroid     include/jess/super.pxd:7-14
+ *
+ * and replays the candidate automaton of Query.__next__
+ * (src/pyjess/_jess.pyx:2197-2283) on top.  This library instead takes whole
+ * batches (every template against every structure), runs the search on the
+ * GPU and returns the final, ordered hit list of each structure, with the
+ * automaton (rmsd filter, NaN-rotation skip, best_match, max_candidates)
+ * already applied.  Plain C types only; every call returns a pjg_status and
+ * never throws.  Handles are immutable after creation and may be shared by
+ * threads; each pjg_query call runs on its own stream with its own scratch.
+ */
+#ifndef PJG_H
+#define PJG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    PJG_OK = 0,
+    PJG_ERR_INVALID = 1,       /* malformed input or parameter            */
+    PJG_ERR_OOM = 2,           /* device or host allocation failed        */
+    PJG_ERR_CUDA = 3,          /* CUDA runtime error (message available)  */
+    PJG_ERR_NO_DEVICE = 4,     /* no CUDA device visible                  */
+    PJG_ERR_TIMEOUT = 5,       /* a kernel's bounded work loop ran out    */
+    PJG_ERR_CAPACITY = 6       /* an internal buffer limit was exceeded   */
+} pjg_status;
+
+/* ignore_chain modes, as the reference's IgnoreType
+ * (patches/Template.h.patch:17 ignoreNone, ignoreResidues, ignoreAtoms). */
+enum { PJG_IGNORE_NONE = 0, PJG_IGNORE_RESIDUES = 1, PJG_IGNORE_ATOMS = 2 };
+
+/* precision / launch modes of pjg_query */
+enum {
+    /* FP64 distance tests, one structure per launch sequence: the plain
+     * GPU method the batched path is measured against. */
+    PJG_MODE_PLAIN_FP64 = 0,
+    /* all pairs in one launch sequence; distance tests in FP32 on
+     * centroid-relative coordinates with a guard band, anything inside the
+     * band rechecked in FP64 with the reference's operation order. */
+    PJG_MODE_BATCHED_FP32 = 1,
+    /* all pairs in one launch sequence, FP64 distance tests. */
+    PJG_MODE_BATCHED_FP64 = 2
+};
+
+/*
+ * Templates, packed.  T templates with A atoms in total; template t owns
+ * atoms [atom_offset[t], atom_offset[t+1]).  Each template atom carries the
+ * fields of the reference's TessAtom (patches/TessAtom.h.patch:31-44):
+ * match code, residue number, chain characters, position, distance weight,
+ * atom-name alternatives and residue-name alternatives.  Names are 4 bytes,
+ * encoded as in the reference ('_' for blanks, residue names 3 chars + NUL).
+ * Corresponds to Template.__init__ / TemplateAtom.__init__
+ * (src/pyjess/_jess.pyx:1399-1495, 1825-1912) plus Jess_addTemplate.
+ */
+typedef struct {
+    int32_t n_templates;
+    const int32_t *atom_offset;      /* [T+1]                              */
+    const int32_t *code;             /* [A] match mode                     */
+    const int32_t *res_seq;          /* [A]                                */
+    const uint8_t *chain;            /* [A*2] chainID1, chainID2           */
+    const double *xyz;               /* [A*3]                              */
+    const double *dist_weight;       /* [A]                                */
+    const int32_t *name_offset;      /* [A+1] into names                   */
+    const uint8_t *names;            /* [*4]                               */
+    const int32_t *resname_offset;   /* [A+1] into resnames                */
+    const uint8_t *resnames;         /* [*4]                               */
+    const int32_t *dim;              /* [T] number of distinct residues    */
+} pjg_template_set;
+
+/*
+ * Structures (molecules), packed.  S structures with N atoms in total;
+ * structure s owns atoms [atom_offset[s], atom_offset[s+1]).  Only the Atom
+ * fields the search reads (patches/Atom.h.patch:7-26): coordinates, serial,
+ * name, residue name, chain characters, residue number.
+ * Corresponds to Molecule.__init__ (src/pyjess/_jess.pyx:632-684).
+ */
+typedef struct {
+    int32_t n_structures;
+    const int64_t *atom_offset;      /* [S+1]                              */
+    const double *xyz;               /* [N*3]                              */
+    const uint8_t *name;             /* [N*4]                              */
+    const uint8_t *resname;          /* [N*4] 3 chars + NUL                */
+    const uint8_t *chain;            /* [N*2]                              */
+    const int32_t *res_seq;          /* [N]                                */
+    const int32_t *serial;           /* [N]                                */
+} pjg_structure_set;
+
+/* Query parameters: the arguments of Jess.query
+ * (src/pyjess/_jess.pyx:2758-2869) plus the GPU execution mode. */
+typedef struct {
+    double rmsd_threshold;
+    double distance_cutoff;          /* Jess_query t                       */
+    double max_dynamic_distance;     /* Jess_query s                       */
+    int32_t max_candidates;          /* -1: unlimited                      */
+    int32_t ignore_chain;            /* PJG_IGNORE_*                       */
+    int32_t best_match;              /* 0/1                                */
+    int32_t reorder;                 /* 0/1                                */
+    int32_t mode;                    /* PJG_MODE_*                         */
+    double guard_band;               /* Angstrom, FP32 mode (0: 1e-4)      */
+} pjg_query_params;
+
+/* Per-query counters and device timings (milliseconds, CUDA events). */
+typedef struct {
+    int64_t pairs;                   /* template x structure pairs         */
+    int64_t candidate_entries;       /* sum of candidate-list lengths      */
+    int64_t partials;                /* partial assignments generated      */
+    int64_t complete;                /* complete assignments (all atoms)   */
+    int64_t passing;                 /* complete with rmsd <= threshold    */
+    int64_t hits;                    /* after the automaton                */
+    int64_t fp64_rechecks;           /* guard-band rechecks (FP32 mode)    */
+    int64_t bytes_candidates;        /* algorithmic bytes, candidate stage */
+    int64_t bytes_expansion;         /* algorithmic bytes, expansion stage */
+    int64_t bytes_superposition;     /* algorithmic bytes, superposition   */
+    double ms_candidates;
+    double ms_expansion;
+    double ms_superposition;
+    double ms_total;                 /* device time of the whole query     */
+    int32_t launches;                /* kernels launched by the query      */
+    int32_t chunks;                  /* structure chunks processed         */
+} pjg_stats;
+
+typedef struct pjg_templates pjg_templates;
+typedef struct pjg_structures pjg_structures;
+typedef struct pjg_results pjg_results;
+
+/* Library / device --------------------------------------------------------*/
+
+/* Replaces nothing (the reference has no device); returns PJG_OK and the
+ * device ordinal in use, or PJG_ERR_NO_DEVICE. */
+pjg_status pjg_init(int32_t device);
+
+/* Last error message of the calling thread (never NULL). */
+const char *pjg_last_error(void);
+
+/* Templates ---------------------------------------------------------------*/
+
+/* Replaces Jess_create + Jess_addTemplate per template + TessTemplate_copy
+ * (patches/Jess.c.patch:63-72, patches/TessTemplate.c.patch:265-337).
+ * Builds the distance matrices (TessAtom_distance, patches/TessAtom.c.patch
+ * :229-244), the per-pair annulus radii and the candidate signatures, and
+ * uploads them.  Template t keeps index t; the search visits templates in
+ * reverse index order as the reference's prepend-list does. */
+pjg_status pjg_templates_create(const pjg_template_set *set, pjg_templates **out);
+
+/* Replaces Jess_free (patches/Jess.c.patch:52-61). */
+void pjg_templates_destroy(pjg_templates *t);
+
+/* Structures --------------------------------------------------------------*/
+
+/* Replaces Molecule creation + ResIndex_create (patches/ResIndex.c.patch
+ * :24-119, src/pyjess/_jess.pyx:632-684): sorts each structure's atoms by
+ * (residue name, serial), builds the residue buckets and the FP64 and
+ * centroid-relative FP32 coordinate arrays, and uploads them. */
+pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **out);
+
+/* Replaces Molecule_free. */
+void pjg_structures_destroy(pjg_structures *s);
+
+/* Query -------------------------------------------------------------------*/
+
+/* Replaces Jess_query + the JessQuery_next / Scanner_next loop +
+ * JessQuery_superposition + the Query.__next__ automaton
+ * (patches/Jess.c.patch:74-216, patches/Scanner.c.patch:110-336,
+ * src/pyjess/_jess.pyx:2197-2283) for every structure of `s` against every
+ * template of `t`.  Results are ordered by structure, then by template in
+ * reverse index order, then by the reference's candidate order. */
+pjg_status pjg_query(const pjg_templates *t, const pjg_structures *s,
+                     const pjg_query_params *params, pjg_results **out);
+
+/* Number of hits in total and the number of template atoms of hit i's
+ * template (the length of its atom list). */
+int64_t pjg_results_count(const pjg_results *r);
+/* Sum over hits of the template atom count (size of the atom index array). */
+int64_t pjg_results_atom_count(const pjg_results *r);
+
+/* Copy the hits out.  Each array may be NULL to skip it.
+ *   structure[i], template_index[i]    which pair hit i belongs to
+ *   ordinal[i]     position of hit i in its pair's candidate stream
+ *   rmsd[i]        Superposition_rmsd
+ *   rotation[9i]   Superposition_rotation (row major, molecule -> template)
+ *   centres[6i]    Superposition_centroid(0) then (1): molecule, template
+ *   atom_offset[i] start of hit i in atoms (size count+1)
+ *   atoms[]        structure-relative atom indices, in template atom order
+ *                  (JessQuery_atoms, patches/Jess.c.patch:121-126) */
+pjg_status pjg_results_copy(const pjg_results *r, int32_t *structure,
+                            int32_t *template_index, int64_t *ordinal,
+                            double *rmsd, double *rotation, double *centres,
+                            int64_t *atom_offset, int32_t *atoms);
+
+/* NaN-rotation events that Query.__next__ reports as UserWarning
+ * (src/pyjess/_jess.pyx:2238-2251): for each event, the structure and the
+ * number of hits of that structure that precede it. */
+int64_t pjg_results_warning_count(const pjg_results *r);
+pjg_status pjg_results_warnings(const pjg_results *r, int32_t *structure,
+                                int64_t *hits_before);
+
+/* Counters and device timings of the query that produced `r`. */
+pjg_status pjg_results_stats(const pjg_results *r, pjg_stats *stats);
+
+void pjg_results_destroy(pjg_results *r);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PJG_H */
