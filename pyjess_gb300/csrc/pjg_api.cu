@@ -1,0 +1,935 @@
+// pjg_api.cu — C ABI of libpjg (include/pjg.h): template / structure
+// upload, the query pipeline and its host-side automaton.
+//
+// Pipeline of pjg_query (all on one CUDA stream owned by the call):
+//   k_params                      annulus radii for the query's r and s
+//   k_candidates<count>           |C| and |R| of every (structure, signature)
+//   k_struct_totals               candidate entries per structure
+//   per structure chunk (bounded entry budget):
+//     k_scan_*                    list offsets
+//     k_candidates<fill>          lists in candidate order
+//     k_leaf_order                lists in kd leaf order
+//     k_search                    complete assignments, ordered per pair
+//     k_superpose                 rmsd / rotation / centroids, rmsd filter
+//   host: order by (structure, template descending, ordinal) and replay the
+//   Query.__next__ automaton (src/pyjess/_jess.pyx:2197-2283) per pair.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/pjg.h"
+#include "pjg_common.cuh"
+#include "pjg_kernels.cuh"
+
+using namespace pjg;
+
+namespace {
+
+thread_local std::string g_error = "";
+
+pjg_status fail(pjg_status st, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_error = buf;
+    return st;
+}
+
+#define CUDA_TRY(expr)                                                                          \
+    do {                                                                                        \
+        cudaError_t _e = (expr);                                                                \
+        if (_e != cudaSuccess) {                                                                \
+            status = fail(_e == cudaErrorMemoryAllocation ? PJG_ERR_OOM : PJG_ERR_CUDA,         \
+                          "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e), __FILE__,     \
+                          __LINE__);                                                            \
+            goto done;                                                                          \
+        }                                                                                       \
+    } while (0)
+
+inline uint8_t up(uint8_t c) { return (c >= 'a' && c <= 'z') ? (uint8_t)(c & ~0x20) : c; }
+
+inline uint32_t pack_upper(const uint8_t *b) {
+    return (uint32_t)up(b[0]) | ((uint32_t)up(b[1]) << 8) | ((uint32_t)up(b[2]) << 16) |
+           ((uint32_t)up(b[3]) << 24);
+}
+
+inline uint32_t pack_lit(const char *s) { return pack_upper((const uint8_t *)s); }
+
+// device buffer helper (stream ordered)
+template <typename T>
+struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+};
+
+template <typename T>
+cudaError_t dalloc(DBuf<T> &b, size_t n, cudaStream_t st) {
+    if (b.n >= n && b.p) return cudaSuccess;
+    if (b.p) cudaFreeAsync(b.p, st);
+    b.p = nullptr;
+    b.n = 0;
+    size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+    cudaError_t e = cudaMallocAsync((void **)&b.p, bytes, st);
+    if (e == cudaSuccess) b.n = std::max<size_t>(n, 1);
+    return e;
+}
+
+template <typename T>
+void dfree(DBuf<T> &b, cudaStream_t st) {
+    if (b.p) cudaFreeAsync(b.p, st);
+    b.p = nullptr;
+    b.n = 0;
+}
+
+template <typename T>
+cudaError_t upload(T **dst, const std::vector<T> &v) {
+    size_t bytes = std::max<size_t>(v.size(), 1) * sizeof(T);
+    cudaError_t e = cudaMalloc((void **)dst, bytes);
+    if (e != cudaSuccess) return e;
+    if (!v.empty()) e = cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return e;
+}
+
+// Chemically equivalent atom pairs used by match mode 1 (see the oracle's
+// same_position rule; pinned by the reference fixture for ASN OD1/ND2).
+struct PartnerDef { const char *res; const char *a; const char *b; };
+const PartnerDef PARTNER_TABLE[] = {
+    {"ASP", "_OD1", "_OD2"}, {"GLU", "_OE1", "_OE2"}, {"ASN", "_OD1", "_ND2"},
+    {"GLN", "_OE1", "_NE2"}, {"ARG", "_NH1", "_NH2"}, {"HIS", "_ND1", "_CD2"},
+    {"HIS", "_CE1", "_NE2"}, {"PHE", "_CD1", "_CD2"}, {"PHE", "_CE1", "_CE2"},
+    {"TYR", "_CD1", "_CD2"}, {"TYR", "_CE1", "_CE2"}, {"LEU", "_CD1", "_CD2"},
+    {"VAL", "_CG1", "_CG2"},
+};
+
+uint32_t res_lit(const char *three) {
+    uint8_t b[4] = {(uint8_t)three[0], (uint8_t)three[1], (uint8_t)three[2], 0};
+    return pack_upper(b);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Handles
+
+struct pjg_templates {
+    int32_t T = 0, A = 0, nmax = 0, G = 0;
+    std::vector<int32_t> atom_begin, param_begin, dim;
+    // device
+    int32_t *d_atom_begin = nullptr, *d_sig = nullptr, *d_key = nullptr, *d_param_begin = nullptr;
+    double *d_pos = nullptr, *d_weight = nullptr, *d_dist = nullptr;
+    int32_t *d_code = nullptr, *d_rule = nullptr, *d_mainchain = nullptr, *d_name_begin = nullptr,
+            *d_res_begin = nullptr, *d_partner_begin = nullptr;
+    uint32_t *d_names = nullptr, *d_resnames = nullptr, *d_partner_res = nullptr, *d_partner_name = nullptr;
+    int64_t n_params = 0;
+    int device = 0;
+};
+
+struct pjg_structures {
+    int32_t S = 0;
+    int64_t N = 0;
+    int32_t max_atoms = 0;
+    double max_radius = 0.0;
+    std::vector<int64_t> atom_base;
+    int64_t *d_atom_base = nullptr;
+    int32_t *d_atom_count = nullptr;
+    double *d_xyz64 = nullptr;
+    float4 *d_xyz32 = nullptr;
+    uint32_t *d_name = nullptr, *d_resname = nullptr;
+    int32_t *d_sorted = nullptr;
+    int32_t *d_bucket_begin = nullptr, *d_bucket_lo = nullptr, *d_bucket_hi = nullptr;
+    uint32_t *d_bucket_name = nullptr;
+    int device = 0;
+};
+
+struct HitRec {
+    int32_t s, t;
+    int64_t ordinal;
+    double rmsd;
+    int32_t nan_rot;
+    double rot[9], centres[6];
+    int64_t atom_at;  // into atom store
+};
+
+struct pjg_results {
+    std::vector<int32_t> structure, tpl;
+    std::vector<int64_t> ordinal;
+    std::vector<double> rmsd, rot, centres;
+    std::vector<int64_t> atom_offset{0};
+    std::vector<int32_t> atoms;
+    std::vector<int32_t> warn_structure;
+    std::vector<int64_t> warn_before;
+    pjg_stats stats{};
+};
+
+extern "C" {
+
+const char *pjg_last_error(void) { return g_error.c_str(); }
+
+pjg_status pjg_init(int32_t device) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        return fail(PJG_ERR_NO_DEVICE, "no CUDA device: %s", e == cudaSuccess ? "count is 0" : cudaGetErrorString(e));
+    if (device < 0 || device >= n) return fail(PJG_ERR_INVALID, "device %d out of range (%d devices)", device, n);
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return fail(PJG_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+    return PJG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Templates
+
+pjg_status pjg_templates_create(const pjg_template_set *set, pjg_templates **out) {
+    pjg_status status = PJG_OK;
+    if (!set || !out) return fail(PJG_ERR_INVALID, "null argument");
+    if (set->n_templates < 0) return fail(PJG_ERR_INVALID, "negative template count");
+    int T = set->n_templates;
+    if (T > 0 && (!set->atom_offset)) return fail(PJG_ERR_INVALID, "null atom_offset");
+    int A = T > 0 ? set->atom_offset[T] : 0;
+    if (A > 0 && (!set->code || !set->res_seq || !set->chain || !set->xyz || !set->dist_weight ||
+                  !set->name_offset || !set->resname_offset))
+        return fail(PJG_ERR_INVALID, "null template atom array");
+    pjg_templates *h = new pjg_templates;
+    cudaGetDevice(&h->device);
+    h->T = T;
+    h->A = A;
+    h->atom_begin.assign(set->atom_offset, set->atom_offset + T + 1);
+    if (T == 0) h->atom_begin = {0};
+    std::vector<int32_t> sig(A), key(A);
+    std::vector<double> pos(3 * (size_t)A), weight(A);
+    // signatures
+    std::map<std::vector<uint32_t>, int> sig_ids;
+    std::vector<int32_t> s_code, s_rule, s_main, s_nb{0}, s_rb{0}, s_pb{0};
+    std::vector<uint32_t> s_names, s_res, s_pres, s_pname;
+    for (int t = 0; t < T; t++) {
+        int a0 = set->atom_offset[t], a1 = set->atom_offset[t + 1];
+        if (a1 < a0) {
+            delete h;
+            return fail(PJG_ERR_INVALID, "template %d: decreasing atom offsets", t);
+        }
+        if (a1 - a0 > 32) {
+            delete h;
+            return fail(PJG_ERR_INVALID, "template %d has %d atoms; at most 32 are supported", t, a1 - a0);
+        }
+        h->nmax = std::max(h->nmax, a1 - a0);
+    }
+    for (int a = 0; a < A; a++) {
+        int code = set->code[a];
+        bool valid = (code >= -1 && code <= 8) || (code >= 100 && code <= 107);
+        if (!valid) {
+            delete h;
+            return fail(PJG_ERR_INVALID, "template atom %d: invalid match mode %d", a, code);
+        }
+        std::vector<uint32_t> names, res;
+        for (int q = set->name_offset[a]; q < set->name_offset[a + 1]; q++) names.push_back(pack_upper(set->names + 4 * q));
+        for (int q = set->resname_offset[a]; q < set->resname_offset[a + 1]; q++) {
+            uint32_t r = pack_upper(set->resnames + 4 * q);
+            if (std::find(res.begin(), res.end(), r) == res.end()) res.push_back(r);
+        }
+        std::vector<uint32_t> keyv;
+        keyv.push_back((uint32_t)code);
+        keyv.push_back((uint32_t)names.size());
+        keyv.insert(keyv.end(), names.begin(), names.end());
+        keyv.insert(keyv.end(), res.begin(), res.end());
+        auto it = sig_ids.find(keyv);
+        int id;
+        if (it == sig_ids.end()) {
+            id = (int)s_code.size();
+            sig_ids.emplace(keyv, id);
+            int mode = code >= 100 ? code - 100 : code;
+            int rule = mode == -1 ? RULE_ANY : mode == 1 ? RULE_NAME_OR_PARTNER : mode == 2 ? RULE_NAME_OR_MAINCHAIN
+                     : mode == 3 ? RULE_ELEMENT : RULE_NAME;
+            s_code.push_back(code);
+            s_rule.push_back(rule);
+            int mc = 0;
+            for (uint32_t nm : names)
+                if (nm == pack_lit("_CA_") || nm == pack_lit("_N__") || nm == pack_lit("_O__")) mc = 1;
+            s_main.push_back(mc);
+            s_names.insert(s_names.end(), names.begin(), names.end());
+            s_nb.push_back((int32_t)s_names.size());
+            s_res.insert(s_res.end(), res.begin(), res.end());
+            s_rb.push_back((int32_t)s_res.size());
+            if (rule == RULE_NAME_OR_PARTNER) {
+                for (uint32_t nm : names)
+                    for (const PartnerDef &p : PARTNER_TABLE) {
+                        if (nm == pack_lit(p.a)) {
+                            s_pres.push_back(res_lit(p.res));
+                            s_pname.push_back(pack_lit(p.b));
+                        }
+                        if (nm == pack_lit(p.b)) {
+                            s_pres.push_back(res_lit(p.res));
+                            s_pname.push_back(pack_lit(p.a));
+                        }
+                    }
+            }
+            s_pb.push_back((int32_t)s_pres.size());
+        } else {
+            id = it->second;
+        }
+        sig[a] = id;
+        key[a] = make_key(set->res_seq[a], set->chain[2 * a + 1]);
+        for (int d = 0; d < 3; d++) pos[3 * (size_t)a + d] = set->xyz[3 * (size_t)a + d];
+        weight[a] = set->dist_weight[a];
+    }
+    h->G = (int32_t)s_code.size();
+    // distance matrices (TessAtom_distance, patches/TessAtom.c.patch:229-244;
+    // Template.__init__, src/pyjess/_jess.pyx:1894-1901)
+    std::vector<double> dist;
+    h->param_begin.push_back(0);
+    for (int t = 0; t < T; t++) {
+        int a0 = set->atom_offset[t], n = set->atom_offset[t + 1] - a0;
+        size_t base = dist.size();
+        dist.resize(base + (size_t)n * n, 0.0);
+        for (int i = 0; i < n; i++)
+            for (int j = i + 1; j < n; j++) {
+                double acc = 0.0;
+                for (int d = 0; d < 3; d++) {
+                    double tmp = pos[3 * (size_t)(a0 + i) + d] - pos[3 * (size_t)(a0 + j) + d];
+                    acc += tmp * tmp;
+                }
+                acc = std::sqrt(acc);
+                dist[base + (size_t)i * n + j] = acc;
+                dist[base + (size_t)j * n + i] = acc;
+            }
+        h->param_begin.push_back((int32_t)dist.size());
+    }
+    h->n_params = (int64_t)dist.size();
+    if (set->dim) h->dim.assign(set->dim, set->dim + T);
+    {
+        cudaError_t e = cudaSuccess;
+        if (e == cudaSuccess) e = upload(&h->d_atom_begin, h->atom_begin);
+        if (e == cudaSuccess) e = upload(&h->d_sig, sig);
+        if (e == cudaSuccess) e = upload(&h->d_key, key);
+        if (e == cudaSuccess) e = upload(&h->d_param_begin, h->param_begin);
+        if (e == cudaSuccess) e = upload(&h->d_pos, pos);
+        if (e == cudaSuccess) e = upload(&h->d_weight, weight);
+        if (e == cudaSuccess) e = upload(&h->d_dist, dist);
+        if (e == cudaSuccess) e = upload(&h->d_code, s_code);
+        if (e == cudaSuccess) e = upload(&h->d_rule, s_rule);
+        if (e == cudaSuccess) e = upload(&h->d_mainchain, s_main);
+        if (e == cudaSuccess) e = upload(&h->d_name_begin, s_nb);
+        if (e == cudaSuccess) e = upload(&h->d_names, s_names);
+        if (e == cudaSuccess) e = upload(&h->d_res_begin, s_rb);
+        if (e == cudaSuccess) e = upload(&h->d_resnames, s_res);
+        if (e == cudaSuccess) e = upload(&h->d_partner_begin, s_pb);
+        if (e == cudaSuccess) e = upload(&h->d_partner_res, s_pres);
+        if (e == cudaSuccess) e = upload(&h->d_partner_name, s_pname);
+        if (e != cudaSuccess) {
+            status = fail(e == cudaErrorMemoryAllocation ? PJG_ERR_OOM : PJG_ERR_CUDA, "template upload: %s",
+                          cudaGetErrorString(e));
+            pjg_templates_destroy(h);
+            return status;
+        }
+    }
+    *out = h;
+    return PJG_OK;
+}
+
+void pjg_templates_destroy(pjg_templates *h) {
+    if (!h) return;
+    void *ptrs[] = {h->d_atom_begin, h->d_sig, h->d_key, h->d_param_begin, h->d_pos, h->d_weight, h->d_dist,
+                    h->d_code, h->d_rule, h->d_mainchain, h->d_name_begin, h->d_names, h->d_res_begin,
+                    h->d_resnames, h->d_partner_begin, h->d_partner_res, h->d_partner_name};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    delete h;
+}
+
+// ---------------------------------------------------------------------------
+// Structures
+
+pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **out) {
+    if (!set || !out) return fail(PJG_ERR_INVALID, "null argument");
+    if (set->n_structures < 0) return fail(PJG_ERR_INVALID, "negative structure count");
+    int S = set->n_structures;
+    if (S > 0 && !set->atom_offset) return fail(PJG_ERR_INVALID, "null atom_offset");
+    int64_t N = S > 0 ? set->atom_offset[S] : 0;
+    if (N > 0 && (!set->xyz || !set->name || !set->resname || !set->chain || !set->res_seq || !set->serial))
+        return fail(PJG_ERR_INVALID, "null structure atom array");
+    pjg_structures *h = new pjg_structures;
+    cudaGetDevice(&h->device);
+    h->S = S;
+    h->N = N;
+    std::vector<int64_t> base(std::max(S, 0));
+    std::vector<int32_t> count(std::max(S, 0));
+    std::vector<float4> xyz32(N);
+    std::vector<uint32_t> name(N), resname(N);
+    std::vector<int32_t> sorted(N), bucket_begin{0}, bucket_lo, bucket_hi;
+    std::vector<uint32_t> bucket_name;
+    for (int s = 0; s < S; s++) {
+        int64_t b0 = set->atom_offset[s], b1 = set->atom_offset[s + 1];
+        if (b1 < b0) {
+            delete h;
+            return fail(PJG_ERR_INVALID, "structure %d: decreasing atom offsets", s);
+        }
+        if (b1 - b0 > INT32_MAX / 2) {
+            delete h;
+            return fail(PJG_ERR_INVALID, "structure %d too large", s);
+        }
+        int n = (int)(b1 - b0);
+        base[s] = b0;
+        count[s] = n;
+        h->max_atoms = std::max(h->max_atoms, n);
+        double c[3] = {0, 0, 0};
+        for (int i = 0; i < n; i++)
+            for (int d = 0; d < 3; d++) c[d] += set->xyz[3 * (b0 + i) + d];
+        if (n > 0)
+            for (int d = 0; d < 3; d++) c[d] /= (double)n;
+        for (int i = 0; i < n; i++) {
+            int64_t a = b0 + i;
+            double dx = set->xyz[3 * a] - c[0], dy = set->xyz[3 * a + 1] - c[1], dz = set->xyz[3 * a + 2] - c[2];
+            double r = std::sqrt(dx * dx + dy * dy + dz * dz);
+            if (r > h->max_radius) h->max_radius = r;
+            int32_t k = make_key(set->res_seq[a], set->chain[2 * a + 1]);
+            float kf;
+            std::memcpy(&kf, &k, 4);
+            xyz32[a] = make_float4((float)dx, (float)dy, (float)dz, kf);
+            name[a] = pack_upper(set->name + 4 * a);
+            resname[a] = pack_upper(set->resname + 4 * a);
+        }
+        // ResIndex: stable order by (residue name, serial)
+        std::vector<int32_t> idx(n);
+        std::iota(idx.begin(), idx.end(), 0);
+        auto bigkey = [&](int i) {
+            const uint8_t *r = set->resname + 4 * (b0 + i);
+            return ((uint32_t)up(r[0]) << 24) | ((uint32_t)up(r[1]) << 16) | ((uint32_t)up(r[2]) << 8) | up(r[3]);
+        };
+        std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) {
+            uint32_t kx = bigkey(x), ky = bigkey(y);
+            if (kx != ky) return kx < ky;
+            return set->serial[b0 + x] < set->serial[b0 + y];
+        });
+        for (int i = 0; i < n; i++) {
+            sorted[b0 + i] = idx[i];
+            uint32_t rn = resname[b0 + idx[i]];
+            if (i == 0 || rn != bucket_name.back()) {
+                if (i > 0) bucket_hi.push_back(i);
+                bucket_name.push_back(rn);
+                bucket_lo.push_back(i);
+            }
+        }
+        if (n > 0) bucket_hi.push_back(n);
+        bucket_begin.push_back((int32_t)bucket_name.size());
+    }
+    h->atom_base = base;
+    std::vector<double> xyz64(set->xyz, set->xyz + 3 * N);
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = upload(&h->d_atom_base, base);
+    if (e == cudaSuccess) e = upload(&h->d_atom_count, count);
+    if (e == cudaSuccess) e = upload(&h->d_xyz64, xyz64);
+    if (e == cudaSuccess) e = upload(&h->d_xyz32, xyz32);
+    if (e == cudaSuccess) e = upload(&h->d_name, name);
+    if (e == cudaSuccess) e = upload(&h->d_resname, resname);
+    if (e == cudaSuccess) e = upload(&h->d_sorted, sorted);
+    if (e == cudaSuccess) e = upload(&h->d_bucket_begin, bucket_begin);
+    if (e == cudaSuccess) e = upload(&h->d_bucket_name, bucket_name);
+    if (e == cudaSuccess) e = upload(&h->d_bucket_lo, bucket_lo);
+    if (e == cudaSuccess) e = upload(&h->d_bucket_hi, bucket_hi);
+    if (e != cudaSuccess) {
+        pjg_status st = fail(e == cudaErrorMemoryAllocation ? PJG_ERR_OOM : PJG_ERR_CUDA, "structure upload: %s",
+                             cudaGetErrorString(e));
+        pjg_structures_destroy(h);
+        return st;
+    }
+    *out = h;
+    return PJG_OK;
+}
+
+void pjg_structures_destroy(pjg_structures *h) {
+    if (!h) return;
+    void *ptrs[] = {h->d_atom_base, h->d_atom_count, h->d_xyz64, h->d_xyz32, h->d_name, h->d_resname,
+                    h->d_sorted, h->d_bucket_begin, h->d_bucket_name, h->d_bucket_lo, h->d_bucket_hi};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    delete h;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Query
+
+namespace {
+
+__global__ void k_struct_totals(int32_t S, int32_t G, const int32_t *count, int64_t *totals) {
+    int lane = threadIdx.x & 31;
+    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = warp; s < S; s += nw) {
+        int64_t acc = 0;
+        for (int g = lane; g < G; g += 32) acc += count[s * G + g];
+        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) totals[s] = acc;
+    }
+}
+
+int sm_count() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+// exclusive scan in[0..n) -> out[0..n), recursive over tile sums
+template <typename T>
+cudaError_t scan_exclusive(const T *in, int64_t n, int64_t *out, std::vector<DBuf<int64_t>> &tmp,
+                           cudaStream_t st, int depth = 0) {
+    if (n <= 0) return cudaSuccess;
+    const int TILE = SCAN_TILE_ITEMS;
+    int64_t tiles = (n + TILE - 1) / TILE;
+    if ((int)tmp.size() < 2 * (depth + 1)) tmp.resize(2 * (depth + 1));
+    cudaError_t e = dalloc(tmp[2 * depth], (size_t)tiles, st);
+    if (e != cudaSuccess) return e;
+    e = dalloc(tmp[2 * depth + 1], (size_t)tiles, st);
+    if (e != cudaSuccess) return e;
+    int64_t *sums = tmp[2 * depth].p, *soff = tmp[2 * depth + 1].p;
+    if constexpr (sizeof(T) == 4) launch_scan_tiles_i32(st, in, n, out, sums);
+    else launch_scan_tiles_i64(st, in, n, out, sums);
+    if (tiles > 1) {
+        e = scan_exclusive<int64_t>(sums, tiles, soff, tmp, st, depth + 1);
+        if (e != cudaSuccess) return e;
+        launch_scan_add(st, out, n, soff);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *sp, const pjg_query_params *P,
+                                pjg_results **out) {
+    pjg_status status = PJG_OK;
+    if (!tp || !sp || !P || !out) return fail(PJG_ERR_INVALID, "null argument");
+    if (P->ignore_chain < 0 || P->ignore_chain > 2) return fail(PJG_ERR_INVALID, "invalid ignore_chain %d", P->ignore_chain);
+    if (P->max_candidates < -1) return fail(PJG_ERR_INVALID, "invalid max_candidates %d", P->max_candidates);
+    if (P->mode < 0 || P->mode > 2) return fail(PJG_ERR_INVALID, "invalid mode %d", P->mode);
+    if (!std::isfinite(P->distance_cutoff) || !std::isfinite(P->max_dynamic_distance))
+        return fail(PJG_ERR_INVALID, "non-finite distance parameters");
+
+    pjg_results *res = new pjg_results;
+    const int T = tp->T, S = sp->S, G = tp->G;
+    const bool fp32 = P->mode == PJG_MODE_BATCHED_FP32;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[8] = {};
+    DBuf<AnnulusParam> d_params;
+    DBuf<int32_t> d_count, d_scanned, d_cand_atom, d_leaf_atom, d_pair_counter;
+    DBuf<int64_t> d_offset, d_totals;
+    DBuf<float4> d_cand_xyz, d_leaf_xyz;
+    DBuf<unsigned long long> d_counters, d_ccount, d_pcount;
+    DBuf<int32_t> d_c_pair, d_c_atoms, d_p_pair, d_p_nan, d_p_atoms;
+    DBuf<int64_t> d_c_ord, d_p_row, d_p_ord;
+    DBuf<double> d_p_rmsd, d_p_rot, d_p_cen;
+    std::vector<DBuf<int64_t>> scan_tmp;
+    std::vector<HitRec> recs;
+    std::vector<int32_t> rec_atoms;
+    const int stride = std::max(tp->nmax, 1);
+    unsigned long long counters[C_NUM] = {};
+    float ms = 0.f;
+    double ms_cand = 0, ms_exp = 0, ms_sup = 0, ms_total = 0;
+    int launches = 0, chunks = 0;
+    std::vector<int64_t> totals(S);
+
+    if (T == 0 || S == 0) {
+        *out = res;
+        return PJG_OK;
+    }
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (dev != tp->device || dev != sp->device) {
+            delete res;
+            return fail(PJG_ERR_INVALID, "templates, structures and the calling thread use different devices");
+        }
+    }
+    CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    for (auto &e : ev) CUDA_TRY(cudaEventCreate(&e));
+    CUDA_TRY(cudaEventRecord(ev[0], st));
+
+    {
+        // guard band: the requested width, widened if the FP32 rounding bound
+        // of the largest structure needs more (error of a squared distance is
+        // below 2^-24 (10.4 R d + 4 d^2) for coordinates within R of the
+        // centroid; see DESIGN)
+        double g = P->guard_band > 0 ? P->guard_band : 1e-4;
+        double bound = 2.0 * std::ldexp(1.0, -24) * (5.2 * sp->max_radius + 2.0 * (2.0 * sp->max_radius + 1.0));
+        if (bound > g) g = bound;
+        CUDA_TRY(dalloc(d_params, (size_t)std::max<int64_t>(tp->n_params, 1), st));
+        launch_params(st, T, tp->d_atom_begin, tp->d_param_begin, tp->d_dist, tp->d_weight,
+                      P->distance_cutoff, P->max_dynamic_distance, g, d_params.p);
+        launches++;
+        CUDA_TRY(cudaGetLastError());
+    }
+    CUDA_TRY(dalloc(d_counters, C_NUM, st));
+    CUDA_TRY(cudaMemsetAsync(d_counters.p, 0, C_NUM * sizeof(unsigned long long), st));
+    CUDA_TRY(dalloc(d_pair_counter, 1, st));
+    CUDA_TRY(dalloc(d_ccount, 1, st));
+    CUDA_TRY(dalloc(d_pcount, 1, st));
+
+    {
+        // pass 1: list lengths for every (structure, signature)
+        int64_t W = (int64_t)S * G;
+        CUDA_TRY(dalloc(d_count, (size_t)W, st));
+        CUDA_TRY(dalloc(d_scanned, (size_t)W, st));
+        CUDA_TRY(dalloc(d_totals, (size_t)S, st));
+        ChunkView cv{S, sp->d_atom_base, sp->d_atom_count, sp->d_xyz64, sp->d_xyz32, sp->d_name, sp->d_resname,
+                     sp->d_sorted, sp->d_bucket_begin, sp->d_bucket_name, sp->d_bucket_lo, sp->d_bucket_hi};
+        SigView sv{G, tp->d_code, tp->d_rule, tp->d_mainchain, tp->d_name_begin, tp->d_names, tp->d_res_begin,
+                   tp->d_resnames, tp->d_partner_begin, tp->d_partner_res, tp->d_partner_name};
+        int blocks = (int)std::min<int64_t>((W + 7) / 8, (int64_t)sm_count() * 32);
+        launch_candidates(st, std::max(blocks, 1), false, cv, sv, d_count.p, d_scanned.p, nullptr, nullptr, nullptr);
+        k_struct_totals<<<std::max(1, std::min(S, sm_count() * 8)), 256, 0, st>>>(S, G, d_count.p, d_totals.p);
+        launches += 2;
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaMemcpyAsync(totals.data(), d_totals.p, sizeof(int64_t) * S, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+    }
+
+    {
+        // chunks of structures under an entry budget
+        const int64_t ENTRY_BUDGET = 48ll << 20;
+        const int max_chunk = P->mode == PJG_MODE_PLAIN_FP64 ? 1 : 4096;
+        int s0 = 0;
+        int64_t c_cap = 1 << 20, p_cap = 1 << 18;
+        CUDA_TRY(dalloc(d_c_pair, c_cap, st));
+        CUDA_TRY(dalloc(d_c_ord, c_cap, st));
+        CUDA_TRY(dalloc(d_c_atoms, (size_t)c_cap * stride, st));
+        while (s0 < S) {
+            int s1 = s0;
+            int64_t entries = 0;
+            while (s1 < S && (s1 == s0 || (entries + totals[s1] <= ENTRY_BUDGET && s1 - s0 < max_chunk))) {
+                entries += totals[s1];
+                s1++;
+            }
+            chunks++;
+            const int Sc = s1 - s0;
+            const int64_t Wc = (int64_t)Sc * G;
+            ChunkView cv{Sc, sp->d_atom_base + s0, sp->d_atom_count + s0, sp->d_xyz64, sp->d_xyz32, sp->d_name,
+                         sp->d_resname, sp->d_sorted, sp->d_bucket_begin + s0, sp->d_bucket_name, sp->d_bucket_lo,
+                         sp->d_bucket_hi};
+            SigView sv{G, tp->d_code, tp->d_rule, tp->d_mainchain, tp->d_name_begin, tp->d_names, tp->d_res_begin,
+                       tp->d_resnames, tp->d_partner_begin, tp->d_partner_res, tp->d_partner_name};
+            int32_t *cnt_c = d_count.p + (int64_t)s0 * G;
+            int32_t *scn_c = d_scanned.p + (int64_t)s0 * G;
+            CUDA_TRY(dalloc(d_offset, (size_t)Wc, st));
+            CUDA_TRY(cudaEventRecord(ev[1], st));
+            CUDA_TRY(scan_exclusive(cnt_c, Wc, d_offset.p, scan_tmp, st));
+            CUDA_TRY(dalloc(d_cand_atom, (size_t)entries, st));
+            CUDA_TRY(dalloc(d_leaf_atom, (size_t)entries, st));
+            CUDA_TRY(dalloc(d_cand_xyz, (size_t)entries, st));
+            CUDA_TRY(dalloc(d_leaf_xyz, (size_t)entries, st));
+            {
+                int blocks = (int)std::min<int64_t>((Wc + 7) / 8, (int64_t)sm_count() * 32);
+                launch_candidates(st, std::max(blocks, 1), true, cv, sv, nullptr, nullptr, d_offset.p, d_cand_atom.p,
+                                  d_cand_xyz.p);
+                int lb = (int)std::min<int64_t>((Wc + 127) / 128, (int64_t)sm_count() * 16);
+                launch_leaf_order(st, std::max(lb, 1), cv, G, cnt_c, d_offset.p, d_cand_atom.p, d_cand_xyz.p,
+                                  d_leaf_atom.p, d_leaf_xyz.p);
+                launches += 2;
+                CUDA_TRY(cudaGetLastError());
+            }
+            CUDA_TRY(cudaEventRecord(ev[2], st));
+            TemplateView tv{T, tp->nmax, tp->d_atom_begin, tp->d_sig, tp->d_pos, tp->d_key, tp->d_param_begin,
+                            d_params.p};
+            CandView cd{G, cnt_c, d_offset.p, d_cand_atom.p, d_cand_xyz.p, d_leaf_atom.p, d_leaf_xyz.p};
+            SearchArgs sa;
+            sa.n_pairs = Sc * T;
+            if ((int64_t)Sc * T > INT32_MAX) {
+                status = fail(PJG_ERR_CAPACITY, "too many pairs in one chunk");
+                goto done;
+            }
+            sa.ignore_chain = P->ignore_chain;
+            sa.reorder = P->reorder;
+            sa.best_match = P->best_match;
+            sa.max_candidates = P->max_candidates;
+            sa.warp_smem = 16 * 1024;
+            {
+                const char *b = getenv("PJG_KERNEL_BUDGET_S");
+                double sec = b ? atof(b) : 120.0;
+                if (!(sec > 0)) sec = 120.0;
+                sa.budget_ns = (uint64_t)(sec * 1e9);
+            }
+            bool wide = sp->max_atoms > 65535;
+            // counters before this chunk's search, restored if it must rerun
+            unsigned long long snap[C_NUM];
+            CUDA_TRY(cudaMemcpyAsync(snap, d_counters.p, sizeof snap, cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(cudaStreamSynchronize(st));
+            for (int attempt = 0; attempt < 8; attempt++) {
+                CUDA_TRY(cudaMemsetAsync(d_pair_counter.p, 0, sizeof(int32_t), st));
+                CUDA_TRY(cudaMemsetAsync(d_ccount.p, 0, sizeof(unsigned long long), st));
+                CompleteRows cr{d_ccount.p, c_cap, stride, d_c_pair.p, d_c_ord.p, d_c_atoms.p};
+                int grid = sm_count() * 8;
+                CUDA_TRY(launch_search(st, grid, wide, fp32, cv, tv, cd, sa, d_pair_counter.p, scn_c, cr, d_counters.p));
+                launches++;
+                CUDA_TRY(cudaGetLastError());
+                unsigned long long nc = 0;
+                CUDA_TRY(cudaMemcpyAsync(&nc, d_ccount.p, sizeof nc, cudaMemcpyDeviceToHost, st));
+                CUDA_TRY(cudaStreamSynchronize(st));
+                if ((int64_t)nc <= c_cap) break;
+                // the row buffer was too small: grow and run the chunk again
+                // (the counters of the failed attempt are rolled back)
+                c_cap = (int64_t)nc + nc / 4 + 1024;
+                CUDA_TRY(dalloc(d_c_pair, c_cap, st));
+                CUDA_TRY(dalloc(d_c_ord, c_cap, st));
+                CUDA_TRY(dalloc(d_c_atoms, (size_t)c_cap * stride, st));
+                CUDA_TRY(cudaMemcpyAsync(d_counters.p, snap, sizeof snap, cudaMemcpyHostToDevice, st));
+            }
+            CUDA_TRY(cudaEventRecord(ev[3], st));
+            {
+                unsigned long long nc = 0;
+                CUDA_TRY(cudaMemcpyAsync(&nc, d_ccount.p, sizeof nc, cudaMemcpyDeviceToHost, st));
+                CUDA_TRY(cudaStreamSynchronize(st));
+                CompleteRows cr{d_ccount.p, c_cap, stride, d_c_pair.p, d_c_ord.p, d_c_atoms.p};
+                int64_t need = std::max<int64_t>((int64_t)nc, 1);
+                if (need > p_cap) p_cap = need;
+                CUDA_TRY(dalloc(d_p_row, p_cap, st));
+                CUDA_TRY(dalloc(d_p_pair, p_cap, st));
+                CUDA_TRY(dalloc(d_p_ord, p_cap, st));
+                CUDA_TRY(dalloc(d_p_rmsd, p_cap, st));
+                CUDA_TRY(dalloc(d_p_nan, p_cap, st));
+                CUDA_TRY(dalloc(d_p_rot, (size_t)p_cap * 9, st));
+                CUDA_TRY(dalloc(d_p_cen, (size_t)p_cap * 6, st));
+                CUDA_TRY(dalloc(d_p_atoms, (size_t)p_cap * stride, st));
+                CUDA_TRY(cudaMemsetAsync(d_pcount.p, 0, sizeof(unsigned long long), st));
+                PassRows pr{d_pcount.p, p_cap, stride, d_p_row.p, d_p_pair.p, d_p_ord.p, d_p_rmsd.p,
+                            d_p_nan.p, d_p_rot.p, d_p_cen.p, d_p_atoms.p};
+                SuperArgs su{P->rmsd_threshold};
+                TemplateView tv2 = tv;
+                if (nc > 0) {
+                    int blocks = (int)std::min<int64_t>(((int64_t)nc + 7) / 8, (int64_t)sm_count() * 32);
+                    launch_superpose(st, blocks, cv, tv2, su, cr, pr, d_counters.p);
+                    launches++;
+                    CUDA_TRY(cudaGetLastError());
+                }
+                CUDA_TRY(cudaEventRecord(ev[4], st));
+                unsigned long long np = 0;
+                CUDA_TRY(cudaMemcpyAsync(&np, d_pcount.p, sizeof np, cudaMemcpyDeviceToHost, st));
+                CUDA_TRY(cudaStreamSynchronize(st));
+                if ((int64_t)np > p_cap) {
+                    status = fail(PJG_ERR_CAPACITY, "passing-row buffer overflow");
+                    goto done;
+                }
+                std::vector<int32_t> pair(np), nan(np), atoms((size_t)np * stride);
+                std::vector<int64_t> ord(np);
+                std::vector<double> rm(np), rot((size_t)np * 9), cen((size_t)np * 6);
+                if (np > 0) {
+                    CUDA_TRY(cudaMemcpyAsync(pair.data(), d_p_pair.p, np * 4, cudaMemcpyDeviceToHost, st));
+                    CUDA_TRY(cudaMemcpyAsync(nan.data(), d_p_nan.p, np * 4, cudaMemcpyDeviceToHost, st));
+                    CUDA_TRY(cudaMemcpyAsync(ord.data(), d_p_ord.p, np * 8, cudaMemcpyDeviceToHost, st));
+                    CUDA_TRY(cudaMemcpyAsync(rm.data(), d_p_rmsd.p, np * 8, cudaMemcpyDeviceToHost, st));
+                    CUDA_TRY(cudaMemcpyAsync(rot.data(), d_p_rot.p, np * 72, cudaMemcpyDeviceToHost, st));
+                    CUDA_TRY(cudaMemcpyAsync(cen.data(), d_p_cen.p, np * 48, cudaMemcpyDeviceToHost, st));
+                    CUDA_TRY(cudaMemcpyAsync(atoms.data(), d_p_atoms.p, (size_t)np * stride * 4, cudaMemcpyDeviceToHost, st));
+                    CUDA_TRY(cudaStreamSynchronize(st));
+                }
+                for (unsigned long long i = 0; i < np; i++) {
+                    HitRec r;
+                    r.s = s0 + pair[i] / T;
+                    r.t = pair[i] % T;
+                    r.ordinal = ord[i];
+                    r.rmsd = rm[i];
+                    r.nan_rot = nan[i];
+                    std::memcpy(r.rot, &rot[9 * i], 72);
+                    std::memcpy(r.centres, &cen[6 * i], 48);
+                    r.atom_at = (int64_t)rec_atoms.size();
+                    int n = tp->atom_begin[r.t + 1] - tp->atom_begin[r.t];
+                    rec_atoms.insert(rec_atoms.end(), &atoms[(size_t)i * stride], &atoms[(size_t)i * stride] + n);
+                    recs.push_back(r);
+                }
+                float m1 = 0, m2 = 0, m3 = 0;
+                cudaEventElapsedTime(&m1, ev[1], ev[2]);
+                cudaEventElapsedTime(&m2, ev[2], ev[3]);
+                cudaEventElapsedTime(&m3, ev[3], ev[4]);
+                ms_cand += m1;
+                ms_exp += m2;
+                ms_sup += m3;
+            }
+            s0 = s1;
+        }
+    }
+    CUDA_TRY(cudaMemcpyAsync(counters, d_counters.p, sizeof counters, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaEventRecord(ev[5], st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    cudaEventElapsedTime(&ms, ev[0], ev[5]);
+    ms_total = ms;
+    if (counters[C_ERROR] == 3) {
+        status = fail(PJG_ERR_TIMEOUT, "search kernel exceeded its time budget (PJG_KERNEL_BUDGET_S)");
+        goto done;
+    }
+    if (counters[C_ERROR]) {
+        status = fail(PJG_ERR_CAPACITY, "search kernel reported error %llu (template too large for the frontier tile)",
+                      counters[C_ERROR]);
+        goto done;
+    }
+
+    {
+        // order: structure, template in reverse index order (the reference's
+        // prepend list, patches/Jess.c.patch:63-72), stream ordinal
+        std::vector<size_t> idx(recs.size());
+        std::iota(idx.begin(), idx.end(), 0);
+        std::sort(idx.begin(), idx.end(), [&](size_t a, size_t b) {
+            const HitRec &x = recs[a], &y = recs[b];
+            if (x.s != y.s) return x.s < y.s;
+            if (x.t != y.t) return x.t > y.t;
+            return x.ordinal < y.ordinal;
+        });
+        // automaton of Query.__next__ per pair (closed form):
+        //  best_match: over rows with ordinal <= M+1 (M = max_candidates),
+        //    keep the first strict minimum; a NaN rotation that would have
+        //    improved the minimum raises a warning instead.
+        //  otherwise: every passing row is a hit, except that the template's
+        //    stream is cut at the first candidate whose distance from the
+        //    previous hit (or from the template start) is M+1.
+        const int M = P->max_candidates;
+        int cur_s = -1;
+        int64_t hits_in_s = 0;
+        size_t i = 0;
+        while (i < idx.size()) {
+            size_t j = i;
+            const HitRec &h0 = recs[idx[i]];
+            while (j < idx.size() && recs[idx[j]].s == h0.s && recs[idx[j]].t == h0.t) j++;
+            if (h0.s != cur_s) {
+                cur_s = h0.s;
+                hits_in_s = 0;
+            }
+            auto push_hit = [&](const HitRec &h) {
+                res->structure.push_back(h.s);
+                res->tpl.push_back(h.t);
+                res->ordinal.push_back(h.ordinal);
+                res->rmsd.push_back(h.rmsd);
+                res->rot.insert(res->rot.end(), h.rot, h.rot + 9);
+                res->centres.insert(res->centres.end(), h.centres, h.centres + 6);
+                int n = tp->atom_begin[h.t + 1] - tp->atom_begin[h.t];
+                res->atoms.insert(res->atoms.end(), rec_atoms.begin() + h.atom_at, rec_atoms.begin() + h.atom_at + n);
+                res->atom_offset.push_back((int64_t)res->atoms.size());
+                hits_in_s++;
+            };
+            if (P->best_match) {
+                double cur = INFINITY;
+                const HitRec *best = nullptr;
+                for (size_t q = i; q < j; q++) {
+                    const HitRec &h = recs[idx[q]];
+                    if (M >= 0 && h.ordinal > (int64_t)M + 1) break;
+                    if (h.rmsd < cur) {
+                        if (h.nan_rot) {
+                            res->warn_structure.push_back(h.s);
+                            res->warn_before.push_back(hits_in_s);
+                        } else {
+                            cur = h.rmsd;
+                            best = &h;
+                        }
+                    }
+                }
+                if (best) push_hit(*best);
+            } else {
+                int64_t base = 0;
+                for (size_t q = i; q < j; q++) {
+                    const HitRec &h = recs[idx[q]];
+                    if (M >= 0 && h.ordinal > base + M + 1) break;
+                    if (h.nan_rot) {
+                        res->warn_structure.push_back(h.s);
+                        res->warn_before.push_back(hits_in_s);
+                    } else {
+                        push_hit(h);
+                    }
+                    if (M >= 0 && h.ordinal == base + M + 1) break;
+                    if (!h.nan_rot) base = h.ordinal + 1;
+                }
+            }
+            i = j;
+        }
+    }
+    res->stats.pairs = (int64_t)counters[C_PAIRS];
+    res->stats.candidate_entries = (int64_t)counters[C_CAND];
+    res->stats.partials = (int64_t)counters[C_PARTIALS];
+    res->stats.complete = (int64_t)counters[C_COMPLETE];
+    res->stats.passing = (int64_t)recs.size();
+    res->stats.hits = (int64_t)res->rmsd.size();
+    res->stats.fp64_rechecks = (int64_t)counters[C_RECHECK];
+    res->stats.bytes_candidates = (int64_t)counters[C_BYTES_CAND];
+    res->stats.bytes_expansion = (int64_t)counters[C_BYTES_EXP];
+    {
+        int64_t hb = 0;
+        for (size_t q = 0; q < res->rmsd.size(); q++)
+            hb += 4 * (res->atom_offset[q + 1] - res->atom_offset[q]) + 8 + 72 + 48;
+        res->stats.bytes_superposition = hb;
+    }
+    res->stats.ms_candidates = ms_cand;
+    res->stats.ms_expansion = ms_exp;
+    res->stats.ms_superposition = ms_sup;
+    res->stats.ms_total = ms_total;
+    res->stats.launches = launches;
+    res->stats.chunks = chunks;
+
+done:
+    if (st) {
+        dfree(d_params, st); dfree(d_count, st); dfree(d_scanned, st); dfree(d_cand_atom, st);
+        dfree(d_leaf_atom, st); dfree(d_pair_counter, st); dfree(d_offset, st); dfree(d_totals, st);
+        dfree(d_cand_xyz, st); dfree(d_leaf_xyz, st); dfree(d_counters, st); dfree(d_ccount, st);
+        dfree(d_pcount, st); dfree(d_c_pair, st); dfree(d_c_atoms, st); dfree(d_p_pair, st);
+        dfree(d_p_nan, st); dfree(d_p_atoms, st); dfree(d_c_ord, st); dfree(d_p_row, st);
+        dfree(d_p_ord, st); dfree(d_p_rmsd, st); dfree(d_p_rot, st); dfree(d_p_cen, st);
+        for (auto &b : scan_tmp) dfree(b, st);
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
+    }
+    for (auto &e : ev)
+        if (e) cudaEventDestroy(e);
+    if (status != PJG_OK) {
+        delete res;
+        return status;
+    }
+    *out = res;
+    return PJG_OK;
+}
+
+extern "C" {
+
+int64_t pjg_results_count(const pjg_results *r) { return r ? (int64_t)r->rmsd.size() : 0; }
+
+int64_t pjg_results_atom_count(const pjg_results *r) { return r ? (int64_t)r->atoms.size() : 0; }
+
+pjg_status pjg_results_copy(const pjg_results *r, int32_t *structure, int32_t *template_index, int64_t *ordinal,
+                            double *rmsd, double *rotation, double *centres, int64_t *atom_offset, int32_t *atoms) {
+    if (!r) return fail(PJG_ERR_INVALID, "null results");
+    size_t n = r->rmsd.size();
+    if (structure) std::memcpy(structure, r->structure.data(), n * 4);
+    if (template_index) std::memcpy(template_index, r->tpl.data(), n * 4);
+    if (ordinal) std::memcpy(ordinal, r->ordinal.data(), n * 8);
+    if (rmsd) std::memcpy(rmsd, r->rmsd.data(), n * 8);
+    if (rotation) std::memcpy(rotation, r->rot.data(), n * 72);
+    if (centres) std::memcpy(centres, r->centres.data(), n * 48);
+    if (atom_offset) std::memcpy(atom_offset, r->atom_offset.data(), (n + 1) * 8);
+    if (atoms) std::memcpy(atoms, r->atoms.data(), r->atoms.size() * 4);
+    return PJG_OK;
+}
+
+int64_t pjg_results_warning_count(const pjg_results *r) { return r ? (int64_t)r->warn_structure.size() : 0; }
+
+pjg_status pjg_results_warnings(const pjg_results *r, int32_t *structure, int64_t *hits_before) {
+    if (!r) return fail(PJG_ERR_INVALID, "null results");
+    size_t n = r->warn_structure.size();
+    if (structure) std::memcpy(structure, r->warn_structure.data(), n * 4);
+    if (hits_before) std::memcpy(hits_before, r->warn_before.data(), n * 8);
+    return PJG_OK;
+}
+
+pjg_status pjg_results_stats(const pjg_results *r, pjg_stats *stats) {
+    if (!r || !stats) return fail(PJG_ERR_INVALID, "null argument");
+    *stats = r->stats;
+    return PJG_OK;
+}
+
+void pjg_results_destroy(pjg_results *r) { delete r; }
+
+}  // extern "C"

@@ -1,0 +1,1060 @@
+// pjg_kernels.cu — device kernels of libpjg (sm_103a).
+//
+// The search replaces Jess's per-pair Scanner (patches/Scanner.c.patch:
+// 110-336) + KdTree range queries (patches/KdTree.c.patch:226-298) +
+// superposition (patches/Super.c.patch) with:
+//
+//   k_params      annulus radii of every ordered template-atom pair
+//   k_candidates  candidate lists per (structure, signature), count + fill
+//   k_scan_*      exclusive scan of list lengths
+//   k_leaf_order  the kd-tree leaf order of each list (exact qselect replay)
+//   k_search      warp-per-pair, order-preserving frontier expansion
+//   k_superpose   warp-per-candidate FP64 quaternion superposition
+//
+// FP64 arithmetic that decides a hit is written with __dadd_rn/__dsub_rn/
+// __dmul_rn so it is never contracted into FMA and matches the reference's
+// (x86-64, unfused) operation order bit for bit.
+
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <climits>
+#include <cstdint>
+
+#include "pjg_common.cuh"
+#include "pjg_kernels.cuh"
+
+namespace pjg {
+
+#define FULL_MASK 0xffffffffu
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// ---------------------------------------------------------------------------
+// k_params: AnnulusParam for every ordered pair (p, q) of every template.
+// Scanner_next (patches/Scanner.c.patch:308-325): theta = (r + w_p) + w_q
+// clipped to s, min = d - theta, max = d + theta, min raised to 0.5;
+// Annulus_reuse (patches/Annulus.c.patch:107-139): swap if b < a, clamp at
+// 0, squares a*a and b*b, box half-width b.
+
+__global__ void k_params(int n_templates, const int32_t *atom_begin, const int32_t *param_begin,
+                         const double *dist, const double *weight, double r, double s, double g,
+                         AnnulusParam *out) {
+    int t = blockIdx.x;
+    if (t >= n_templates) return;
+    int a0 = atom_begin[t];
+    int n = atom_begin[t + 1] - a0;
+    int base = param_begin[t];
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+        int p = idx / n, q = idx % n;
+        double d = dist[base + idx];
+        double theta = __dadd_rn(__dadd_rn(r, weight[a0 + p]), weight[a0 + q]);
+        if (theta > s) theta = s;
+        double mn = __dsub_rn(d, theta);
+        double mx = __dadd_rn(d, theta);
+        if (mn < 0.5) mn = 0.5;
+        double a = mn, b = mx;
+        if (b < a) {
+            double tmp = a;
+            a = b;
+            b = tmp;
+        }
+        if (a < 0.0) a = 0.0;
+        if (b < 0.0) b = 0.0;
+        AnnulusParam P;
+        P.a2 = __dmul_rn(a, a);
+        P.b2 = __dmul_rn(b, b);
+        P.b = b;
+        double alo = a - g, ahi = a + g, blo = b - g, bhi = b + g;
+        P.thr.x = alo > 0.0 ? __double2float_rd(alo * alo) : -1.0f;
+        P.thr.y = __double2float_ru(ahi * ahi);
+        P.thr.z = blo > 0.0 ? __double2float_rd(blo * blo) : -1.0f;
+        P.thr.w = __double2float_ru(bhi * bhi);
+        P.pad = 0.0;
+        out[base + idx] = P;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Candidate rules.  TessTemplate_candidates (patches/TessTemplate.c.patch:
+// 173-233): codes -1..8 walk the residue buckets of the template atom's
+// residue names (first occurrence of each name only), in ResIndex order
+// (residue name, then serial); other codes scan the molecule in order.
+
+__device__ __forceinline__ bool in_list(uint32_t v, const uint32_t *list, int lo, int hi) {
+    for (int i = lo; i < hi; i++)
+        if (list[i] == v) return true;
+    return false;
+}
+
+// "_CA_", "_N__", "_O__" as little-endian u32
+__device__ __forceinline__ bool is_mainchain(uint32_t nm) {
+    return nm == 0x5F41435Fu || nm == 0x5F5F4E5Fu || nm == 0x5F5F4F5Fu;
+}
+
+__device__ __forceinline__ bool sig_match(const SigView &sv, int g, int rule, uint32_t name,
+                                          uint32_t resname) {
+    int n0 = sv.name_begin[g], n1 = sv.name_begin[g + 1];
+    switch (rule) {
+    case RULE_ANY:
+        return true;
+    case RULE_NAME:
+        return in_list(name, sv.names, n0, n1);
+    case RULE_NAME_OR_PARTNER: {
+        if (in_list(name, sv.names, n0, n1)) return true;
+        for (int i = sv.partner_begin[g]; i < sv.partner_begin[g + 1]; i++)
+            if (sv.partner_res[i] == resname && sv.partner_name[i] == name) return true;
+        return false;
+    }
+    case RULE_NAME_OR_MAINCHAIN:
+        if (in_list(name, sv.names, n0, n1)) return true;
+        return sv.mainchain[g] && is_mainchain(name);
+    case RULE_ELEMENT:
+        for (int i = n0; i < n1; i++)
+            if ((sv.names[i] & 0xFFFFu) == (name & 0xFFFFu)) return true;
+        return false;
+    }
+    return false;
+}
+
+// One warp per (structure, signature).  FILL=false: lengths and scanned
+// counts; FILL=true: write the list in candidate order.
+template <bool FILL>
+__global__ void k_candidates(ChunkView cv, SigView sv, int32_t *count, int32_t *scanned,
+                             const int64_t *offset, int32_t *cand_atom, float4 *cand_xyz) {
+    int lane = lane_id();
+    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    int64_t total = (int64_t)cv.n_structures * sv.n_sigs;
+    for (int64_t w = warp; w < total; w += nwarps) {
+        int s = (int)(w / sv.n_sigs);
+        int g = (int)(w % sv.n_sigs);
+        int code = sv.code[g];
+        int rule = sv.rule[g];
+        int64_t abase = cv.atom_base[s];
+        int nat = cv.atom_count[s];
+        int cnt = 0, sc = 0;
+        int64_t out0 = FILL ? offset[w] : 0;
+        auto visit = [&](int p_lo, int p_hi, bool via_sorted) {
+            for (int p0 = p_lo; p0 < p_hi; p0 += 32) {
+                int p = p0 + lane;
+                bool valid = p < p_hi;
+                bool ok = false;
+                int atom = 0;
+                if (valid) {
+                    atom = via_sorted ? cv.sorted[abase + p] : p;
+                    ok = sig_match(sv, g, rule, cv.name[abase + atom], cv.resname[abase + atom]);
+                }
+                unsigned m = __ballot_sync(FULL_MASK, ok);
+                if (FILL && ok) {
+                    int pos = cnt + __popc(m & ((1u << lane) - 1u));
+                    cand_atom[out0 + pos] = atom;
+                    cand_xyz[out0 + pos] = cv.xyz32[abase + atom];
+                }
+                cnt += __popc(m);
+                sc += min(32, p_hi - p0);
+            }
+        };
+        if (code >= -1 && code <= 8) {
+            int b0 = cv.bucket_begin[s], b1 = cv.bucket_begin[s + 1];
+            for (int ri = sv.res_begin[g]; ri < sv.res_begin[g + 1]; ri++) {
+                uint32_t rn = sv.resnames[ri];
+                int found = -1;
+                for (int bb = b0; bb < b1; bb += 32) {
+                    int b = bb + lane;
+                    unsigned m = __ballot_sync(FULL_MASK, b < b1 && cv.bucket_name[b] == rn);
+                    if (m) {
+                        found = bb + __ffs(m) - 1;
+                        break;
+                    }
+                }
+                if (found < 0) continue;
+                visit(cv.bucket_lo[found], cv.bucket_hi[found], true);
+            }
+        } else {
+            visit(0, nat, false);
+        }
+        if (!FILL && lane == 0) {
+            count[w] = cnt;
+            scanned[w] = sc;
+        }
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// Exclusive scan (int32 -> int64), three phases.
+
+constexpr int SCAN_THREADS = SCAN_TILE_THREADS;
+constexpr int SCAN_ITEMS = SCAN_TILE_ITEMS / SCAN_TILE_THREADS;
+constexpr int SCAN_TILE = SCAN_TILE_ITEMS;
+
+__device__ int64_t block_exclusive_scan(int64_t v, int64_t *total) {
+    __shared__ int64_t warp_sums[SCAN_THREADS / 32];
+    int lane = lane_id(), wid = threadIdx.x >> 5;
+    int64_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int64_t y = __shfl_up_sync(FULL_MASK, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int64_t ws = lane < SCAN_THREADS / 32 ? warp_sums[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            int64_t y = __shfl_up_sync(FULL_MASK, ws, o);
+            if (lane >= o) ws += y;
+        }
+        if (lane < SCAN_THREADS / 32) warp_sums[lane] = ws;
+    }
+    __syncthreads();
+    int64_t before = wid ? warp_sums[wid - 1] : 0;
+    *total = warp_sums[SCAN_THREADS / 32 - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+template <typename T>
+__global__ void k_scan_tiles(const T *in, int64_t n, int64_t *out, int64_t *tile_sums) {
+    int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    int64_t v[SCAN_ITEMS];
+    int64_t local = 0;
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        v[i] = base + i < n ? (int64_t)in[base + i] : 0;
+        local += v[i];
+    }
+    int64_t total;
+    int64_t ex = block_exclusive_scan(local, &total);
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        if (base + i < n) out[base + i] = ex;
+        ex += v[i];
+    }
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+
+__global__ void k_scan_add(int64_t *out, int64_t n, const int64_t *tile_offsets) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += tile_offsets[i / SCAN_TILE];
+}
+
+// ---------------------------------------------------------------------------
+// k_leaf_order: the order in which KdTreeQuery_next reports accepted leaves.
+//
+// KdTree_reuse / KdTreeNode_create (patches/KdTree.c.patch:157-205,
+// 348-456) split a node of n points at n/2 with qselect_r on the axis
+// x, y, z cycling, left child = first n/2 entries of the partitioned index
+// array.  qselect_r (patches/qselect.h.patch:52-119) is median-of-3 pivot +
+// Lomuto partition ("<= pivot" to the left), repeated until the pivot
+// lands on k.  The query pushes the left child, then the right one, so the
+// right subtree is popped first (pinned by the golden fixture): the DFS
+// leaf order is the partitioned index array read backwards.  Pruning only
+// removes subtrees, so accepted leaves always come out in this order.
+
+__device__ __forceinline__ int axis_cmp(double c, double d) { return c < d ? -1 : c > d ? 1 : 0; }
+
+struct KdSel {
+    const int32_t *atom;   // candidate-order atoms of the list
+    const double *xyz;     // structure FP64 coordinates
+    int axis;
+    __device__ double key(int pos) const { return xyz[3 * (int64_t)atom[pos] + axis]; }
+};
+
+__device__ int qs_partition(int32_t *base, int left, int right, int pivot, const KdSel &S) {
+    int store = left;
+    int32_t t = base[right];
+    base[right] = base[pivot];
+    base[pivot] = t;
+    double pv = S.key(base[right]);
+    for (int i = left; i < right; i++) {
+        if (axis_cmp(S.key(base[i]), pv) <= 0) {
+            int32_t u = base[i];
+            base[i] = base[store];
+            base[store] = u;
+            store++;
+        }
+    }
+    t = base[store];
+    base[store] = base[right];
+    base[right] = t;
+    return store;
+}
+
+__device__ int qs_median3(const int32_t *base, int left, int right, const KdSel &S) {
+    int mid = (left + right + 1) / 2;
+    double l = S.key(base[left]), r = S.key(base[right]), m = S.key(base[mid]);
+    if ((axis_cmp(l, m) > 0) != (axis_cmp(l, r) > 0)) return left;
+    if ((axis_cmp(m, l) < 0) != (axis_cmp(m, r) < 0)) return mid;
+    return right;
+}
+
+__device__ void qselect(int32_t *base, int n, int k, const KdSel &S) {
+    int left = 0, right = n - 1;
+    for (;;) {
+        if (left == right) return;
+        int p = qs_median3(base, left, right, S);
+        p = qs_partition(base, left, right, p, S);
+        if (p == k) return;
+        if (k < p) right = p - 1;
+        else left = p + 1;
+    }
+}
+
+__global__ void k_leaf_order(ChunkView cv, int32_t n_sigs, const int32_t *count, const int64_t *offset,
+                             const int32_t *cand_atom, const float4 *cand_xyz, int32_t *leaf_atom,
+                             float4 *leaf_xyz) {
+    int64_t total = (int64_t)cv.n_structures * n_sigs;
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < total;
+         w += (int64_t)gridDim.x * blockDim.x) {
+        int m = count[w];
+        if (m <= 0) continue;
+        int s = (int)(w / n_sigs);
+        int64_t o = offset[w];
+        const int32_t *ca = cand_atom + o;
+        int32_t *perm = leaf_atom + o;  // scratch: candidate positions
+        for (int i = 0; i < m; i++) perm[i] = i;
+        KdSel S{ca, cv.xyz64 + 3 * cv.atom_base[s], 0};
+        // explicit stack of (lo, n, axis); depth <= log2(m) + 2
+        int st_lo[40], st_n[40], st_ax[40];
+        int sp = 0;
+        st_lo[0] = 0;
+        st_n[0] = m;
+        st_ax[0] = 0;
+        sp = 1;
+        while (sp > 0) {
+            sp--;
+            int lo = st_lo[sp], n = st_n[sp], ax = st_ax[sp];
+            if (n <= 1) continue;
+            S.axis = ax;
+            int split = n / 2;
+            qselect(perm + lo, n, split, S);
+            int nx = (ax + 1) % 3;
+            st_lo[sp] = lo + split;
+            st_n[sp] = n - split;
+            st_ax[sp] = nx;
+            sp++;
+            st_lo[sp] = lo;
+            st_n[sp] = split;
+            st_ax[sp] = nx;
+            sp++;
+        }
+        // leaf rank r <-> partitioned position m-1-r
+        for (int r = 0; r < m; r++) leaf_xyz[o + r] = cand_xyz[o + perm[m - 1 - r]];
+        for (int r = 0; r < m / 2; r++) {
+            int32_t x = perm[r], y = perm[m - 1 - r];
+            perm[r] = ca[y];
+            perm[m - 1 - r] = ca[x];
+        }
+        if (m & 1) perm[m / 2] = ca[perm[m / 2]];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Search: warp per (structure, template) pair.
+//
+// The reference's Scanner_next is a depth-first backtracking over levels,
+// level l taking template atom order[l] (order = identity, or sorted by
+// candidate-list length when reorder is on, patches/Scanner.c.patch:97-108,
+// 179-195).  Its stream of complete assignments is ordered
+// lexicographically by (index in the level-0 list, kd leaf rank at level 1,
+// ..., kd leaf rank at level n-1).  Here each level keeps a tile of partial
+// assignments; a tile is expanded against the next level's list in
+// (parent, leaf rank) order with ballot + popc compaction, and a child
+// tile is fully processed before its parent tile continues (depth first
+// over tiles, breadth first inside a tile), which reproduces that order.
+
+struct PairState {
+    // per level
+    int64_t lvl_off[32];
+    int32_t lvl_cnt[32];
+    int32_t tkey[32];
+    int32_t order[32];
+    int32_t F[32];
+    int32_t cnt[32];
+    int32_t par[32];
+    int32_t cnd[32];
+    int32_t rowbase[32];
+};
+
+// Exact FP64 annulus test of the reference (_Annulus_po,
+// patches/Annulus.h.patch:54-68) plus the point-in-box test of the same
+// annulus (its kd query box, patches/Annulus.c.patch:133-137).
+__device__ __forceinline__ bool annulus64(const double *c, const double *x, const AnnulusParam &P,
+                                          bool *in_box) {
+    double sum = 0.0;
+    for (int i = 0; i < 3; i++) {
+        double t = __dsub_rn(c[i], x[i]);
+        sum = __dadd_rn(sum, __dmul_rn(t, t));
+    }
+    bool inside = !(sum < P.a2 || sum > P.b2);
+    bool ib = true;
+    for (int i = 0; i < 3; i++) {
+        if (x[i] < __dsub_rn(c[i], P.b) || x[i] > __dadd_rn(c[i], P.b)) ib = false;
+    }
+    *in_box = ib;
+    return inside;
+}
+
+// The kd query prunes an internal node whose bounding box misses the join
+// box B (intersection of the annulus boxes, Join_computeBox,
+// patches/Join.c.patch:154-190; _Box_ro, patches/Box.h.patch:68-79).  A
+// point inside every annulus box is never pruned; for a point that passes
+// the annulus tests but lies outside B (possible only within rounding of a
+// box face) walk the implicit tree to its leaf as the reference would.
+__device__ bool kd_path_reaches(const int32_t *leaf_atom, int m, int rank, const double *xyz,
+                                const double *Bmin, const double *Bmax) {
+    int q = m - 1 - rank;
+    int lo = 0, hi = m;
+    while (hi - lo > 1) {
+        double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int r = m - hi; r < m - lo; r++) {
+            const double *p = xyz + 3 * (int64_t)leaf_atom[r];
+            for (int i = 0; i < 3; i++) {
+                mn[i] = mn[i] < p[i] ? mn[i] : p[i];
+                mx[i] = mx[i] > p[i] ? mx[i] : p[i];
+            }
+        }
+        for (int i = 0; i < 3; i++)
+            if (mn[i] > Bmax[i] || Bmin[i] > mx[i]) return false;
+        int split = (hi - lo) / 2;
+        if (q < lo + split) hi = lo + split;
+        else lo = lo + split;
+    }
+    return true;
+}
+
+// TessTemplate_check (patches/TessTemplate.c.patch:101-155) for the newest
+// atom against one earlier level, on packed (resSeq << 8 | chainID2) keys.
+__device__ __forceinline__ bool check_pair(int32_t kj, int32_t kn, int32_t tj, int32_t tn, int ignore) {
+    bool same_chain = (kj & 0xFF) == (kn & 0xFF);
+    bool tsame_chain = (tj & 0xFF) == (tn & 0xFF);
+    if (ignore == 0) {
+        if (same_chain != tsame_chain) return false;
+        if (!same_chain) return true;
+    }
+    bool same_res = (kj >> 8) == (kn >> 8);
+    bool tsame_res = (tj >> 8) == (tn >> 8);
+    if (same_res != tsame_res) return false;
+    if (ignore != 2 && same_res && !same_chain) return false;
+    return true;
+}
+
+template <typename RowT, bool FP32>
+__global__ void __launch_bounds__(SEARCH_WARPS * 32)
+    k_search(ChunkView cv, TemplateView tv, CandView cd, SearchArgs sa, int32_t *pair_counter,
+             const int32_t *scanned, CompleteRows out, unsigned long long *counters) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = lane_id();
+    const int wib = threadIdx.x >> 5;
+    unsigned char *wbase = smem + (size_t)wib * sa.warp_smem;
+    PairState &st = *reinterpret_cast<PairState *>(wbase);
+    const size_t o2 = (sizeof(PairState) + 15) & ~size_t(15);
+    RowT *rows = reinterpret_cast<RowT *>(wbase + o2);
+    const int64_t row_units = (int64_t)(sa.warp_smem - o2) / (int64_t)sizeof(RowT);
+    const int T = tv.n_templates;
+    const int G = cd.n_sigs;
+    // wall-time budget: every warp stops taking work, and stops the pair it
+    // is on, once budget_ns have passed since it started (error code 3)
+    uint64_t t_start = 0;
+    if (lane == 0) t_start = global_ns();
+    bool timed_out = false;
+    uint32_t ticks = 0;
+    auto over_budget = [&]() -> bool {
+        if ((++ticks & 255u) != 0) return timed_out;
+        int over = 0;
+        if (lane == 0) over = (global_ns() - t_start) > sa.budget_ns;
+        over = __shfl_sync(FULL_MASK, over, 0);
+        if (over && !timed_out) {
+            timed_out = true;
+            if (lane == 0) atomicMax(&counters[C_ERROR], 3ull);
+        }
+        return timed_out;
+    };
+
+    for (;;) {
+        int pair = 0;
+        if (lane == 0) pair = atomicAdd(pair_counter, 1);
+        pair = __shfl_sync(FULL_MASK, pair, 0);
+        if (pair >= sa.n_pairs || timed_out) break;
+        const int s = pair / T;
+        const int t = pair % T;
+        const int ab = tv.atom_begin[t];
+        const int n = tv.atom_begin[t + 1] - ab;
+        if (n <= 0) continue;
+        const int64_t abase = cv.atom_base[s];
+        const double *xyz64 = cv.xyz64 + 3 * abase;
+
+        // ---- candidate-list lengths, empty-set skip, statistics
+        int k = lane;
+        int64_t lw = 0;
+        int c = INT_MAX, sc = 0;
+        if (k < n) {
+            lw = (int64_t)s * G + tv.sig[ab + k];
+            c = cd.count[lw];
+            sc = scanned[lw];
+        }
+        unsigned zero = __ballot_sync(FULL_MASK, k < n && c == 0);
+        int kstop = zero ? __ffs(zero) - 1 : n - 1;
+        {
+            int64_t bc = (k <= kstop && k < n) ? 8LL * sc + 16LL * c : 0;
+            int64_t cc = (k <= kstop && k < n) ? (int64_t)c : 0;
+            for (int o = 16; o; o >>= 1) {
+                bc += __shfl_xor_sync(FULL_MASK, bc, o);
+                cc += __shfl_xor_sync(FULL_MASK, cc, o);
+            }
+            if (lane == 0) {
+                atomicAdd(&counters[C_PAIRS], 1ull);
+                atomicAdd(&counters[C_BYTES_CAND], (unsigned long long)bc);
+                atomicAdd(&counters[C_CAND], (unsigned long long)cc);
+            }
+        }
+        if (zero) continue;
+        if (n > 32) {
+            if (lane == 0) atomicMax(&counters[C_ERROR], 1ull);
+            continue;
+        }
+
+        // ---- level order (stable by list length, ties by index)
+        int rank = k;
+        if (sa.reorder) {
+            rank = 0;
+            for (int j = 0; j < n; j++) {
+                int cj = __shfl_sync(FULL_MASK, c, j);
+                if (cj < c || (cj == c && j < k)) rank++;
+            }
+        }
+        if (k < n) st.order[rank] = k;
+        __syncwarp();
+        if (lane < n) {
+            int tk = st.order[lane];
+            int64_t w2 = (int64_t)s * G + tv.sig[ab + tk];
+            st.lvl_off[lane] = cd.offset[w2];
+            st.lvl_cnt[lane] = cd.count[w2];
+            st.tkey[lane] = tv.key[ab + tk];
+            st.F[lane] = 0;
+            st.cnt[lane] = 0;
+            st.par[lane] = 0;
+            st.cnd[lane] = 0;
+        }
+        // annulus parameters of template atoms (p, q): prm[p * n + q]
+        const AnnulusParam *prm = tv.params + tv.param_begin[t];
+        // tile capacity: equal row count for levels 0..n-2
+        int cap = 0;
+        if (n >= 2) {
+            int64_t units = (int64_t)(n - 1) * n / 2;
+            int64_t c2 = row_units / units;
+            cap = (int)(c2 > 4096 ? 4096 : c2);
+        }
+        if (lane < n) st.rowbase[lane] = cap * (lane * (lane + 1) / 2);
+        __syncwarp();
+        if (n >= 2 && cap < 1) {
+            if (lane == 0) atomicMax(&counters[C_ERROR], 2ull);
+            continue;
+        }
+
+        int64_t emitted = 0;
+        unsigned long long rechecks = 0;
+        const int m0 = st.lvl_cnt[0];
+        const int64_t off0 = st.lvl_off[0];
+
+        // emit complete rows: `pass` lanes with their level positions
+        auto emit = [&](bool pass, const RowT *prow, int lastpos) -> void {
+            unsigned m = __ballot_sync(FULL_MASK, pass);
+            if (!m) return;
+            int np = __popc(m);
+            int64_t base = 0;
+            if (lane == 0) base = (int64_t)atomicAdd(out.count, (unsigned long long)np);
+            base = __shfl_sync(FULL_MASK, base, 0);
+            if (pass) {
+                int rk = __popc(m & ((1u << lane) - 1u));
+                int64_t ri = base + rk;
+                if (ri < out.capacity) {
+                    int32_t *dst = out.atoms + ri * out.stride;
+                    for (int j = 0; j < n - 1; j++) {
+                        int pos = (int)prow[j];
+                        int32_t at = (j == 0) ? cd.cand_atom[off0 + pos] : cd.leaf_atom[st.lvl_off[j] + pos];
+                        dst[st.order[j]] = at;
+                    }
+                    int32_t at = (n == 1) ? cd.cand_atom[off0 + lastpos]
+                                          : cd.leaf_atom[st.lvl_off[n - 1] + lastpos];
+                    dst[st.order[n - 1]] = at;
+                    out.pair[ri] = pair;
+                    out.ordinal[ri] = emitted + rk;
+                }
+            }
+            emitted += np;
+        };
+
+        bool stop = false;
+        const int64_t stop_at = (sa.best_match && sa.max_candidates >= 0) ? (int64_t)sa.max_candidates + 2 : -1;
+
+        if (n == 1) {
+            // Scanner_next with one level advances the seed index before
+            // reporting (patches/Scanner.c.patch:244-263): seeds 1..m0-1
+            for (int b = 1; b < m0 && !stop; b += 32) {
+                int p = b + lane;
+                emit(p < m0, nullptr, p);
+                if (stop_at >= 0 && emitted >= stop_at) stop = true;
+                if (over_budget()) stop = true;
+            }
+            if (lane == 0) {
+                st.F[0] = m0;
+            }
+        } else {
+            int root = 0;
+            int lev = -1;
+            while (!stop) {
+                if (over_budget()) break;
+                if (lev < 0) {
+                    if (root >= m0) break;
+                    int kk = min(cap, m0 - root);
+                    RowT *r0 = rows + st.rowbase[0];
+                    for (int i = lane; i < kk; i += 32) r0[i] = (RowT)(root + i);
+                    root += kk;
+                    if (lane == 0) {
+                        st.F[0] += kk;
+                        st.cnt[0] = kk;
+                        st.par[0] = 0;
+                        st.cnd[0] = 0;
+                    }
+                    __syncwarp();
+                    lev = 0;
+                    continue;
+                }
+                const int pcnt = st.cnt[lev];
+                int ppar = st.par[lev];
+                if (ppar >= pcnt) {
+                    __syncwarp();
+                    if (lane == 0) st.cnt[lev] = 0;
+                    __syncwarp();
+                    lev--;
+                    continue;
+                }
+                const int child = lev + 1;
+                const int mc = st.lvl_cnt[child];
+                const bool last = (child == n - 1);
+                int ccnt = last ? 0 : st.cnt[child];
+                int batch = last ? 32 : min(32, cap - ccnt);
+                if (batch <= 0) {
+                    __syncwarp();
+                    if (lane == 0) {
+                        st.par[child] = 0;
+                        st.cnd[child] = 0;
+                    }
+                    __syncwarp();
+                    lev = child;
+                    continue;
+                }
+                // lane -> (parent p, candidate rank cr)
+                int pcnd = st.cnd[lev];
+                int tt = pcnd + lane;
+                int p = ppar + tt / mc;
+                int cr = tt % mc;
+                bool valid = lane < batch && p < pcnt;
+                bool pass = false;
+                const RowT *prow = rows + st.rowbase[lev] + (int64_t)p * (lev + 1);
+                if (valid) {
+                    const int64_t coff = st.lvl_off[child];
+                    float4 xc = cd.leaf_xyz[coff + cr];
+                    int32_t kn = __float_as_int(xc.w);
+                    int32_t tn = st.tkey[child];
+                    const int qn = st.order[child];
+                    pass = true;
+                    bool need_path = false;
+                    for (int j = 0; j <= lev && pass; j++) {
+                        int pos = (int)prow[j];
+                        float4 xj = (j == 0) ? cd.cand_xyz[off0 + pos] : cd.leaf_xyz[st.lvl_off[j] + pos];
+                        if (!check_pair(__float_as_int(xj.w), kn, st.tkey[j], tn, sa.ignore_chain)) {
+                            pass = false;
+                            break;
+                        }
+                        const AnnulusParam &PA = prm[st.order[j] * n + qn];
+                        bool exact = !FP32;
+                        if (FP32) {
+                            float dx = xj.x - xc.x, dy = xj.y - xc.y, dz = xj.z - xc.z;
+                            float d2 = dx * dx + dy * dy + dz * dz;
+                            float4 th = PA.thr;
+                            if (d2 < th.x || d2 > th.w) {
+                                pass = false;
+                                break;
+                            }
+                            if (!(d2 >= th.y && d2 <= th.z)) exact = true;
+                        }
+                        if (exact) {
+                            if (FP32) rechecks++;
+                            int32_t aj = (j == 0) ? cd.cand_atom[off0 + pos] : cd.leaf_atom[st.lvl_off[j] + pos];
+                            int32_t an = cd.leaf_atom[coff + cr];
+                            bool inb;
+                            if (!annulus64(xyz64 + 3 * (int64_t)aj, xyz64 + 3 * (int64_t)an, PA, &inb)) {
+                                pass = false;
+                                break;
+                            }
+                            if (!inb) need_path = true;
+                        }
+                    }
+                    if (pass && need_path) {
+                        double Bmin[3] = {-INFINITY, -INFINITY, -INFINITY};
+                        double Bmax[3] = {INFINITY, INFINITY, INFINITY};
+                        for (int j = 0; j <= lev; j++) {
+                            int pos = (int)prow[j];
+                            int32_t aj = (j == 0) ? cd.cand_atom[off0 + pos] : cd.leaf_atom[st.lvl_off[j] + pos];
+                            const double *cj = xyz64 + 3 * (int64_t)aj;
+                            double bj = prm[st.order[j] * n + qn].b;
+                            for (int i = 0; i < 3; i++) {
+                                double lo = __dsub_rn(cj[i], bj), hi = __dadd_rn(cj[i], bj);
+                                Bmin[i] = Bmin[i] > lo ? Bmin[i] : lo;
+                                Bmax[i] = Bmax[i] < hi ? Bmax[i] : hi;
+                            }
+                        }
+                        pass = kd_path_reaches(cd.leaf_atom + coff, mc, cr, xyz64, Bmin, Bmax);
+                    }
+                }
+                // advance the parent cursor by `batch` product positions
+                {
+                    int nt = pcnd + batch;
+                    int np2 = ppar + nt / mc;
+                    int nc2 = nt % mc;
+                    if (np2 >= pcnt) {
+                        np2 = pcnt;
+                        nc2 = 0;
+                    }
+                    __syncwarp();
+                    if (lane == 0) {
+                        st.par[lev] = np2;
+                        st.cnd[lev] = nc2;
+                    }
+                    ppar = np2;
+                }
+                if (last) {
+                    unsigned m = __ballot_sync(FULL_MASK, pass);
+                    emit(pass, prow, cr);
+                    __syncwarp();
+                    if (lane == 0) st.F[child] += __popc(m);
+                    if (stop_at >= 0 && emitted >= stop_at) stop = true;
+                    __syncwarp();
+                } else {
+                    unsigned m = __ballot_sync(FULL_MASK, pass);
+                    if (pass) {
+                        int ci = ccnt + __popc(m & ((1u << lane) - 1u));
+                        RowT *crow = rows + st.rowbase[child] + (int64_t)ci * (child + 1);
+                        for (int j = 0; j <= lev; j++) crow[j] = prow[j];
+                        crow[child] = (RowT)cr;
+                    }
+                    int ncnt = ccnt + __popc(m);
+                    __syncwarp();
+                    if (lane == 0) {
+                        st.cnt[child] = ncnt;
+                        st.F[child] += __popc(m);
+                    }
+                    __syncwarp();
+                    bool parent_done = ppar >= pcnt;
+                    if (ncnt > 0 && (cap - ncnt < min(32, cap) || parent_done)) {
+                        if (lane == 0) {
+                            st.par[child] = 0;
+                            st.cnd[child] = 0;
+                        }
+                        __syncwarp();
+                        lev = child;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        // ---- statistics of the pair
+        for (int o = 16; o; o >>= 1) rechecks += __shfl_xor_sync(FULL_MASK, rechecks, o);
+        if (lane == 0) {
+            int64_t partials = 0, bexp = 0;
+            for (int l = 0; l < n; l++) partials += st.F[l];
+            for (int l = 1; l < n; l++)
+                bexp += 4LL * l * st.F[l - 1] + (4LL * (l + 1) + 16) * st.F[l];
+            atomicAdd(&counters[C_PARTIALS], (unsigned long long)partials);
+            atomicAdd(&counters[C_COMPLETE], (unsigned long long)st.F[n - 1]);
+            atomicAdd(&counters[C_BYTES_EXP], (unsigned long long)bexp);
+            atomicAdd(&counters[C_RECHECK], rechecks);
+        }
+        __syncwarp();
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// Superposition: warp per complete assignment.  Lanes hold the atom pairs
+// (molecule atom, template atom) in template order, the warp reduces the
+// centroids, the squared norms and the 3x3 cross-covariance S in FP64, and
+// lane 0 solves the 4x4 quaternion eigenproblem: the largest root of the
+// characteristic polynomial of Horn's key matrix by Newton's method from
+// the upper bound (sumA + sumB)/2, the quaternion from the adjugate of
+// (K - lambda I).  rmsd = sqrt(max(sumA + sumB - 2 lambda, 0) / n) and R
+// maps molecule coordinates onto the template frame, as
+// Superposition_rmsd / Superposition_rotation do.
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
+    return v;
+}
+
+__device__ double det3(double a, double b, double c, double d, double e, double f, double g, double h,
+                       double i) {
+    return a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+}
+
+__device__ double det4(const double K[4][4]) {
+    double d = 0.0;
+    for (int c = 0; c < 4; c++) {
+        int c0 = c == 0 ? 1 : 0;
+        int c1 = c <= 1 ? 2 : 1;
+        int c2 = c <= 2 ? 3 : 2;
+        double minor = det3(K[1][c0], K[1][c1], K[1][c2], K[2][c0], K[2][c1], K[2][c2], K[3][c0],
+                            K[3][c1], K[3][c2]);
+        d += ((c & 1) ? -1.0 : 1.0) * K[0][c] * minor;
+    }
+    return d;
+}
+
+// 4x4 symmetric Jacobi: fallback eigenvector when the adjugate degenerates
+__device__ void jacobi4_top(double A[4][4], double v[4]) {
+    double V[4][4];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) V[i][j] = i == j ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 50; sweep++) {
+        double off = 0.0;
+        for (int p = 0; p < 4; p++)
+            for (int q = p + 1; q < 4; q++) off += fabs(A[p][q]);
+        if (off < 1e-15) break;
+        for (int p = 0; p < 3; p++)
+            for (int q = p + 1; q < 4; q++) {
+                if (A[p][q] == 0.0) continue;
+                double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+                double tt = 1.0 / (fabs(theta) + sqrt(theta * theta + 1.0));
+                if (theta < 0) tt = -tt;
+                double cc = 1.0 / sqrt(tt * tt + 1.0), ss = tt * cc;
+                for (int r = 0; r < 4; r++) {
+                    double arp = A[r][p], arq = A[r][q];
+                    A[r][p] = cc * arp - ss * arq;
+                    A[r][q] = ss * arp + cc * arq;
+                }
+                for (int r = 0; r < 4; r++) {
+                    double apr = A[p][r], aqr = A[q][r];
+                    A[p][r] = cc * apr - ss * aqr;
+                    A[q][r] = ss * apr + cc * aqr;
+                }
+                for (int r = 0; r < 4; r++) {
+                    double vrp = V[r][p], vrq = V[r][q];
+                    V[r][p] = cc * vrp - ss * vrq;
+                    V[r][q] = ss * vrp + cc * vrq;
+                }
+            }
+    }
+    int best = 0;
+    for (int i = 1; i < 4; i++)
+        if (A[i][i] > A[best][best]) best = i;
+    for (int i = 0; i < 4; i++) v[i] = V[i][best];
+}
+
+__device__ void quaternion_fit(const double S[9], double E0, int n, double *rmsd, double R[9], bool *bad) {
+    const double Sxx = S[0], Sxy = S[1], Sxz = S[2], Syx = S[3], Syy = S[4], Syz = S[5], Szx = S[6],
+                 Szy = S[7], Szz = S[8];
+    double K[4][4] = {{Sxx + Syy + Szz, Syz - Szy, Szx - Sxz, Sxy - Syx},
+                      {Syz - Szy, Sxx - Syy - Szz, Sxy + Syx, Szx + Sxz},
+                      {Szx - Sxz, Sxy + Syx, -Sxx + Syy - Szz, Syz + Szy},
+                      {Sxy - Syx, Szx + Sxz, Syz + Szy, -Sxx - Syy + Szz}};
+    double fro = 0.0;
+    for (int i = 0; i < 9; i++) fro += S[i] * S[i];
+    const double c2 = -2.0 * fro;
+    const double c1 = -8.0 * det3(Sxx, Sxy, Sxz, Syx, Syy, Syz, Szx, Szy, Szz);
+    const double c0 = det4(K);
+    double lam = E0;
+    for (int it = 0; it < 60; it++) {
+        double l2 = lam * lam;
+        double P = (l2 + c2) * l2 + c1 * lam + c0;
+        double dP = 4.0 * l2 * lam + 2.0 * c2 * lam + c1;
+        if (dP == 0.0) break;
+        double step = P / dP;
+        lam -= step;
+        if (fabs(step) <= 1e-14 * fabs(lam) + 1e-300) break;
+    }
+    double r2 = 2.0 * (E0 - lam) / (double)n;
+    *rmsd = sqrt(r2 > 0.0 ? r2 : 0.0);
+    // eigenvector: largest column of adj(K - lam I)
+    double A[4][4];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) A[i][j] = K[i][j] - (i == j ? lam : 0.0);
+    double best[4] = {0, 0, 0, 0}, bestn = -1.0;
+    for (int col = 0; col < 4; col++) {
+        double v[4];
+        for (int row = 0; row < 4; row++) {
+            // cofactor C[col][row] of A (adjugate column `col`)
+            int r0 = col == 0 ? 1 : 0, r1 = col <= 1 ? 2 : 1, r2i = col <= 2 ? 3 : 2;
+            int k0 = row == 0 ? 1 : 0, k1 = row <= 1 ? 2 : 1, k2 = row <= 2 ? 3 : 2;
+            double m = det3(A[r0][k0], A[r0][k1], A[r0][k2], A[r1][k0], A[r1][k1], A[r1][k2], A[r2i][k0],
+                            A[r2i][k1], A[r2i][k2]);
+            v[row] = ((row + col) & 1) ? -m : m;
+        }
+        double nn = v[0] * v[0] + v[1] * v[1] + v[2] * v[2] + v[3] * v[3];
+        if (nn > bestn) {
+            bestn = nn;
+            for (int i = 0; i < 4; i++) best[i] = v[i];
+        }
+    }
+    double scale = 0.0;
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) scale = fmax(scale, fabs(K[i][j]));
+    if (!(bestn > 1e-24 * scale * scale * scale * scale * scale * scale)) {
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) A[i][j] = K[i][j];
+        jacobi4_top(A, best);
+        bestn = best[0] * best[0] + best[1] * best[1] + best[2] * best[2] + best[3] * best[3];
+    }
+    double inv = 1.0 / sqrt(bestn);
+    double q0 = best[0] * inv, q1 = best[1] * inv, q2 = best[2] * inv, q3 = best[3] * inv;
+    R[0] = q0 * q0 + q1 * q1 - q2 * q2 - q3 * q3;
+    R[1] = 2.0 * (q1 * q2 - q0 * q3);
+    R[2] = 2.0 * (q1 * q3 + q0 * q2);
+    R[3] = 2.0 * (q1 * q2 + q0 * q3);
+    R[4] = q0 * q0 - q1 * q1 + q2 * q2 - q3 * q3;
+    R[5] = 2.0 * (q2 * q3 - q0 * q1);
+    R[6] = 2.0 * (q1 * q3 - q0 * q2);
+    R[7] = 2.0 * (q2 * q3 + q0 * q1);
+    R[8] = q0 * q0 - q1 * q1 - q2 * q2 + q3 * q3;
+    // the reference's rotation formula divides by the singular values of the
+    // covariance and is undefined for fewer than three atom pairs
+    *bad = n < 3;
+}
+
+__global__ void k_superpose(ChunkView cv, TemplateView tv, SuperArgs sa, CompleteRows in, PassRows out,
+                            unsigned long long *counters) {
+    int lane = lane_id();
+    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    int64_t nrows = *in.count;
+    if (nrows > in.capacity) nrows = in.capacity;
+    const int T = tv.n_templates;
+    for (int64_t i = warp; i < nrows; i += nwarps) {
+        int pair = in.pair[i];
+        int s = pair / T, t = pair % T;
+        int ab = tv.atom_begin[t];
+        int n = tv.atom_begin[t + 1] - ab;
+        const double *xyz = cv.xyz64 + 3 * cv.atom_base[s];
+        double a[3] = {0, 0, 0}, b[3] = {0, 0, 0};
+        int32_t atom = 0;
+        if (lane < n) {
+            atom = in.atoms[i * in.stride + lane];
+            for (int d = 0; d < 3; d++) {
+                a[d] = xyz[3 * (int64_t)atom + d];
+                b[d] = tv.pos[3 * (ab + lane) + d];
+            }
+        }
+        double ca[3], cb[3];
+        for (int d = 0; d < 3; d++) {
+            ca[d] = warp_sum(a[d]) / (double)n;
+            cb[d] = warp_sum(b[d]) / (double)n;
+        }
+        double ac[3] = {0, 0, 0}, bc[3] = {0, 0, 0};
+        if (lane < n)
+            for (int d = 0; d < 3; d++) {
+                ac[d] = a[d] - ca[d];
+                bc[d] = b[d] - cb[d];
+            }
+        double sumA = warp_sum(ac[0] * ac[0] + ac[1] * ac[1] + ac[2] * ac[2]);
+        double sumB = warp_sum(bc[0] * bc[0] + bc[1] * bc[1] + bc[2] * bc[2]);
+        double S[9];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) S[3 * r + c] = warp_sum(ac[r] * bc[c]);
+        double rmsd = 0.0, R[9];
+        bool bad = false;
+        if (lane == 0) quaternion_fit(S, 0.5 * (sumA + sumB), n, &rmsd, R, &bad);
+        rmsd = __shfl_sync(FULL_MASK, rmsd, 0);
+        if (rmsd <= sa.rmsd_threshold) {
+            int64_t j = 0;
+            if (lane == 0) j = (int64_t)atomicAdd(out.count, 1ull);
+            j = __shfl_sync(FULL_MASK, j, 0);
+            if (j < out.capacity) {
+                if (lane == 0) {
+                    out.row[j] = i;
+                    out.pair[j] = pair;
+                    out.ordinal[j] = in.ordinal[i];
+                    out.rmsd[j] = rmsd;
+                    out.nan_rot[j] = bad ? 1 : 0;
+                    for (int q = 0; q < 9; q++) out.rot[9 * j + q] = R[q];
+                    for (int d = 0; d < 3; d++) {
+                        out.centres[6 * j + d] = ca[d];
+                        out.centres[6 * j + 3 + d] = cb[d];
+                    }
+                }
+                if (lane < n) out.atoms[j * out.stride + lane] = atom;
+            } else if (lane == 0) {
+                atomicAdd(&counters[C_PASS_OVERFLOW], 1ull);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+
+void launch_params(cudaStream_t st, int n_templates, const int32_t *atom_begin, const int32_t *param_begin,
+                   const double *dist, const double *weight, double r, double s, double g, AnnulusParam *out) {
+    if (n_templates > 0) k_params<<<n_templates, 256, 0, st>>>(n_templates, atom_begin, param_begin, dist, weight, r, s, g, out);
+}
+
+void launch_candidates(cudaStream_t st, int blocks, bool fill, const ChunkView &cv, const SigView &sv,
+                       int32_t *count, int32_t *scanned, const int64_t *offset, int32_t *cand_atom,
+                       float4 *cand_xyz) {
+    if (fill) k_candidates<true><<<blocks, 256, 0, st>>>(cv, sv, count, scanned, offset, cand_atom, cand_xyz);
+    else k_candidates<false><<<blocks, 256, 0, st>>>(cv, sv, count, scanned, offset, cand_atom, cand_xyz);
+}
+
+void launch_scan_tiles_i32(cudaStream_t st, const int32_t *in, int64_t n, int64_t *out, int64_t *tile_sums) {
+    int64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    k_scan_tiles<int32_t><<<(unsigned)tiles, SCAN_THREADS, 0, st>>>(in, n, out, tile_sums);
+}
+
+void launch_scan_tiles_i64(cudaStream_t st, const int64_t *in, int64_t n, int64_t *out, int64_t *tile_sums) {
+    int64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    k_scan_tiles<int64_t><<<(unsigned)tiles, SCAN_THREADS, 0, st>>>(in, n, out, tile_sums);
+}
+
+void launch_scan_add(cudaStream_t st, int64_t *out, int64_t n, const int64_t *tile_offsets) {
+    k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, n, tile_offsets);
+}
+
+void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t n_sigs, const int32_t *count,
+                       const int64_t *offset, const int32_t *cand_atom, const float4 *cand_xyz,
+                       int32_t *leaf_atom, float4 *leaf_xyz) {
+    k_leaf_order<<<blocks, 128, 0, st>>>(cv, n_sigs, count, offset, cand_atom, cand_xyz, leaf_atom, leaf_xyz);
+}
+
+template <typename RowT, bool FP32>
+static cudaError_t search_variant(cudaStream_t st, int grid, const ChunkView &cv, const TemplateView &tv,
+                                  const CandView &cd, const SearchArgs &sa, int32_t *pair_counter,
+                                  const int32_t *scanned, const CompleteRows &out, unsigned long long *counters) {
+    size_t smem = (size_t)sa.warp_smem * SEARCH_WARPS;
+    cudaError_t e = cudaFuncSetAttribute(k_search<RowT, FP32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_search<RowT, FP32><<<grid, SEARCH_WARPS * 32, smem, st>>>(cv, tv, cd, sa, pair_counter, scanned, out, counters);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_search(cudaStream_t st, int grid, bool wide, bool fp32, const ChunkView &cv,
+                          const TemplateView &tv, const CandView &cd, const SearchArgs &sa, int32_t *pair_counter,
+                          const int32_t *scanned, const CompleteRows &out, unsigned long long *counters) {
+    if (wide)
+        return fp32 ? search_variant<uint32_t, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters)
+                    : search_variant<uint32_t, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters);
+    return fp32 ? search_variant<uint16_t, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters)
+                : search_variant<uint16_t, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters);
+}
+
+void launch_superpose(cudaStream_t st, int blocks, const ChunkView &cv, const TemplateView &tv,
+                      const SuperArgs &sa, const CompleteRows &in, const PassRows &out,
+                      unsigned long long *counters) {
+    k_superpose<<<blocks, 256, 0, st>>>(cv, tv, sa, in, out, counters);
+}
+
+}  // namespace pjg

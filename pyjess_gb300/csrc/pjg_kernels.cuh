@@ -1,0 +1,83 @@
+// pjg_kernels.cuh — kernel declarations and launch argument blocks.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "pjg_common.cuh"
+
+namespace pjg {
+
+constexpr int SEARCH_WARPS = 4;        // warps per block of k_search
+
+struct SearchArgs {
+    int32_t n_pairs;                   // chunk structures x templates
+    int32_t ignore_chain;
+    int32_t reorder;
+    int32_t best_match;
+    int32_t max_candidates;
+    int32_t warp_smem;                 // bytes of shared memory per warp
+    uint64_t budget_ns;                // per-warp wall-time budget (globaltimer)
+};
+
+struct SuperArgs {
+    double rmsd_threshold;
+};
+
+// Complete assignments written by k_search.
+struct CompleteRows {
+    unsigned long long *count;
+    int64_t capacity;
+    int32_t stride;                    // >= max template atoms
+    int32_t *pair;                     // chunk-local pair = s * T + t
+    int64_t *ordinal;                  // position in the pair's stream
+    int32_t *atoms;                    // [capacity * stride], template order
+};
+
+// Complete assignments with rmsd <= threshold, written by k_superpose.
+struct PassRows {
+    unsigned long long *count;
+    int64_t capacity;
+    int32_t stride;
+    int64_t *row;
+    int32_t *pair;
+    int64_t *ordinal;
+    double *rmsd;
+    int32_t *nan_rot;
+    double *rot;                       // [9 * capacity]
+    double *centres;                   // [6 * capacity]
+    int32_t *atoms;                    // [capacity * stride]
+};
+
+// Host-side launchers (the kernels themselves live in pjg_kernels.cu).
+
+void launch_params(cudaStream_t st, int n_templates, const int32_t *atom_begin, const int32_t *param_begin,
+                   const double *dist, const double *weight, double r, double s, double g, AnnulusParam *out);
+
+void launch_candidates(cudaStream_t st, int blocks, bool fill, const ChunkView &cv, const SigView &sv,
+                       int32_t *count, int32_t *scanned, const int64_t *offset, int32_t *cand_atom,
+                       float4 *cand_xyz);
+
+// exclusive scan of one tile (SCAN_TILE entries) per block
+constexpr int SCAN_TILE_THREADS = 512;
+constexpr int SCAN_TILE_ITEMS = 2048;
+void launch_scan_tiles_i32(cudaStream_t st, const int32_t *in, int64_t n, int64_t *out, int64_t *tile_sums);
+void launch_scan_tiles_i64(cudaStream_t st, const int64_t *in, int64_t n, int64_t *out, int64_t *tile_sums);
+void launch_scan_add(cudaStream_t st, int64_t *out, int64_t n, const int64_t *tile_offsets);
+
+void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t n_sigs, const int32_t *count,
+                       const int64_t *offset, const int32_t *cand_atom, const float4 *cand_xyz,
+                       int32_t *leaf_atom, float4 *leaf_xyz);
+
+// k_search variant: wide = 32-bit frontier entries (structures above 65535
+// atoms), fp32 = guarded FP32 distance tests (else exact FP64 throughout)
+cudaError_t launch_search(cudaStream_t st, int grid, bool wide, bool fp32, const ChunkView &cv,
+                          const TemplateView &tv, const CandView &cd, const SearchArgs &sa, int32_t *pair_counter,
+                          const int32_t *scanned, const CompleteRows &out, unsigned long long *counters);
+
+void launch_superpose(cudaStream_t st, int blocks, const ChunkView &cv, const TemplateView &tv,
+                      const SuperArgs &sa, const CompleteRows &in, const PassRows &out,
+                      unsigned long long *counters);
+
+}  // namespace pjg

@@ -1,0 +1,238 @@
+"""GPU parity: libpjg against the CPU oracle and the reference's golden vectors.
+
+Bar: the ordered hit list of every structure is identical (template,
+stream ordinal and every matched atom, in the reference's order); RMSD within
+RMSD_TOL of the FP64 oracle; rotations within ROT_TOL; the search counters
+(pairs, partial assignments, complete assignments, algorithmic bytes) equal
+the oracle's instrumented counts.
+"""
+
+import numpy as np
+import pytest
+
+from helpers import hit_keys, parse_block
+
+pytestmark = pytest.mark.gpu
+
+RMSD_TOL = 1e-9    # Angstrom, GPU quaternion solver vs oracle Jacobi (FP64)
+ROT_TOL = 1e-7
+
+MODES = ("fp32", "fp64", "plain")
+
+
+def gpu_query(ptemplates, pstructures, mode="fp32", **kw):
+    from pyjess_gb300 import _native
+    from pyjess_gb300._abi import QueryParams
+
+    P = QueryParams(
+        rmsd_threshold=kw["rmsd_threshold"], distance_cutoff=kw["distance_cutoff"],
+        max_dynamic_distance=kw["max_dynamic_distance"],
+        max_candidates=-1 if kw.get("max_candidates") is None else kw["max_candidates"],
+        ignore_chain=kw.get("ignore_chain", 0), best_match=int(kw.get("best_match", False)),
+        reorder=int(kw.get("reorder", True)),
+        mode={"fp32": _native.MODE_BATCHED_FP32, "fp64": _native.MODE_BATCHED_FP64,
+              "plain": _native.MODE_PLAIN_FP64}[mode])
+    res = _native.query(_native.Templates(ptemplates), _native.Structures(pstructures), P)
+    return res
+
+
+def compare(ptemplates, pstructures, mode="fp32", check_stats=True, **kw):
+    from oracle import oracle
+
+    ref = oracle.query(ptemplates, pstructures, threads=8, **kw)
+    res = gpu_query(ptemplates, pstructures, mode=mode, **kw)
+    g = res.arrays()
+    r = ref["hits"]
+    assert hit_keys(g) == hit_keys(r)
+    if r["count"]:
+        err = np.abs(g["rmsd"] - r["rmsd"]).max()
+        assert err <= RMSD_TOL, err
+        assert np.abs(g["rotation"] - r["rotation"]).max() <= ROT_TOL
+        assert np.abs(g["centres"] - r["centres"]).max() <= 1e-9
+    gw = res.warnings()
+    assert list(gw[0]) == list(ref["warnings"][0]) and list(gw[1]) == list(ref["warnings"][1])
+    if check_stats and kw.get("max_candidates") is None:
+        gs, os_ = res.stats(), ref["stats"]
+        for key in ("pairs", "candidate_entries", "partials", "complete", "bytes_candidates",
+                    "bytes_expansion"):
+            assert gs[key] == os_[key], (key, gs[key], os_[key])
+    return res, ref
+
+
+# --- reference golden vectors through the public API -------------------------
+
+
+@pytest.mark.parametrize("reorder", [False, True])
+def test_golden_1amy(t133, amy, golden_blocks, reorder):
+    from pyjess_gb300 import Jess
+
+    jess = Jess([t133])
+    hits = list(jess.query(amy, 2, 4, 4, reorder=reorder))
+    assert len(hits) == 156
+    serials = [tuple(a.serial for a in h.atoms(False)) for h in hits]
+    golden = [tuple(int(l[6:11]) for l in b.strip().splitlines()[1:-1]) for b in golden_blocks]
+    if not reorder:
+        assert serials == golden
+    else:
+        assert sorted(serials) == sorted(golden)
+    by = dict(zip(golden, golden_blocks))
+    for hit, key in zip(hits, serials):
+        _, rmsd, det, loge, lines = parse_block(by[key])
+        assert hit.rmsd == pytest.approx(rmsd, abs=5e-4)
+        assert hit.determinant == pytest.approx(det, abs=0.05)
+        assert hit.log_evalue == pytest.approx(loge, abs=0.0051)
+        for atom, line in zip(hit.atoms(), lines):
+            assert atom.x == pytest.approx(float(line[31:39]), abs=5e-4)
+            assert atom.y == pytest.approx(float(line[39:47]), abs=5e-4)
+            assert atom.z == pytest.approx(float(line[47:55]), abs=5e-4)
+
+
+def test_golden_doctest(t133, t412, amy):
+    from test_oracle_golden import DOCTEST_DUMP, DOCTEST_RMSD
+    from pyjess_gb300 import Jess
+
+    jess = Jess([t133, t412])
+    hits = list(jess.query(amy, 2, 2, 2))
+    assert [h.template().id for h in hits] == ["2om2"] * 13
+    for hit, prefix in zip(hits, DOCTEST_RMSD):
+        assert repr(hit.rmsd)[:6] == prefix[:6] or abs(hit.rmsd - float(prefix)) < 1e-4
+    assert hits[0].dumps() == DOCTEST_DUMP
+    best = list(jess.query(amy, 2, 2, 2, best_match=True))
+    assert len(best) == 1 and round(best[0].rmsd, 3) == 1.071
+
+
+@pytest.mark.parametrize("ignore,expected", [(None, 0), ("residues", 2), ("atoms", 7)])
+def test_golden_ignore_chain(t412, ayx, ignore, expected):
+    from pyjess_gb300 import Jess
+
+    assert len(list(Jess([t412]).query(ayx, 3, 3, 3, ignore_chain=ignore))) == expected
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("reorder", [False, True])
+def test_golden_vs_oracle_all_modes(t133, t412, amy, mode, reorder):
+    from pyjess_gb300 import Jess
+    from pyjess_gb300._pack import pack_molecules
+
+    jess = Jess([t133, t412, t133])
+    compare(jess._packed_templates(), pack_molecules([amy]), mode=mode, rmsd_threshold=2,
+            distance_cutoff=4, max_dynamic_distance=4, reorder=reorder)
+
+
+@pytest.mark.parametrize("mc", [0, 1, 3, 10])
+@pytest.mark.parametrize("best", [False, True])
+def test_automaton_max_candidates(t133, t412, amy, mc, best):
+    from pyjess_gb300 import Jess
+    from pyjess_gb300._pack import pack_molecules
+
+    jess = Jess([t133, t412, t133])
+    compare(jess._packed_templates(), pack_molecules([amy]), rmsd_threshold=2, distance_cutoff=4,
+            max_dynamic_distance=4, max_candidates=mc, best_match=best)
+
+
+# --- synthetic workloads --------------------------------------------------------
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_config0(mode):
+    from pyjess_gb300 import workloads as W
+
+    wl = W.config(0)
+    compare(wl.templates, wl.structures, mode=mode, **wl.params)
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_config1_bit_exact_order(mode):
+    from pyjess_gb300 import workloads as W
+
+    wl = W.config(1)
+    res, ref = compare(wl.templates, wl.structures, mode=mode, **wl.params)
+    assert ref["hits"]["count"] > 100
+
+
+@pytest.mark.parametrize("index", [2, 3])
+@pytest.mark.parametrize("mode", ["fp32", "fp64"])
+def test_config_batched_reduced(index, mode):
+    from pyjess_gb300 import workloads as W
+
+    wl = W.config(index, n_structures=40, n_templates=300)
+    compare(wl.templates, wl.structures, mode=mode, **wl.params)
+
+
+def test_config3_adversarial_guard_band():
+    """Structures whose atoms sit within 1e-6 A of annulus boundaries: the
+    FP32 filter must send them to the FP64 recheck and decide as the oracle."""
+    from pyjess_gb300 import workloads as W
+
+    wl = W.config(3, n_structures=20, n_templates=200)
+    res, ref = compare(wl.templates, wl.structures, mode="fp32", **wl.params)
+    assert res.stats()["fp64_rechecks"] > 0
+
+
+@pytest.mark.parametrize("best", [False, True])
+def test_config4_dense_reduced(best):
+    from pyjess_gb300 import workloads as W
+
+    wl = W.config(4, n_structures=3, n_templates=6)
+    p = dict(wl.params)
+    p["max_candidates"] = 50
+    compare(wl.templates, wl.structures, best_match=best, **p)
+
+
+@pytest.mark.parametrize("ignore", [0, 1, 2])
+def test_ignore_chain_synthetic(ignore):
+    from pyjess_gb300 import workloads as W
+
+    wl = W.config(2, n_structures=10, n_templates=100)
+    compare(wl.templates, wl.structures, ignore_chain=ignore, **wl.params)
+
+
+# --- edge cases -------------------------------------------------------------------
+
+
+def test_empty_inputs(t133):
+    from pyjess_gb300 import Jess, Molecule
+
+    assert list(Jess().query(Molecule(), 2, 2, 4)) == []
+    assert list(Jess([t133]).query(Molecule(), 2, 2, 4)) == []
+
+
+def test_single_atom_and_tiny_templates(amy):
+    """One-atom templates: the scanner skips the first seed and every
+    superposition is degenerate (NaN rotation), so only warnings come out."""
+    from pyjess_gb300 import Jess, Template, TemplateAtom
+    from pyjess_gb300._pack import pack_molecules
+
+    one = Template([TemplateAtom(chain_id="A", residue_number=1, x=0, y=0, z=0, residue_names=["SER"],
+                                 atom_names=["OG"], match_mode=0)], id="one")
+    jess = Jess([one])
+    res, ref = compare(jess._packed_templates(), pack_molecules([amy[:400]]), rmsd_threshold=2,
+                       distance_cutoff=2, max_dynamic_distance=2, check_stats=False)
+    assert res.arrays()["count"] == 0
+    assert len(res.warnings()[0]) == len(ref["warnings"][0]) > 0
+    with pytest.warns(UserWarning):
+        assert list(jess.query(amy[:400], 2, 2, 2)) == []
+
+
+def test_no_candidates_skips_template(t133, amy):
+    from pyjess_gb300 import Jess, Template, TemplateAtom
+    from pyjess_gb300._pack import pack_molecules
+
+    ghost = Template([TemplateAtom(chain_id="A", residue_number=1, x=0, y=0, z=0, residue_names=["XYZ"],
+                                   atom_names=["QQ"], match_mode=0)] * 3, id="ghost")
+    jess = Jess([t133, ghost])
+    compare(jess._packed_templates(), pack_molecules([amy]), rmsd_threshold=2, distance_cutoff=4,
+            max_dynamic_distance=4)
+
+
+def test_query_many_matches_query(t133, t412, amy, ayx):
+    from pyjess_gb300 import Jess
+
+    jess = Jess([t133, t412])
+    mols = [amy, ayx, amy[:1000]]
+    many = jess.query_many(mols, 2, 3, 3)
+    for mol, hits in zip(mols, many):
+        single = list(jess.query(mol, 2, 3, 3))
+        assert [tuple(a.serial for a in h.atoms(False)) for h in hits] == \
+               [tuple(a.serial for a in h.atoms(False)) for h in single]
+        assert [h.rmsd for h in hits] == [h.rmsd for h in single]
