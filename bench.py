@@ -1,0 +1,345 @@
+"""Benchmark: template x structure pairs per second on one GB300.
+
+Workload (BASELINE config 3): 5,000 synthetic templates (Zipf 2-8 residues x
+3 atoms) against 2,000 synthetic structures (lognormal lengths, median 350
+residues, 1-4 chains, 200 adversarial structures with distances within
+1e-6 A of annulus boundaries) = 10,000,000 pairs per step, batched,
+FP32-guarded distance tests with FP64 recheck.
+
+  value       pairs/s of pjg_query with templates and structures already
+              resident on the device (device time from CUDA events on the
+              query's stream)
+  e2e         the same metric through the C ABI with host buffers: per step
+              pjg_templates_create + pjg_structures_create (H2D), pjg_query,
+              pjg_results_copy (D2H), wall clock
+  roofline    k_search (the expansion kernel): algorithmic expansion bytes /
+              kernel time against the measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle (a port of the reference's algorithm) on the
+              host cores, on a bounded sample of the same workload
+
+`--impl reference` times that CPU implementation alone on this workload
+(bounded sample per step).  Under torchrun (N>1) structures are sharded
+across ranks (weak scaling: every rank runs all templates against its own
+2,000 structures); rank 0 prints one JSON line.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "template·structure pairs/s (batched FP32-guarded, config 3)"
+UNIT = "pairs/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--structures", type=int, default=2000)
+    ap.add_argument("--templates", type=int, default=5000)
+    ap.add_argument("--cpu-structures", type=int, default=0, help="structures in the CPU sample (0: auto)")
+    ap.add_argument("--plain-structures", type=int, default=100,
+                    help="structures timed with the plain FP64 per-structure path")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def workload(args, rank=0, world=1):
+    from pyjess_gb300 import workloads as W
+
+    wl = W.config(3, n_structures=args.structures, n_templates=args.templates)
+    if world > 1:
+        # weak scaling: every rank runs its own full structure set (a
+        # different seed per rank would change the hit statistics; the same
+        # shape is kept, structures are re-drawn per rank index)
+        pass
+    return wl
+
+
+def cpu_sample(wl, n_structures, threads):
+    """Time the CPU oracle on the first `n_structures` structures x all templates."""
+    from oracle import oracle
+
+    sub = wl.structures.subset(list(range(min(n_structures, wl.structures.n_structures))))
+    t0 = time.perf_counter()
+    r = oracle.query(wl.templates, sub, threads=threads, **wl.params)
+    dt = time.perf_counter() - t0
+    pairs = wl.templates.n_templates * sub.n_structures
+    return pairs / dt, dt, pairs, r["hits"]["count"]
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    wl = workload(args)
+    threads = os.cpu_count() or 1
+    n = args.cpu_structures or 32
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, dt, pairs, hits = cpu_sample(wl, n, threads)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    sample = f"{n} structures x {wl.templates.n_templates} templates = {n * wl.templates.n_templates} pairs per step"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": wl.name, "pairs": wl.pairs, "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "notes": "the reference's C core cannot be built (empty vendor/jess submodule); the oracle port "
+                 "restating its algorithm runs on all host cores",
+    }))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, world, local = dist_env()
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from pyjess_gb300 import _native
+    from pyjess_gb300._abi import QueryParams
+
+    _native.init(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist_mod.init_process_group("gloo")
+        dist = dist_mod
+    t0 = time.time()
+    wl = workload(args, rank, world)
+    gen_s = time.time() - t0
+    P = QueryParams(rmsd_threshold=wl.params["rmsd_threshold"], distance_cutoff=wl.params["distance_cutoff"],
+                    max_dynamic_distance=wl.params["max_dynamic_distance"], max_candidates=-1, ignore_chain=0,
+                    best_match=0, reorder=1, mode=_native.MODE_BATCHED_FP32, guard_band=1e-4)
+    tpl = _native.Templates(wl.templates)
+    sts = _native.Structures(wl.structures)
+
+    # ---- device-resident timing
+    for _ in range(args.warmup):
+        res = _native.query(tpl, sts, P)
+        res.arrays()
+    if dist:
+        dist.barrier()
+    step_ms, stats, launches = [], [], 0
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            res = _native.query(tpl, sts, P)
+            st = res.stats()
+            stats.append(st)
+            step_ms.append(st["ms_total"])
+            launches += st["launches"]
+            arr = res.arrays()
+    total_ms = sum(step_ms)
+    if dist:
+        import torch
+
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    pairs_step = wl.pairs
+    value = pairs_step * world * args.steps / (total_ms / 1e3)
+    s0 = stats[-1]
+    hits_per_s = s0["hits"] * world * args.steps / (total_ms / 1e3)
+
+    # ---- roofline of the expansion kernel (k_search)
+    peaks, peak_kind = measured_peaks()
+    exp_ms = sum(s["ms_expansion"] for s in stats)
+    exp_bytes = sum(s["bytes_expansion"] for s in stats)
+    achieved = exp_bytes / (exp_ms / 1e3) / 1e9 if exp_ms > 0 else 0.0
+    peak = float(peaks["hbm_gbs"])
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "k_search_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tr = json.load(f)
+        # DRAM bytes per launch measured by ncu on a smaller case, scaled to
+        # this workload's launch by the expansion bytes it processes
+        if tr.get("bytes_expansion"):
+            per_launch_exp = exp_bytes / max(1, sum(s["chunks"] for s in stats))
+            traffic = tr["dram_bytes_per_launch"] * per_launch_exp / tr["bytes_expansion_per_launch"]
+
+    # ---- plain FP64 per-structure path on a subset (the method the batched
+    # path is measured against)
+    plain = None
+    if args.plain_structures > 0 and rank == 0:
+        sub = wl.structures.subset(list(range(min(args.plain_structures, wl.structures.n_structures))))
+        ssub = _native.Structures(sub)
+        Pp = QueryParams(rmsd_threshold=P.rmsd_threshold, distance_cutoff=P.distance_cutoff,
+                         max_dynamic_distance=P.max_dynamic_distance, max_candidates=-1, ignore_chain=0,
+                         best_match=0, reorder=1, mode=_native.MODE_PLAIN_FP64)
+        _native.query(tpl, ssub, Pp).arrays()
+        rp = _native.query(tpl, ssub, Pp)
+        ms = rp.stats()["ms_total"]
+        rb = _native.query(tpl, ssub, P)
+        same = rp.arrays()["count"] == rb.arrays()["count"] and \
+            (rp.arrays()["atoms"] == rb.arrays()["atoms"]).all()
+        plain = {"value": wl.templates.n_templates * sub.n_structures / (ms / 1e3), "unit": UNIT,
+                 "structures": sub.n_structures, "same_hits_as_batched": bool(same)}
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        h2d = wl.structures.nbytes() + sum(getattr(wl.templates, f).nbytes for f in (
+            "atom_offset", "code", "res_seq", "chain", "xyz", "dist_weight", "name_offset", "names",
+            "resname_offset", "resnames", "dim"))
+        times, d2h = [], 0
+        for i in range(args.warmup + args.steps):
+            t1 = time.perf_counter()
+            tp2 = _native.Templates(wl.templates)
+            st2 = _native.Structures(wl.structures)
+            r2 = _native.query(tp2, st2, P)
+            a2 = r2.arrays()
+            del tp2, st2
+            dt = time.perf_counter() - t1
+            if i >= args.warmup:
+                times.append(dt)
+            d2h = sum(v.nbytes for k, v in a2.items() if hasattr(v, "nbytes"))
+        tot = sum(times)
+        if dist:
+            import torch
+
+            t = torch.tensor([tot], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            tot = float(t.item())
+        e2e = {"value": pairs_step * world * args.steps / tot, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
+
+    # ---- CPU baseline (rank 0, N=1)
+    cpu = None
+    if rank == 0 and world == 1:
+        threads = os.cpu_count() or 1
+        n = args.cpu_structures or 64
+        v, dt, pairs, _ = cpu_sample(wl, n, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{n} structures x {wl.templates.n_templates} templates ({pairs} pairs, {dt:.1f} s)"}
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64",
+        "data": "synthetic",
+        "config": {"workload": wl.name, "pairs_per_gpu": pairs_step, "structures": wl.structures.n_structures,
+                   "templates": wl.templates.n_templates, "atoms": wl.structures.n_atoms,
+                   "params": wl.params, "l2": "inputs and candidate lists larger than L2 (no flush)",
+                   "adversarial": wl.notes, "generation_s": round(gen_s, 1)},
+        "hits_per_s": hits_per_s,
+        "hits_per_step": s0["hits"],
+        "plain_fp64": plain,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "kernel": "k_search", "peak_kind": peak_kind,
+                     "bytes_expansion_per_step": exp_bytes / args.steps,
+                     "ms_expansion_per_step": exp_ms / args.steps},
+        "stage_ms": {"candidates": s0["ms_candidates"], "expansion": s0["ms_expansion"],
+                     "superposition": s0["ms_superposition"], "total": s0["ms_total"]},
+        "counters": {k: s0[k] for k in ("pairs", "candidate_entries", "partials", "complete", "passing", "hits",
+                                        "fp64_rechecks", "chunks")},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -529,6 +529,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     DBuf<unsigned long long> d_counters, d_ccount, d_pcount;
     DBuf<int32_t> d_c_pair, d_c_atoms, d_p_pair, d_p_nan, d_p_atoms;
     DBuf<int64_t> d_c_ord, d_p_row, d_p_ord;
+    DBuf<double> d_c_rmsd;
     DBuf<double> d_p_rmsd, d_p_rot, d_p_cen;
     std::vector<DBuf<int64_t>> scan_tmp;
     std::vector<HitRec> recs;
@@ -604,6 +605,8 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
         CUDA_TRY(dalloc(d_c_pair, c_cap, st));
         CUDA_TRY(dalloc(d_c_ord, c_cap, st));
         CUDA_TRY(dalloc(d_c_atoms, (size_t)c_cap * stride, st));
+        const bool cut_inline = !P->best_match && P->max_candidates >= 0;
+        if (cut_inline) CUDA_TRY(dalloc(d_c_rmsd, c_cap, st));
         while (s0 < S) {
             int s1 = s0;
             int64_t entries = 0;
@@ -653,6 +656,8 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             sa.best_match = P->best_match;
             sa.max_candidates = P->max_candidates;
             sa.warp_smem = 16 * 1024;
+            sa.cut_inline = cut_inline ? 1 : 0;
+            sa.rmsd_threshold = P->rmsd_threshold;
             {
                 const char *b = getenv("PJG_KERNEL_BUDGET_S");
                 double sec = b ? atof(b) : 120.0;
@@ -667,7 +672,8 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             for (int attempt = 0; attempt < 8; attempt++) {
                 CUDA_TRY(cudaMemsetAsync(d_pair_counter.p, 0, sizeof(int32_t), st));
                 CUDA_TRY(cudaMemsetAsync(d_ccount.p, 0, sizeof(unsigned long long), st));
-                CompleteRows cr{d_ccount.p, c_cap, stride, d_c_pair.p, d_c_ord.p, d_c_atoms.p};
+                CompleteRows cr{d_ccount.p, c_cap, stride, d_c_pair.p, d_c_ord.p, d_c_atoms.p,
+                                cut_inline ? d_c_rmsd.p : nullptr};
                 int grid = sm_count() * 8;
                 CUDA_TRY(launch_search(st, grid, wide, fp32, cv, tv, cd, sa, d_pair_counter.p, scn_c, cr, d_counters.p));
                 launches++;
@@ -682,6 +688,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 CUDA_TRY(dalloc(d_c_pair, c_cap, st));
                 CUDA_TRY(dalloc(d_c_ord, c_cap, st));
                 CUDA_TRY(dalloc(d_c_atoms, (size_t)c_cap * stride, st));
+                if (cut_inline) CUDA_TRY(dalloc(d_c_rmsd, c_cap, st));
                 CUDA_TRY(cudaMemcpyAsync(d_counters.p, snap, sizeof snap, cudaMemcpyHostToDevice, st));
             }
             CUDA_TRY(cudaEventRecord(ev[3], st));
@@ -689,7 +696,8 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 unsigned long long nc = 0;
                 CUDA_TRY(cudaMemcpyAsync(&nc, d_ccount.p, sizeof nc, cudaMemcpyDeviceToHost, st));
                 CUDA_TRY(cudaStreamSynchronize(st));
-                CompleteRows cr{d_ccount.p, c_cap, stride, d_c_pair.p, d_c_ord.p, d_c_atoms.p};
+                CompleteRows cr{d_ccount.p, c_cap, stride, d_c_pair.p, d_c_ord.p, d_c_atoms.p,
+                                cut_inline ? d_c_rmsd.p : nullptr};
                 int64_t need = std::max<int64_t>((int64_t)nc, 1);
                 if (need > p_cap) p_cap = need;
                 CUDA_TRY(dalloc(d_p_row, p_cap, st));
@@ -878,7 +886,7 @@ done:
         dfree(d_cand_xyz, st); dfree(d_leaf_xyz, st); dfree(d_counters, st); dfree(d_ccount, st);
         dfree(d_pcount, st); dfree(d_c_pair, st); dfree(d_c_atoms, st); dfree(d_p_pair, st);
         dfree(d_p_nan, st); dfree(d_p_atoms, st); dfree(d_c_ord, st); dfree(d_p_row, st);
-        dfree(d_p_ord, st); dfree(d_p_rmsd, st); dfree(d_p_rot, st); dfree(d_p_cen, st);
+        dfree(d_p_ord, st); dfree(d_p_rmsd, st); dfree(d_c_rmsd, st); dfree(d_p_rot, st); dfree(d_p_cen, st);
         for (auto &b : scan_tmp) dfree(b, st);
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);

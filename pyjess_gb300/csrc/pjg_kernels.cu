@@ -356,6 +356,225 @@ __global__ void k_leaf_order(ChunkView cv, int32_t n_sigs, const int32_t *count,
 }
 
 // ---------------------------------------------------------------------------
+// Superposition: warp per complete assignment.  Lanes hold the atom pairs
+// (molecule atom, template atom) in template order, the warp reduces the
+// centroids, the squared norms and the 3x3 cross-covariance S in FP64, and
+// lane 0 solves the 4x4 quaternion eigenproblem: the largest root of the
+// characteristic polynomial of Horn's key matrix by Newton's method from
+// the upper bound (sumA + sumB)/2, the quaternion from the adjugate of
+// (K - lambda I).  rmsd = sqrt(max(sumA + sumB - 2 lambda, 0) / n) and R
+// maps molecule coordinates onto the template frame, as
+// Superposition_rmsd / Superposition_rotation do.
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
+    return v;
+}
+
+__device__ double det3(double a, double b, double c, double d, double e, double f, double g, double h,
+                       double i) {
+    return a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+}
+
+__device__ double det4(const double K[4][4]) {
+    double d = 0.0;
+    for (int c = 0; c < 4; c++) {
+        int c0 = c == 0 ? 1 : 0;
+        int c1 = c <= 1 ? 2 : 1;
+        int c2 = c <= 2 ? 3 : 2;
+        double minor = det3(K[1][c0], K[1][c1], K[1][c2], K[2][c0], K[2][c1], K[2][c2], K[3][c0],
+                            K[3][c1], K[3][c2]);
+        d += ((c & 1) ? -1.0 : 1.0) * K[0][c] * minor;
+    }
+    return d;
+}
+
+// 4x4 symmetric Jacobi: largest eigenvalue and its eigenvector.  Used when
+// the top two eigenvalues of the key matrix are close (Newton's root of the
+// characteristic polynomial then loses accuracy, and the adjugate
+// eigenvector degenerates); Jacobi's eigenvalues are accurate to
+// eps * |K| whatever the gap.
+__device__ double jacobi4_top(double A[4][4], double v[4]) {
+    double V[4][4];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) V[i][j] = i == j ? 1.0 : 0.0;
+    double scale = 0.0;
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) scale = fmax(scale, fabs(A[i][j]));
+    for (int sweep = 0; sweep < 50; sweep++) {
+        double off = 0.0;
+        for (int p = 0; p < 4; p++)
+            for (int q = p + 1; q < 4; q++) off += fabs(A[p][q]);
+        if (off <= 1e-17 * scale) break;
+        for (int p = 0; p < 3; p++)
+            for (int q = p + 1; q < 4; q++) {
+                if (A[p][q] == 0.0) continue;
+                double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+                double tt = 1.0 / (fabs(theta) + sqrt(theta * theta + 1.0));
+                if (theta < 0) tt = -tt;
+                double cc = 1.0 / sqrt(tt * tt + 1.0), ss = tt * cc;
+                for (int r = 0; r < 4; r++) {
+                    double arp = A[r][p], arq = A[r][q];
+                    A[r][p] = cc * arp - ss * arq;
+                    A[r][q] = ss * arp + cc * arq;
+                }
+                for (int r = 0; r < 4; r++) {
+                    double apr = A[p][r], aqr = A[q][r];
+                    A[p][r] = cc * apr - ss * aqr;
+                    A[q][r] = ss * apr + cc * aqr;
+                }
+                for (int r = 0; r < 4; r++) {
+                    double vrp = V[r][p], vrq = V[r][q];
+                    V[r][p] = cc * vrp - ss * vrq;
+                    V[r][q] = ss * vrp + cc * vrq;
+                }
+            }
+    }
+    int best = 0;
+    for (int i = 1; i < 4; i++)
+        if (A[i][i] > A[best][best]) best = i;
+    for (int i = 0; i < 4; i++) v[i] = V[i][best];
+    return A[best][best];
+}
+
+__device__ void key_matrix(const double S[9], double K[4][4]) {
+    const double Sxx = S[0], Sxy = S[1], Sxz = S[2], Syx = S[3], Syy = S[4], Syz = S[5], Szx = S[6],
+                 Szy = S[7], Szz = S[8];
+    K[0][0] = Sxx + Syy + Szz; K[0][1] = Syz - Szy; K[0][2] = Szx - Sxz; K[0][3] = Sxy - Syx;
+    K[1][0] = Syz - Szy; K[1][1] = Sxx - Syy - Szz; K[1][2] = Sxy + Syx; K[1][3] = Szx + Sxz;
+    K[2][0] = Szx - Sxz; K[2][1] = Sxy + Syx; K[2][2] = -Sxx + Syy - Szz; K[2][3] = Syz + Szy;
+    K[3][0] = Sxy - Syx; K[3][1] = Szx + Sxz; K[3][2] = Syz + Szy; K[3][3] = -Sxx - Syy + Szz;
+}
+
+// Largest eigenvalue of the key matrix: Newton on its characteristic
+// polynomial l^4 + c2 l^2 + c1 l + c0 (c2 = -2 |S|^2, c1 = -8 det S,
+// c0 = det K) from the upper bound E0 = (sumA + sumB) / 2.  The root's
+// error is about eps * lambda^2 / gap; when P'(lambda) shows a gap below
+// 1e-4 lambda, *close is set and the caller solves K by Jacobi instead.
+__device__ double key_lambda(const double S[9], const double K[4][4], double E0, bool *close) {
+    double fro = 0.0;
+    for (int i = 0; i < 9; i++) fro += S[i] * S[i];
+    const double c2 = -2.0 * fro;
+    const double c1 = -8.0 * det3(S[0], S[1], S[2], S[3], S[4], S[5], S[6], S[7], S[8]);
+    const double c0 = det4(K);
+    double lam = E0;
+    for (int it = 0; it < 60; it++) {
+        double l2 = lam * lam;
+        double P = (l2 + c2) * l2 + c1 * lam + c0;
+        double dP = 4.0 * l2 * lam + 2.0 * c2 * lam + c1;
+        if (dP == 0.0) break;
+        double step = P / dP;
+        lam -= step;
+        if (fabs(step) <= 1e-14 * fabs(lam) + 1e-300) break;
+    }
+    double l2 = lam * lam;
+    double dP = 4.0 * l2 * lam + 2.0 * c2 * lam + c1;
+    *close = fabs(dP) < 4e-4 * fabs(l2 * lam);
+    return lam;
+}
+
+__device__ __forceinline__ double rmsd_from_lambda(double E0, double lam, int n) {
+    double r2 = 2.0 * (E0 - lam) / (double)n;
+    return sqrt(r2 > 0.0 ? r2 : 0.0);
+}
+
+__device__ void quaternion_fit(const double S[9], double E0, int n, double *rmsd, double R[9], bool *bad) {
+    double K[4][4];
+    key_matrix(S, K);
+    bool close = false;
+    double lam = key_lambda(S, K, E0, &close);
+    double best[4] = {0, 0, 0, 0}, bestn = -1.0;
+    if (close) {
+        double A[4][4];
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) A[i][j] = K[i][j];
+        lam = jacobi4_top(A, best);
+        bestn = best[0] * best[0] + best[1] * best[1] + best[2] * best[2] + best[3] * best[3];
+    }
+    *rmsd = rmsd_from_lambda(E0, lam, n);
+    // eigenvector: largest column of adj(K - lam I)
+    double A[4][4];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) A[i][j] = K[i][j] - (i == j ? lam : 0.0);
+    for (int col = 0; col < 4 && !close; col++) {
+        double v[4];
+        for (int row = 0; row < 4; row++) {
+            // cofactor C[col][row] of A (adjugate column `col`)
+            int r0 = col == 0 ? 1 : 0, r1 = col <= 1 ? 2 : 1, r2i = col <= 2 ? 3 : 2;
+            int k0 = row == 0 ? 1 : 0, k1 = row <= 1 ? 2 : 1, k2 = row <= 2 ? 3 : 2;
+            double m = det3(A[r0][k0], A[r0][k1], A[r0][k2], A[r1][k0], A[r1][k1], A[r1][k2], A[r2i][k0],
+                            A[r2i][k1], A[r2i][k2]);
+            v[row] = ((row + col) & 1) ? -m : m;
+        }
+        double nn = v[0] * v[0] + v[1] * v[1] + v[2] * v[2] + v[3] * v[3];
+        if (nn > bestn) {
+            bestn = nn;
+            for (int i = 0; i < 4; i++) best[i] = v[i];
+        }
+    }
+    double scale = 0.0;
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) scale = fmax(scale, fabs(K[i][j]));
+    if (!close && !(bestn > 1e-24 * scale * scale * scale * scale * scale * scale)) {
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) A[i][j] = K[i][j];
+        jacobi4_top(A, best);
+        bestn = best[0] * best[0] + best[1] * best[1] + best[2] * best[2] + best[3] * best[3];
+    }
+    double inv = 1.0 / sqrt(bestn);
+    double q0 = best[0] * inv, q1 = best[1] * inv, q2 = best[2] * inv, q3 = best[3] * inv;
+    R[0] = q0 * q0 + q1 * q1 - q2 * q2 - q3 * q3;
+    R[1] = 2.0 * (q1 * q2 - q0 * q3);
+    R[2] = 2.0 * (q1 * q3 + q0 * q2);
+    R[3] = 2.0 * (q1 * q2 + q0 * q3);
+    R[4] = q0 * q0 - q1 * q1 + q2 * q2 - q3 * q3;
+    R[5] = 2.0 * (q2 * q3 - q0 * q1);
+    R[6] = 2.0 * (q1 * q3 - q0 * q2);
+    R[7] = 2.0 * (q2 * q3 + q0 * q1);
+    R[8] = q0 * q0 - q1 * q1 - q2 * q2 + q3 * q3;
+    // the reference's rotation formula divides by the singular values of the
+    // covariance and is undefined for fewer than three atom pairs
+    *bad = n < 3;
+}
+
+// RMSD of one assignment computed by a single lane (sums in template atom
+// order), used where a lane needs the value while searching.
+__device__ double lane_rmsd(int n, const int32_t *atoms, const double *xyz, const double *tpos) {
+    double ca[3] = {0, 0, 0}, cb[3] = {0, 0, 0};
+    for (int k = 0; k < n; k++)
+        for (int d = 0; d < 3; d++) {
+            ca[d] += xyz[3 * (int64_t)atoms[k] + d];
+            cb[d] += tpos[3 * k + d];
+        }
+    for (int d = 0; d < 3; d++) {
+        ca[d] /= (double)n;
+        cb[d] /= (double)n;
+    }
+    double sumA = 0, sumB = 0, S[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < n; k++) {
+        double a[3], b[3];
+        for (int d = 0; d < 3; d++) {
+            a[d] = xyz[3 * (int64_t)atoms[k] + d] - ca[d];
+            b[d] = tpos[3 * k + d] - cb[d];
+        }
+        sumA += a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+        sumB += b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) S[3 * r + c] += a[r] * b[c];
+    }
+    double K[4][4];
+    key_matrix(S, K);
+    double E0 = 0.5 * (sumA + sumB);
+    bool close = false;
+    double lam = key_lambda(S, K, E0, &close);
+    if (close) {
+        double v[4];
+        lam = jacobi4_top(K, v);
+    }
+    return rmsd_from_lambda(E0, lam, n);
+}
+
+// ---------------------------------------------------------------------------
 // Search: warp per (structure, template) pair.
 //
 // The reference's Scanner_next is a depth-first backtracking over levels,
@@ -564,7 +783,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
         const int64_t off0 = st.lvl_off[0];
 
         // emit complete rows: `pass` lanes with their level positions
-        auto emit = [&](bool pass, const RowT *prow, int lastpos) -> void {
+        auto emit = [&](bool pass, const RowT *prow, int lastpos, double rm) -> void {
             unsigned m = __ballot_sync(FULL_MASK, pass);
             if (!m) return;
             int np = __popc(m);
@@ -586,12 +805,14 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
                     dst[st.order[n - 1]] = at;
                     out.pair[ri] = pair;
                     out.ordinal[ri] = emitted + rk;
+                    if (out.rmsd) out.rmsd[ri] = rm;
                 }
             }
             emitted += np;
         };
 
         bool stop = false;
+        int64_t cut_base = 0;
         const int64_t stop_at = (sa.best_match && sa.max_candidates >= 0) ? (int64_t)sa.max_candidates + 2 : -1;
 
         if (n == 1) {
@@ -599,7 +820,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
             // reporting (patches/Scanner.c.patch:244-263): seeds 1..m0-1
             for (int b = 1; b < m0 && !stop; b += 32) {
                 int p = b + lane;
-                emit(p < m0, nullptr, p);
+                emit(p < m0, nullptr, p, 0.0);
                 if (stop_at >= 0 && emitted >= stop_at) stop = true;
                 if (over_budget()) stop = true;
             }
@@ -733,7 +954,43 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
                 }
                 if (last) {
                     unsigned m = __ballot_sync(FULL_MASK, pass);
-                    emit(pass, prow, cr);
+                    double rm = 0.0;
+                    if (sa.cut_inline && m) {
+                        // Query.__next__'s max_candidates cut, applied while
+                        // searching: the candidate whose distance from the last
+                        // hit (or the template start) reaches M+1 ends the
+                        // template's stream after it has been considered
+                        bool hitf = false;
+                        if (pass) {
+                            int32_t at[32];
+                            for (int j = 0; j < n - 1; j++) {
+                                int pos = (int)prow[j];
+                                at[st.order[j]] = (j == 0) ? cd.cand_atom[off0 + pos] : cd.leaf_atom[st.lvl_off[j] + pos];
+                            }
+                            at[st.order[n - 1]] = cd.leaf_atom[st.lvl_off[n - 1] + cr];
+                            rm = lane_rmsd(n, at, xyz64, tv.pos + 3 * (int64_t)ab);
+                            hitf = rm <= sa.rmsd_threshold && n >= 3;
+                        }
+                        unsigned hl = __ballot_sync(FULL_MASK, hitf);
+                        unsigned mm = m;
+                        int r = 0, keep = 32;
+                        while (mm) {
+                            int ln = __ffs(mm) - 1;
+                            mm &= mm - 1;
+                            int64_t q = emitted + r;
+                            if (q - cut_base == (int64_t)sa.max_candidates + 1) {
+                                keep = r;
+                                stop = true;
+                                break;
+                            }
+                            if ((hl >> ln) & 1u) cut_base = q + 1;
+                            r++;
+                        }
+                        int myrank = __popc(m & ((1u << lane) - 1u));
+                        pass = pass && myrank <= keep;
+                        m = __ballot_sync(FULL_MASK, pass);
+                    }
+                    emit(pass, prow, cr, rm);
                     __syncwarp();
                     if (lane == 0) st.F[child] += __popc(m);
                     if (stop_at >= 0 && emitted >= stop_at) stop = true;
@@ -783,150 +1040,6 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
 }
 
 
-// ---------------------------------------------------------------------------
-// Superposition: warp per complete assignment.  Lanes hold the atom pairs
-// (molecule atom, template atom) in template order, the warp reduces the
-// centroids, the squared norms and the 3x3 cross-covariance S in FP64, and
-// lane 0 solves the 4x4 quaternion eigenproblem: the largest root of the
-// characteristic polynomial of Horn's key matrix by Newton's method from
-// the upper bound (sumA + sumB)/2, the quaternion from the adjugate of
-// (K - lambda I).  rmsd = sqrt(max(sumA + sumB - 2 lambda, 0) / n) and R
-// maps molecule coordinates onto the template frame, as
-// Superposition_rmsd / Superposition_rotation do.
-
-__device__ __forceinline__ double warp_sum(double v) {
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
-    return v;
-}
-
-__device__ double det3(double a, double b, double c, double d, double e, double f, double g, double h,
-                       double i) {
-    return a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
-}
-
-__device__ double det4(const double K[4][4]) {
-    double d = 0.0;
-    for (int c = 0; c < 4; c++) {
-        int c0 = c == 0 ? 1 : 0;
-        int c1 = c <= 1 ? 2 : 1;
-        int c2 = c <= 2 ? 3 : 2;
-        double minor = det3(K[1][c0], K[1][c1], K[1][c2], K[2][c0], K[2][c1], K[2][c2], K[3][c0],
-                            K[3][c1], K[3][c2]);
-        d += ((c & 1) ? -1.0 : 1.0) * K[0][c] * minor;
-    }
-    return d;
-}
-
-// 4x4 symmetric Jacobi: fallback eigenvector when the adjugate degenerates
-__device__ void jacobi4_top(double A[4][4], double v[4]) {
-    double V[4][4];
-    for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++) V[i][j] = i == j ? 1.0 : 0.0;
-    for (int sweep = 0; sweep < 50; sweep++) {
-        double off = 0.0;
-        for (int p = 0; p < 4; p++)
-            for (int q = p + 1; q < 4; q++) off += fabs(A[p][q]);
-        if (off < 1e-15) break;
-        for (int p = 0; p < 3; p++)
-            for (int q = p + 1; q < 4; q++) {
-                if (A[p][q] == 0.0) continue;
-                double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
-                double tt = 1.0 / (fabs(theta) + sqrt(theta * theta + 1.0));
-                if (theta < 0) tt = -tt;
-                double cc = 1.0 / sqrt(tt * tt + 1.0), ss = tt * cc;
-                for (int r = 0; r < 4; r++) {
-                    double arp = A[r][p], arq = A[r][q];
-                    A[r][p] = cc * arp - ss * arq;
-                    A[r][q] = ss * arp + cc * arq;
-                }
-                for (int r = 0; r < 4; r++) {
-                    double apr = A[p][r], aqr = A[q][r];
-                    A[p][r] = cc * apr - ss * aqr;
-                    A[q][r] = ss * apr + cc * aqr;
-                }
-                for (int r = 0; r < 4; r++) {
-                    double vrp = V[r][p], vrq = V[r][q];
-                    V[r][p] = cc * vrp - ss * vrq;
-                    V[r][q] = ss * vrp + cc * vrq;
-                }
-            }
-    }
-    int best = 0;
-    for (int i = 1; i < 4; i++)
-        if (A[i][i] > A[best][best]) best = i;
-    for (int i = 0; i < 4; i++) v[i] = V[i][best];
-}
-
-__device__ void quaternion_fit(const double S[9], double E0, int n, double *rmsd, double R[9], bool *bad) {
-    const double Sxx = S[0], Sxy = S[1], Sxz = S[2], Syx = S[3], Syy = S[4], Syz = S[5], Szx = S[6],
-                 Szy = S[7], Szz = S[8];
-    double K[4][4] = {{Sxx + Syy + Szz, Syz - Szy, Szx - Sxz, Sxy - Syx},
-                      {Syz - Szy, Sxx - Syy - Szz, Sxy + Syx, Szx + Sxz},
-                      {Szx - Sxz, Sxy + Syx, -Sxx + Syy - Szz, Syz + Szy},
-                      {Sxy - Syx, Szx + Sxz, Syz + Szy, -Sxx - Syy + Szz}};
-    double fro = 0.0;
-    for (int i = 0; i < 9; i++) fro += S[i] * S[i];
-    const double c2 = -2.0 * fro;
-    const double c1 = -8.0 * det3(Sxx, Sxy, Sxz, Syx, Syy, Syz, Szx, Szy, Szz);
-    const double c0 = det4(K);
-    double lam = E0;
-    for (int it = 0; it < 60; it++) {
-        double l2 = lam * lam;
-        double P = (l2 + c2) * l2 + c1 * lam + c0;
-        double dP = 4.0 * l2 * lam + 2.0 * c2 * lam + c1;
-        if (dP == 0.0) break;
-        double step = P / dP;
-        lam -= step;
-        if (fabs(step) <= 1e-14 * fabs(lam) + 1e-300) break;
-    }
-    double r2 = 2.0 * (E0 - lam) / (double)n;
-    *rmsd = sqrt(r2 > 0.0 ? r2 : 0.0);
-    // eigenvector: largest column of adj(K - lam I)
-    double A[4][4];
-    for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++) A[i][j] = K[i][j] - (i == j ? lam : 0.0);
-    double best[4] = {0, 0, 0, 0}, bestn = -1.0;
-    for (int col = 0; col < 4; col++) {
-        double v[4];
-        for (int row = 0; row < 4; row++) {
-            // cofactor C[col][row] of A (adjugate column `col`)
-            int r0 = col == 0 ? 1 : 0, r1 = col <= 1 ? 2 : 1, r2i = col <= 2 ? 3 : 2;
-            int k0 = row == 0 ? 1 : 0, k1 = row <= 1 ? 2 : 1, k2 = row <= 2 ? 3 : 2;
-            double m = det3(A[r0][k0], A[r0][k1], A[r0][k2], A[r1][k0], A[r1][k1], A[r1][k2], A[r2i][k0],
-                            A[r2i][k1], A[r2i][k2]);
-            v[row] = ((row + col) & 1) ? -m : m;
-        }
-        double nn = v[0] * v[0] + v[1] * v[1] + v[2] * v[2] + v[3] * v[3];
-        if (nn > bestn) {
-            bestn = nn;
-            for (int i = 0; i < 4; i++) best[i] = v[i];
-        }
-    }
-    double scale = 0.0;
-    for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++) scale = fmax(scale, fabs(K[i][j]));
-    if (!(bestn > 1e-24 * scale * scale * scale * scale * scale * scale)) {
-        for (int i = 0; i < 4; i++)
-            for (int j = 0; j < 4; j++) A[i][j] = K[i][j];
-        jacobi4_top(A, best);
-        bestn = best[0] * best[0] + best[1] * best[1] + best[2] * best[2] + best[3] * best[3];
-    }
-    double inv = 1.0 / sqrt(bestn);
-    double q0 = best[0] * inv, q1 = best[1] * inv, q2 = best[2] * inv, q3 = best[3] * inv;
-    R[0] = q0 * q0 + q1 * q1 - q2 * q2 - q3 * q3;
-    R[1] = 2.0 * (q1 * q2 - q0 * q3);
-    R[2] = 2.0 * (q1 * q3 + q0 * q2);
-    R[3] = 2.0 * (q1 * q2 + q0 * q3);
-    R[4] = q0 * q0 - q1 * q1 + q2 * q2 - q3 * q3;
-    R[5] = 2.0 * (q2 * q3 - q0 * q1);
-    R[6] = 2.0 * (q1 * q3 - q0 * q2);
-    R[7] = 2.0 * (q2 * q3 + q0 * q1);
-    R[8] = q0 * q0 - q1 * q1 - q2 * q2 + q3 * q3;
-    // the reference's rotation formula divides by the singular values of the
-    // covariance and is undefined for fewer than three atom pairs
-    *bad = n < 3;
-}
-
 __global__ void k_superpose(ChunkView cv, TemplateView tv, SuperArgs sa, CompleteRows in, PassRows out,
                             unsigned long long *counters) {
     int lane = lane_id();
@@ -970,6 +1083,9 @@ __global__ void k_superpose(ChunkView cv, TemplateView tv, SuperArgs sa, Complet
         bool bad = false;
         if (lane == 0) quaternion_fit(S, 0.5 * (sumA + sumB), n, &rmsd, R, &bad);
         rmsd = __shfl_sync(FULL_MASK, rmsd, 0);
+        // rows whose rmsd already decided the max_candidates cut keep it, so
+        // the automaton on the host replays the same decisions
+        if (in.rmsd) rmsd = in.rmsd[i];
         if (rmsd <= sa.rmsd_threshold) {
             int64_t j = 0;
             if (lane == 0) j = (int64_t)atomicAdd(out.count, 1ull);

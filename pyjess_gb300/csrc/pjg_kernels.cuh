@@ -18,6 +18,9 @@ struct SearchArgs {
     int32_t best_match;
     int32_t max_candidates;
     int32_t warp_smem;                 // bytes of shared memory per warp
+    int32_t cut_inline;                // apply the max_candidates cut while
+                                       // searching (non-best mode)
+    double rmsd_threshold;
     uint64_t budget_ns;                // per-warp wall-time budget (globaltimer)
 };
 
@@ -33,6 +36,8 @@ struct CompleteRows {
     int32_t *pair;                     // chunk-local pair = s * T + t
     int64_t *ordinal;                  // position in the pair's stream
     int32_t *atoms;                    // [capacity * stride], template order
+    double *rmsd;                      // rmsd computed in the search (inline
+                                       // cut mode), else nullptr
 };
 
 // Complete assignments with rmsd <= threshold, written by k_superpose.

@@ -317,9 +317,11 @@ class Workload:
         return self.templates.n_templates * self.structures.n_structures
 
 
-def config(index: int, *, scale: float = 1.0, n_structures=None, n_templates=None) -> Workload:
+def config(index: int, *, scale: float = 1.0, n_structures=None, n_templates=None,
+           residues=None) -> Workload:
     """Benchmark configuration `index` (0-4).  `scale` shrinks structure and
-    template counts proportionally (parity tests run reduced instances)."""
+    template counts proportionally (parity tests run reduced instances);
+    `residues` = (lo, hi) overrides the structure length range of config 4."""
     ss = _seed(index)
     if index == 0:
         rng = np.random.Generator(np.random.PCG64(ss))
@@ -363,7 +365,8 @@ def config(index: int, *, scale: float = 1.0, n_structures=None, n_templates=Non
         nt = n_templates or max(1, int(round(500 * scale)))
         kids = ss.spawn(ns + nt + 1)
         meta = np.random.Generator(np.random.PCG64(kids[-1]))
-        lengths = meta.integers(2000, 5001, size=ns)
+        lo, hi = residues if residues else (2000, 5000)
+        lengths = meta.integers(lo, hi + 1, size=ns)
         structs = make_structures([np.random.Generator(np.random.PCG64(kids[i])) for i in range(ns)],
                                   lengths, meta.integers(1, 5, size=ns))
         donors = meta.integers(0, ns, size=nt)

@@ -15,6 +15,12 @@ from helpers import hit_keys, parse_block
 pytestmark = pytest.mark.gpu
 
 RMSD_TOL = 1e-9    # Angstrom, GPU quaternion solver vs oracle Jacobi (FP64)
+# Rotation entries.  Where the covariance is well conditioned
+# (s3/s1 > 1e-3) the GPU quaternion rotation and the oracle's polar
+# decomposition agree to ROT_TOL.  For near-coplanar assignments the polar
+# formula (like the reference's, undefined at rank < 3) loses accuracy, so
+# there the GPU rotation is checked against an SVD Kabsch solution instead,
+# and everywhere it must reproduce the reported rmsd when applied.
 ROT_TOL = 1e-7
 
 MODES = ("fp32", "fp64", "plain")
@@ -36,6 +42,61 @@ def gpu_query(ptemplates, pstructures, mode="fp32", **kw):
     return res
 
 
+def check_rotations(g, r, ptemplates, pstructures, limit=5000):
+    """GPU rotations: proper, optimal (they reproduce the reported rmsd),
+    equal to the oracle's where the fit is well conditioned and to an SVD
+    Kabsch rotation elsewhere (see ROT_TOL)."""
+    for i in range(min(g["count"], limit)):
+        R = g["rotation"][i].reshape(3, 3)
+        assert abs(np.linalg.det(R) - 1.0) < 1e-9
+        s, t = int(g["structure"][i]), int(g["template"][i])
+        a0, a1 = g["atom_offset"][i], g["atom_offset"][i + 1]
+        mol = pstructures.xyz[pstructures.atom_offset[s] + g["atoms"][a0:a1]]
+        tpl = ptemplates.xyz[ptemplates.atom_offset[t]:ptemplates.atom_offset[t + 1]]
+        c = g["centres"][i]
+        fit = (mol - c[:3]) @ R.T + c[3:]
+        rmsd = np.sqrt(((fit - tpl) ** 2).sum() / len(tpl))
+        assert abs(rmsd - g["rmsd"][i]) < 1e-7, (i, rmsd, g["rmsd"][i])
+        if len(tpl) < 3:
+            continue
+        a, b = mol - mol.mean(0), tpl - tpl.mean(0)
+        U, sv, Vt = np.linalg.svd(a.T @ b)
+        cond = sv[2] / sv[0] if sv[0] > 0 else 0.0
+        if cond > 1e-3:
+            assert np.abs(R - r["rotation"][i].reshape(3, 3)).max() <= ROT_TOL
+        elif cond > 1e-9:
+            d = np.sign(np.linalg.det(Vt.T @ U.T))
+            Rk = Vt.T @ np.diag([1, 1, d]) @ U.T
+            assert np.abs(R - Rk).max() <= 1e-12 / cond + 1e-9
+
+
+def svd_rmsd(mol, tpl):
+    a, b = mol - mol.mean(0), tpl - tpl.mean(0)
+    M = a.T @ b
+    sv = np.linalg.svd(M, compute_uv=False)
+    lam = sv[0] + sv[1] + (sv[2] if np.linalg.det(M) > 0 else -sv[2])
+    e = (a * a).sum() + (b * b).sum() - 2 * lam
+    return np.sqrt(max(e, 0.0) / len(a)), sv
+
+
+def check_rmsd(g, r, ptemplates, pstructures):
+    """|rmsd_gpu - rmsd_oracle| <= RMSD_TOL.  The oracle, like the reference,
+    takes singular values as square roots of the eigenvalues of M^T M, which
+    loses accuracy when the smallest singular value is tiny (s3/s1 < 1e-5:
+    near-coplanar atom sets); there the GPU value must instead be within
+    RMSD_TOL of an SVD of M itself.  Returns the largest GPU-oracle gap."""
+    err = np.abs(g["rmsd"] - r["rmsd"])
+    for i in np.flatnonzero(err > RMSD_TOL):
+        s, t = int(g["structure"][i]), int(g["template"][i])
+        a0, a1 = g["atom_offset"][i], g["atom_offset"][i + 1]
+        mol = pstructures.xyz[pstructures.atom_offset[s] + g["atoms"][a0:a1]]
+        tpl = ptemplates.xyz[ptemplates.atom_offset[t]:ptemplates.atom_offset[t + 1]]
+        exact, sv = svd_rmsd(mol, tpl)
+        assert sv[2] < 1e-5 * sv[0], (i, err[i], sv)
+        assert abs(g["rmsd"][i] - exact) <= RMSD_TOL, (i, g["rmsd"][i], exact)
+    return float(err.max())
+
+
 def compare(ptemplates, pstructures, mode="fp32", check_stats=True, **kw):
     from oracle import oracle
 
@@ -45,10 +106,9 @@ def compare(ptemplates, pstructures, mode="fp32", check_stats=True, **kw):
     r = ref["hits"]
     assert hit_keys(g) == hit_keys(r)
     if r["count"]:
-        err = np.abs(g["rmsd"] - r["rmsd"]).max()
-        assert err <= RMSD_TOL, err
-        assert np.abs(g["rotation"] - r["rotation"]).max() <= ROT_TOL
+        check_rmsd(g, r, ptemplates, pstructures)
         assert np.abs(g["centres"] - r["centres"]).max() <= 1e-9
+        check_rotations(g, r, ptemplates, pstructures)
     gw = res.warnings()
     assert list(gw[0]) == list(ref["warnings"][0]) and list(gw[1]) == list(ref["warnings"][1])
     if check_stats and kw.get("max_candidates") is None:
@@ -173,7 +233,7 @@ def test_config3_adversarial_guard_band():
 def test_config4_dense_reduced(best):
     from pyjess_gb300 import workloads as W
 
-    wl = W.config(4, n_structures=3, n_templates=6)
+    wl = W.config(4, n_structures=3, n_templates=6, residues=(300, 500))
     p = dict(wl.params)
     p["max_candidates"] = 50
     compare(wl.templates, wl.structures, best_match=best, **p)
