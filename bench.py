@@ -332,7 +332,7 @@ def main():
         "stage_ms": {"candidates": s0["ms_candidates"], "expansion": s0["ms_expansion"],
                      "superposition": s0["ms_superposition"], "total": s0["ms_total"]},
         "counters": {k: s0[k] for k in ("pairs", "candidate_entries", "partials", "complete", "passing", "hits",
-                                        "fp64_rechecks", "chunks")},
+                                        "fp64_rechecks", "leaf_exact", "chunks")},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": launches,

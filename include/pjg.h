@@ -124,6 +124,7 @@ typedef struct {
     int64_t passing;                 /* complete with rmsd <= threshold    */
     int64_t hits;                    /* after the automaton                */
     int64_t fp64_rechecks;           /* guard-band rechecks (FP32 mode)    */
+    int64_t leaf_exact;              /* lists ordered by the exact replay  */
     int64_t bytes_candidates;        /* algorithmic bytes, candidate stage */
     int64_t bytes_expansion;         /* algorithmic bytes, expansion stage */
     int64_t bytes_superposition;     /* algorithmic bytes, superposition   */

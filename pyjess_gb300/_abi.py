@@ -60,6 +60,7 @@ class Stats(C.Structure):
         ("passing", C.c_int64),
         ("hits", C.c_int64),
         ("fp64_rechecks", C.c_int64),
+        ("leaf_exact", C.c_int64),
         ("bytes_candidates", C.c_int64),
         ("bytes_expansion", C.c_int64),
         ("bytes_superposition", C.c_int64),

@@ -524,7 +524,11 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     cudaEvent_t ev[8] = {};
     DBuf<AnnulusParam> d_params;
     DBuf<int32_t> d_count, d_scanned, d_cand_atom, d_leaf_atom, d_pair_counter;
-    DBuf<int64_t> d_offset, d_totals;
+    DBuf<int64_t> d_offset, d_totals, d_boff;
+    DBuf<int32_t> d_nblk;
+    DBuf<int64_t> d_exact_list;
+    DBuf<unsigned long long> d_exact_count;
+    DBuf<float4> d_blk_lo, d_blk_hi;
     DBuf<float4> d_cand_xyz, d_leaf_xyz;
     DBuf<unsigned long long> d_counters, d_ccount, d_pcount;
     DBuf<int32_t> d_c_pair, d_c_atoms, d_p_pair, d_p_nan, d_p_atoms;
@@ -627,6 +631,22 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             CUDA_TRY(dalloc(d_offset, (size_t)Wc, st));
             CUDA_TRY(cudaEventRecord(ev[1], st));
             CUDA_TRY(scan_exclusive(cnt_c, Wc, d_offset.p, scan_tmp, st));
+            // blocks of 32 leaves: counts, offsets, total (one small sync)
+            int64_t nblocks = 0;
+            CUDA_TRY(dalloc(d_nblk, (size_t)Wc, st));
+            CUDA_TRY(dalloc(d_boff, (size_t)Wc, st));
+            launch_block_counts(st, Wc, cnt_c, d_nblk.p);
+            CUDA_TRY(scan_exclusive(d_nblk.p, Wc, d_boff.p, scan_tmp, st));
+            {
+                int64_t lastoff = 0;
+                int32_t lastn = 0;
+                CUDA_TRY(cudaMemcpyAsync(&lastoff, d_boff.p + Wc - 1, 8, cudaMemcpyDeviceToHost, st));
+                CUDA_TRY(cudaMemcpyAsync(&lastn, d_nblk.p + Wc - 1, 4, cudaMemcpyDeviceToHost, st));
+                CUDA_TRY(cudaStreamSynchronize(st));
+                nblocks = lastoff + lastn;
+            }
+            CUDA_TRY(dalloc(d_blk_lo, (size_t)std::max<int64_t>(nblocks, 1), st));
+            CUDA_TRY(dalloc(d_blk_hi, (size_t)std::max<int64_t>(nblocks, 1), st));
             CUDA_TRY(dalloc(d_cand_atom, (size_t)entries, st));
             CUDA_TRY(dalloc(d_leaf_atom, (size_t)entries, st));
             CUDA_TRY(dalloc(d_cand_xyz, (size_t)entries, st));
@@ -635,16 +655,20 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 int blocks = (int)std::min<int64_t>((Wc + 7) / 8, (int64_t)sm_count() * 32);
                 launch_candidates(st, std::max(blocks, 1), true, cv, sv, nullptr, nullptr, d_offset.p, d_cand_atom.p,
                                   d_cand_xyz.p);
-                int lb = (int)std::min<int64_t>((Wc + 127) / 128, (int64_t)sm_count() * 16);
-                launch_leaf_order(st, std::max(lb, 1), cv, G, cnt_c, d_offset.p, d_cand_atom.p, d_cand_xyz.p,
-                                  d_leaf_atom.p, d_leaf_xyz.p);
-                launches += 2;
+                int lb = (int)std::min<int64_t>((Wc + LEAF_WARPS - 1) / LEAF_WARPS, (int64_t)sm_count() * 32);
+                CUDA_TRY(dalloc(d_exact_list, (size_t)Wc, st));
+                CUDA_TRY(dalloc(d_exact_count, 1, st));
+                launch_leaf_order(st, std::max(lb, 1), cv, G, cnt_c, d_offset.p, d_boff.p, d_cand_atom.p,
+                                  d_cand_xyz.p, d_leaf_atom.p, d_leaf_xyz.p, d_blk_lo.p, d_blk_hi.p, d_exact_list.p,
+                                  d_exact_count.p, d_counters.p);
+                launches += 6;
                 CUDA_TRY(cudaGetLastError());
             }
             CUDA_TRY(cudaEventRecord(ev[2], st));
             TemplateView tv{T, tp->nmax, tp->d_atom_begin, tp->d_sig, tp->d_pos, tp->d_key, tp->d_param_begin,
                             d_params.p};
-            CandView cd{G, cnt_c, d_offset.p, d_cand_atom.p, d_cand_xyz.p, d_leaf_atom.p, d_leaf_xyz.p};
+            CandView cd{G, cnt_c, d_offset.p, d_cand_atom.p, d_cand_xyz.p, d_leaf_atom.p, d_leaf_xyz.p,
+                        d_boff.p, d_blk_lo.p, d_blk_hi.p};
             SearchArgs sa;
             sa.n_pairs = Sc * T;
             if ((int64_t)Sc * T > INT32_MAX) {
@@ -655,7 +679,14 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             sa.reorder = P->reorder;
             sa.best_match = P->best_match;
             sa.max_candidates = P->max_candidates;
-            sa.warp_smem = 16 * 1024;
+            {
+                // shared memory per warp: pair state + tiles of >= 64
+                // entries for every level but the last
+                int levels = std::max(1, tp->nmax - 1);
+                size_t entry = sp->max_atoms > 65535 ? 8 : 4;
+                size_t need = 2816 + entry * 64 * (size_t)levels;
+                sa.warp_smem = (int)((std::max<size_t>(need, 8192) + 15) & ~size_t(15));
+            }
             sa.cut_inline = cut_inline ? 1 : 0;
             sa.rmsd_threshold = P->rmsd_threshold;
             {
@@ -864,6 +895,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     res->stats.passing = (int64_t)recs.size();
     res->stats.hits = (int64_t)res->rmsd.size();
     res->stats.fp64_rechecks = (int64_t)counters[C_RECHECK];
+    res->stats.leaf_exact = (int64_t)counters[C_LEAF_EXACT];
     res->stats.bytes_candidates = (int64_t)counters[C_BYTES_CAND];
     res->stats.bytes_expansion = (int64_t)counters[C_BYTES_EXP];
     {
@@ -886,7 +918,8 @@ done:
         dfree(d_cand_xyz, st); dfree(d_leaf_xyz, st); dfree(d_counters, st); dfree(d_ccount, st);
         dfree(d_pcount, st); dfree(d_c_pair, st); dfree(d_c_atoms, st); dfree(d_p_pair, st);
         dfree(d_p_nan, st); dfree(d_p_atoms, st); dfree(d_c_ord, st); dfree(d_p_row, st);
-        dfree(d_p_ord, st); dfree(d_p_rmsd, st); dfree(d_c_rmsd, st); dfree(d_p_rot, st); dfree(d_p_cen, st);
+        dfree(d_p_ord, st); dfree(d_p_rmsd, st); dfree(d_c_rmsd, st); dfree(d_boff, st); dfree(d_nblk, st);
+        dfree(d_blk_lo, st); dfree(d_blk_hi, st); dfree(d_exact_list, st); dfree(d_exact_count, st); dfree(d_p_rot, st); dfree(d_p_cen, st);
         for (auto &b : scan_tmp) dfree(b, st);
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);

@@ -102,6 +102,9 @@ struct CandView {
     const float4 *cand_xyz;
     const int32_t *leaf_atom;       // structure-local atom, kd leaf order
     const float4 *leaf_xyz;
+    const int64_t *blk_offset;      // first block of the list
+    const float4 *blk_lo;           // bounding box of each block of 32
+    const float4 *blk_hi;           //   consecutive leaves (FP32)
 };
 
 // Counters accumulated by the kernels (int64, device).
@@ -118,6 +121,7 @@ enum Counter : int {
     C_BYTES_SUP,
     C_OVERFLOW,       // complete-row buffer overflow (rows dropped)
     C_PASS_OVERFLOW,  // passing-row buffer overflow
+    C_LEAF_EXACT,     // lists ordered by the exact sequential replay
     C_ERROR,          // error code: 1 template > 32 atoms, 2 frontier tile too
                       // small, 3 time budget exhausted (0 = none)
     C_NUM

@@ -256,6 +256,17 @@ __global__ void k_scan_add(int64_t *out, int64_t n, const int64_t *tile_offsets)
 // right subtree is popped first (pinned by the golden fixture): the DFS
 // leaf order is the partitioned index array read backwards.  Pruning only
 // removes subtrees, so accepted leaves always come out in this order.
+//
+// Fast path (warp per list, shared memory): when no node has a tie at its
+// median boundary (equal axis values on both sides of position n/2), each
+// node's left/right sets are the n/2 smallest / the rest whatever the
+// arrangement qselect leaves behind, so the leaf order follows from a
+// rank-based recursive median split computed by all lanes.  The FP32
+// centroid-relative keys are a monotone rounding of the FP64 coordinates, so
+// a tie there only sends the list to the exact path.  Exact path: the
+// literal sequential qselect replay on the FP64 coordinates.  Each list also
+// gets the bounding boxes of its blocks of 32 consecutive leaves (the
+// search culls whole blocks against a parent's join box).
 
 __device__ __forceinline__ int axis_cmp(double c, double d) { return c < d ? -1 : c > d ? 1 : 0; }
 
@@ -306,53 +317,463 @@ __device__ void qselect(int32_t *base, int n, int k, const KdSel &S) {
     }
 }
 
-__global__ void k_leaf_order(ChunkView cv, int32_t n_sigs, const int32_t *count, const int64_t *offset,
-                             const int32_t *cand_atom, const float4 *cand_xyz, int32_t *leaf_atom,
-                             float4 *leaf_xyz) {
-    int64_t total = (int64_t)cv.n_structures * n_sigs;
-    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < total;
-         w += (int64_t)gridDim.x * blockDim.x) {
-        int m = count[w];
-        if (m <= 0) continue;
-        int s = (int)(w / n_sigs);
-        int64_t o = offset[w];
-        const int32_t *ca = cand_atom + o;
-        int32_t *perm = leaf_atom + o;  // scratch: candidate positions
-        for (int i = 0; i < m; i++) perm[i] = i;
-        KdSel S{ca, cv.xyz64 + 3 * cv.atom_base[s], 0};
-        // explicit stack of (lo, n, axis); depth <= log2(m) + 2
-        int st_lo[40], st_n[40], st_ax[40];
-        int sp = 0;
-        st_lo[0] = 0;
-        st_n[0] = m;
-        st_ax[0] = 0;
-        sp = 1;
-        while (sp > 0) {
-            sp--;
-            int lo = st_lo[sp], n = st_n[sp], ax = st_ax[sp];
-            if (n <= 1) continue;
-            S.axis = ax;
-            int split = n / 2;
-            qselect(perm + lo, n, split, S);
-            int nx = (ax + 1) % 3;
-            st_lo[sp] = lo + split;
-            st_n[sp] = n - split;
-            st_ax[sp] = nx;
-            sp++;
-            st_lo[sp] = lo;
-            st_n[sp] = split;
-            st_ax[sp] = nx;
-            sp++;
-        }
-        // leaf rank r <-> partitioned position m-1-r
-        for (int r = 0; r < m; r++) leaf_xyz[o + r] = cand_xyz[o + perm[m - 1 - r]];
-        for (int r = 0; r < m / 2; r++) {
-            int32_t x = perm[r], y = perm[m - 1 - r];
-            perm[r] = ca[y];
-            perm[m - 1 - r] = ca[x];
-        }
-        if (m & 1) perm[m / 2] = ca[perm[m / 2]];
+// exact replay: perm[0..m) receives the partitioned candidate positions
+__device__ __noinline__ void kd_exact(int32_t *perm, int m, const int32_t *ca, const double *xyz) {
+    for (int i = 0; i < m; i++) perm[i] = i;
+    KdSel S{ca, xyz, 0};
+    int st_lo[40], st_n[40], st_ax[40];
+    int sp = 1;
+    st_lo[0] = 0;
+    st_n[0] = m;
+    st_ax[0] = 0;
+    while (sp > 0) {
+        sp--;
+        int lo = st_lo[sp], n = st_n[sp], ax = st_ax[sp];
+        if (n <= 1) continue;
+        S.axis = ax;
+        int split = n / 2;
+        qselect(perm + lo, n, split, S);
+        int nx = (ax + 1) % 3;
+        st_lo[sp] = lo + split;
+        st_n[sp] = n - split;
+        st_ax[sp] = nx;
+        sp++;
+        st_lo[sp] = lo;
+        st_n[sp] = split;
+        st_ax[sp] = nx;
+        sp++;
     }
+}
+
+struct LeafWarp {
+    float v[3][LEAF_FAST_MAX];       // FP32 coordinates by candidate index
+    float cur[LEAF_FAST_MAX];        // current axis values in position order
+    uint16_t ord[2][LEAF_FAST_MAX];  // candidate index at each position
+    uint16_t seg_lo[LEAF_FAST_MAX];  // node (segment) of each position
+    uint16_t seg_n[LEAF_FAST_MAX];
+};
+
+__global__ void __launch_bounds__(LEAF_WARPS * 32)
+    k_leaf_order(ChunkView cv, int32_t n_sigs, const int32_t *count, const int64_t *offset,
+                 const int64_t *blk_offset, const int32_t *cand_atom, const float4 *cand_xyz,
+                 int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
+                 int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters) {
+    __shared__ LeafWarp sh[LEAF_WARPS];
+    const int lane = lane_id();
+    LeafWarp &L = sh[threadIdx.x >> 5];
+    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    int64_t total = (int64_t)cv.n_structures * n_sigs;
+    unsigned long long slow = 0;
+    for (int64_t w = warp; w < total; w += nwarps) {
+        const int m = count[w];
+        if (m <= 0) continue;
+        const int64_t o = offset[w];
+        const int32_t *ca = cand_atom + o;
+        bool exact = m > LEAF_FAST_MAX;
+        int src = 0;
+        if (!exact) {
+            for (int i = lane; i < m; i += 32) {
+                float4 p = cand_xyz[o + i];
+                L.v[0][i] = p.x;
+                L.v[1][i] = p.y;
+                L.v[2][i] = p.z;
+                L.cur[i] = p.x;
+                L.ord[0][i] = (uint16_t)i;
+                L.seg_lo[i] = 0;
+                L.seg_n[i] = (uint16_t)m;
+            }
+            __syncwarp();
+            int levels = 0;
+            while ((1 << levels) < m) levels++;
+            for (int d = 0; d < levels; d++) {
+                const uint16_t *A = L.ord[src];
+                uint16_t *B = L.ord[src ^ 1];
+                bool tie = false;
+                for (int p = lane; p < m; p += 32) {
+                    const int lo = L.seg_lo[p], n = L.seg_n[p];
+                    const int e = A[p];
+                    if (n <= 1) {
+                        B[p] = (uint16_t)e;
+                        continue;
+                    }
+                    const float x = L.cur[p];
+                    int less = 0, eq = 0, before = 0;
+#pragma unroll 4
+                    for (int q = lo; q < lo + n; q++) {
+                        const float y = L.cur[q];
+                        less += y < x;
+                        eq += y == x;
+                        before += (y < x) | ((y == x) & (q < p));
+                    }
+                    const int k = n / 2;
+                    if (less < k && less + eq > k) tie = true;
+                    B[lo + before] = (uint16_t)e;
+                }
+                __syncwarp();
+                if (__any_sync(FULL_MASK, tie)) {
+                    exact = true;
+                    break;
+                }
+                const int nax = (d + 1) % 3;
+                for (int p = lane; p < m; p += 32) {
+                    const int lo = L.seg_lo[p], n = L.seg_n[p];
+                    L.cur[p] = L.v[nax][B[p]];
+                    if (n <= 1) continue;
+                    const int k = n / 2;
+                    if (p < lo + k) {
+                        L.seg_n[p] = (uint16_t)k;
+                    } else {
+                        L.seg_lo[p] = (uint16_t)(lo + k);
+                        L.seg_n[p] = (uint16_t)(n - k);
+                    }
+                }
+                src ^= 1;
+                __syncwarp();
+            }
+        }
+        if (exact) {
+            // a tie at some median boundary (or a long list): the exact
+            // replay runs in k_leaf_exact, one thread per list
+            slow++;
+            if (lane == 0) exact_list[atomicAdd(exact_count, 1ull)] = w;
+            continue;
+        }
+        {
+            const uint16_t *A = L.ord[src];
+            for (int r = lane; r < m; r += 32) {
+                int e = A[m - 1 - r];
+                leaf_atom[o + r] = ca[e];
+                leaf_xyz[o + r] = cand_xyz[o + e];
+            }
+        }
+        __syncwarp();
+        // bounding boxes of blocks of 32 consecutive leaves
+        const int64_t bo = blk_offset[w];
+        for (int b = 0; b * 32 < m; b++) {
+            int r = b * 32 + lane;
+            float4 p = leaf_xyz[o + (r < m ? r : b * 32)];
+            float mnx = p.x, mny = p.y, mnz = p.z, mxx = p.x, mxy = p.y, mxz = p.z;
+            for (int off = 16; off; off >>= 1) {
+                mnx = fminf(mnx, __shfl_xor_sync(FULL_MASK, mnx, off));
+                mny = fminf(mny, __shfl_xor_sync(FULL_MASK, mny, off));
+                mnz = fminf(mnz, __shfl_xor_sync(FULL_MASK, mnz, off));
+                mxx = fmaxf(mxx, __shfl_xor_sync(FULL_MASK, mxx, off));
+                mxy = fmaxf(mxy, __shfl_xor_sync(FULL_MASK, mxy, off));
+                mxz = fmaxf(mxz, __shfl_xor_sync(FULL_MASK, mxz, off));
+            }
+            if (lane == 0) {
+                blk_lo[bo + b] = make_float4(mnx, mny, mnz, 0.f);
+                blk_hi[bo + b] = make_float4(mxx, mxy, mxz, 0.f);
+            }
+        }
+        __syncwarp();
+    }
+    if (lane == 0 && slow) atomicAdd(&counters[C_LEAF_EXACT], slow);
+}
+
+// Exact replay for the lists k_leaf_order could not order by ranks (a tie
+// at some median boundary, or a list too long for its shared buffer).
+//
+// One warp per list, the partitioned index array in shared memory.  Nodes
+// of more than 32 points are split by the literal qselect_r sequence of
+// median-of-3 pivots and Lomuto partitions, each partition computed by the
+// whole warp: the "<= pivot" elements keep their order (prefix counts), and
+// the ">" elements follow Lomuto's queue behaviour -- each ">" element is
+// appended, each later "<=" element rotates the queue's front to its back --
+// so every append is either a new element or a copy of append number r,
+// resolved by pointer jumping.  Subtrees of at most 32 points are then
+// handed one per lane and replayed sequentially.  Lists longer than
+// EXACT_MAX use the sequential replay on one thread.
+
+struct ExactShared {
+    uint16_t *A;      // partitioned candidate positions
+    double *key;      // axis value by candidate position (current node)
+    uint16_t *X;      // "<=" elements of the partition in order
+    uint16_t *VAL;    // queue appends (0xFFFF until resolved)
+    uint16_t *PTR;    // append -> earlier append it copies
+};
+
+__device__ int warp_partition(const ExactShared &S, int L0, int R0, int piv, unsigned long long *fallback) {
+    const int lane = lane_id();
+    const unsigned lt = (1u << lane) - 1u;
+    __syncwarp();
+    if (lane == 0) {
+        uint16_t t = S.A[R0];
+        S.A[R0] = S.A[piv];
+        S.A[piv] = t;
+    }
+    __syncwarp();
+    const uint16_t P = S.A[R0];
+    const double pv = S.key[P];
+    const int L = R0 - L0;
+    int cf = 0, cpush = 0, crot = 0, capp = 0;
+    for (int c0 = 0; c0 < L; c0 += 32) {
+        const int i = c0 + lane;
+        const bool valid = i < L;
+        uint16_t xi = 0;
+        bool f = false;
+        if (valid) {
+            xi = S.A[L0 + i];
+            f = S.key[xi] <= pv;
+        }
+        const unsigned mf = __ballot_sync(FULL_MASK, valid && f);
+        const unsigned mp = __ballot_sync(FULL_MASK, valid && !f);
+        const int push_before = cpush + __popc(mp & lt);
+        const bool is_push = valid && !f;
+        const bool is_rot = valid && f && push_before > 0;
+        const unsigned mr = __ballot_sync(FULL_MASK, is_rot);
+        const unsigned ma = mp | mr;
+        if (valid && f) S.X[cf + __popc(mf & lt)] = xi;
+        if (is_push || is_rot) {
+            const int k = capp + __popc(ma & lt);
+            if (is_push) {
+                S.VAL[k] = xi;
+                S.PTR[k] = (uint16_t)k;
+            } else {
+                S.VAL[k] = 0xFFFF;
+                S.PTR[k] = (uint16_t)(crot + __popc(mr & lt));
+            }
+        }
+        cf += __popc(mf);
+        cpush += __popc(mp);
+        crot += __popc(mr);
+        capp += __popc(ma);
+    }
+    __syncwarp();
+    // pointer jumping: at most log2(appends) + 1 rounds
+    for (int round = 0; round < 20; round++) {
+        bool open = false;
+        for (int k = lane; k < capp; k += 32) {
+            if (S.VAL[k] != 0xFFFF) continue;
+            const int p = S.PTR[k];
+            const uint16_t v = S.VAL[p];
+            if (v != 0xFFFF) S.VAL[k] = v;
+            else {
+                S.PTR[k] = S.PTR[p];
+                open = true;
+            }
+        }
+        __syncwarp();
+        if (!__any_sync(FULL_MASK, open)) break;
+        if (round == 19 && lane == 0) atomicAdd(fallback, 1ull);
+    }
+    const int C = cf, G = cpush, R = crot;
+    for (int i = lane; i < C; i += 32) S.A[L0 + i] = S.X[i];
+    if (G > 0) {
+        for (int j = 1 + lane; j < G; j += 32) S.A[L0 + C + j] = S.VAL[R + j];
+        if (lane == 0) S.A[R0] = S.VAL[R];
+    }
+    if (lane == 0) S.A[L0 + C] = P;
+    __syncwarp();
+    return L0 + C;
+}
+
+// sequential qselect_r on positions A[0..n) with their FP64 axis values in
+// K[0], K[32], ... (one lane's interleaved slice, kept aligned with A
+// through the swaps)
+__device__ void lane_qselect(uint16_t *A, double *Kb, int n, int k) {
+    auto K = [&](int i) -> double & { return Kb[32 * i]; };
+    int left = 0, right = n - 1;
+    for (;;) {
+        if (left == right) return;
+        int mid = (left + right + 1) / 2;
+        double l = K(left), r = K(right), m = K(mid);
+        int p;
+        if ((axis_cmp(l, m) > 0) != (axis_cmp(l, r) > 0)) p = left;
+        else if ((axis_cmp(m, l) < 0) != (axis_cmp(m, r) < 0)) p = mid;
+        else p = right;
+        uint16_t t = A[right];
+        A[right] = A[p];
+        A[p] = t;
+        double tk = K(right);
+        K(right) = K(p);
+        K(p) = tk;
+        double pv = K(right);
+        int store = left;
+        for (int i = left; i < right; i++) {
+            if (axis_cmp(K(i), pv) <= 0) {
+                uint16_t u = A[i];
+                A[i] = A[store];
+                A[store] = u;
+                double uk = K(i);
+                K(i) = K(store);
+                K(store) = uk;
+                store++;
+            }
+        }
+        t = A[store];
+        A[store] = A[right];
+        A[right] = t;
+        tk = K(store);
+        K(store) = K(right);
+        K(right) = tk;
+        if (store == k) return;
+        if (k < store) right = store - 1;
+        else left = store + 1;
+    }
+}
+
+// MAXN: longest list the instantiation keeps in shared memory; MINN: lists
+// at or below it are left to the smaller instantiation
+template <int MAXN, int MINN>
+__global__ void k_leaf_exact(ChunkView cv, int32_t n_sigs, const int32_t *count, const int64_t *offset,
+                             const int64_t *blk_offset, const int32_t *cand_atom, const float4 *cand_xyz,
+                             int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
+                             const int64_t *exact_list, const unsigned long long *exact_count,
+                             unsigned long long *counters) {
+    extern __shared__ __align__(16) unsigned char esm[];
+    const int lane = lane_id();
+    constexpr int SMEM = MAXN * (8 + 2 * 4);
+    static_assert(MAXN >= 1024, "the per-lane key slices need 8 KB");
+    unsigned char *base = esm + (size_t)(threadIdx.x >> 5) * SMEM;
+    ExactShared S;
+    S.key = reinterpret_cast<double *>(base);
+    S.A = reinterpret_cast<uint16_t *>(base + 8 * MAXN);
+    S.X = S.A + MAXN;
+    S.VAL = S.X + MAXN;
+    S.PTR = S.VAL + MAXN;
+    const int64_t total = (int64_t)*exact_count;
+    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = warp; i < total; i += nwarps) {
+        const int64_t w = exact_list[i];
+        const int m = count[w];
+        if (m <= MINN) continue;
+        const int s = (int)(w / n_sigs);
+        const int64_t o = offset[w];
+        const int32_t *ca = cand_atom + o;
+        const double *xyz = cv.xyz64 + 3 * cv.atom_base[s];
+        if (m > MAXN) {
+            // sequential replay on one lane, global scratch
+            int32_t *perm = leaf_atom + o;
+            if (lane == 0) kd_exact(perm, m, ca, xyz);
+            __syncwarp();
+            for (int r = lane; r < m; r += 32) leaf_xyz[o + r] = cand_xyz[o + perm[m - 1 - r]];
+            __syncwarp();
+            for (int r = lane; r < m / 2; r += 32) {
+                int32_t x = perm[r], y = perm[m - 1 - r];
+                perm[r] = ca[y];
+                perm[m - 1 - r] = ca[x];
+            }
+            if (lane == 0 && (m & 1)) perm[m / 2] = ca[perm[m / 2]];
+        } else {
+            for (int p = lane; p < m; p += 32) S.A[p] = (uint16_t)p;
+            __syncwarp();
+            // large nodes: depth-first stack of (lo, n, axis), lane-uniform
+            int st_lo[24], st_n[24], st_ax[24];
+            int sp = 1;
+            st_lo[0] = 0;
+            st_n[0] = m;
+            st_ax[0] = 0;
+            // small subtrees collected for the lanes: (lo, n, axis) packed
+            uint32_t small_mine[8];
+            int n_small_mine = 0, n_small = 0;
+            while (sp > 0) {
+                sp--;
+                const int lo = st_lo[sp], n = st_n[sp], ax = st_ax[sp];
+                if (n <= 1) continue;
+                if (n <= 32) {
+                    // lane (n_small % 32) replays this subtree later
+                    if ((n_small & 31) == lane && n_small_mine < 8)
+                        small_mine[n_small_mine++] = (uint32_t)lo | ((uint32_t)n << 16) | ((uint32_t)ax << 24);
+                    // children of nodes above 32 points have at least 16, so a
+                    // list of EXACT_MAX points has at most 256 such subtrees
+                    n_small++;
+                    continue;
+                }
+                for (int p = lane; p < n; p += 32) S.key[S.A[lo + p]] = xyz[3 * (int64_t)ca[S.A[lo + p]] + ax];
+                __syncwarp();
+                const int k = n / 2;
+                int left = 0, right = n - 1;
+                while (left != right) {
+                    const int L0 = lo + left, R0 = lo + right;
+                    const int mid = (L0 + R0 + 1) / 2;
+                    const double l = S.key[S.A[L0]], r = S.key[S.A[R0]], mm = S.key[S.A[mid]];
+                    int piv;
+                    if ((axis_cmp(l, mm) > 0) != (axis_cmp(l, r) > 0)) piv = L0;
+                    else if ((axis_cmp(mm, l) < 0) != (axis_cmp(mm, r) < 0)) piv = mid;
+                    else piv = R0;
+                    const int store = warp_partition(S, L0, R0, piv, &counters[C_ERROR]) - lo;
+                    if (store == k) break;
+                    if (k < store) right = store - 1;
+                    else left = store + 1;
+                }
+                const int nx = (ax + 1) % 3;
+                st_lo[sp] = lo + k;
+                st_n[sp] = n - k;
+                st_ax[sp] = nx;
+                sp++;
+                st_lo[sp] = lo;
+                st_n[sp] = k;
+                st_ax[sp] = nx;
+                sp++;
+            }
+            __syncwarp();
+            // small subtrees, one lane each: the sequential recursion, with
+            // the node's axis values staged in this lane's 32-slot slice of
+            // the (now free) key array
+            double *K = S.key + lane;  // element e of this lane's slice at K[32 e]
+            for (int q = 0; q < n_small_mine; q++) {
+                uint32_t v = small_mine[q];
+                int slo = v & 0xFFFF, sn = (v >> 16) & 0xFF, sax = v >> 24;
+                int ql[8], qn[8], qa[8];
+                int qs = 1;
+                ql[0] = slo;
+                qn[0] = sn;
+                qa[0] = sax;
+                while (qs > 0) {
+                    qs--;
+                    int lo = ql[qs], n = qn[qs], ax = qa[qs];
+                    if (n <= 1) continue;
+                    int k = n / 2;
+                    for (int e = 0; e < n; e++) K[32 * e] = xyz[3 * (int64_t)ca[S.A[lo + e]] + ax];
+                    lane_qselect(S.A + lo, K, n, k);
+                    int nx = (ax + 1) % 3;
+                    ql[qs] = lo + k;
+                    qn[qs] = n - k;
+                    qa[qs] = nx;
+                    qs++;
+                    ql[qs] = lo;
+                    qn[qs] = k;
+                    qa[qs] = nx;
+                    qs++;
+                }
+            }
+            __syncwarp();
+            if (n_small > 256 && lane == 0) atomicMax(&counters[C_ERROR], 4ull);
+            for (int r = lane; r < m; r += 32) {
+                int e = S.A[m - 1 - r];
+                leaf_atom[o + r] = ca[e];
+                leaf_xyz[o + r] = cand_xyz[o + e];
+            }
+        }
+        __syncwarp();
+        const int64_t bo = blk_offset[w];
+        for (int b = 0; b * 32 < m; b++) {
+            int r = b * 32 + lane;
+            float4 p = leaf_xyz[o + (r < m ? r : b * 32)];
+            float mnx = p.x, mny = p.y, mnz = p.z, mxx = p.x, mxy = p.y, mxz = p.z;
+            for (int off = 16; off; off >>= 1) {
+                mnx = fminf(mnx, __shfl_xor_sync(FULL_MASK, mnx, off));
+                mny = fminf(mny, __shfl_xor_sync(FULL_MASK, mny, off));
+                mnz = fminf(mnz, __shfl_xor_sync(FULL_MASK, mnz, off));
+                mxx = fmaxf(mxx, __shfl_xor_sync(FULL_MASK, mxx, off));
+                mxy = fmaxf(mxy, __shfl_xor_sync(FULL_MASK, mxy, off));
+                mxz = fmaxf(mxz, __shfl_xor_sync(FULL_MASK, mxz, off));
+            }
+            if (lane == 0) {
+                blk_lo[bo + b] = make_float4(mnx, mny, mnz, 0.f);
+                blk_hi[bo + b] = make_float4(mxx, mxy, mxz, 0.f);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void k_block_counts(int64_t n, const int32_t *count, int32_t *nblk) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) nblk[i] = (count[i] + 31) / 32;
 }
 
 // ---------------------------------------------------------------------------
@@ -583,14 +1004,25 @@ __device__ double lane_rmsd(int n, const int32_t *atoms, const double *xyz, cons
 // 179-195).  Its stream of complete assignments is ordered
 // lexicographically by (index in the level-0 list, kd leaf rank at level 1,
 // ..., kd leaf rank at level n-1).  Here each level keeps a tile of partial
-// assignments; a tile is expanded against the next level's list in
-// (parent, leaf rank) order with ballot + popc compaction, and a child
-// tile is fully processed before its parent tile continues (depth first
-// over tiles, breadth first inside a tile), which reproduces that order.
+// assignments (entries = position in the level's list + index of the
+// parent entry one level up); a tile is expanded against the next level's
+// list in (parent, leaf rank) order with ballot + popc compaction, and a
+// child tile is fully processed before its parent tile continues (depth
+// first over tiles, breadth first inside a tile), which reproduces that
+// order.
+//
+// Two expansion modes per level.  Block mode (lists of 32 or more): one
+// parent at a time; its chain of atoms, key bits and FP32 annulus bounds
+// sit in shared memory and are read by all lanes as broadcasts; the
+// parent's join box (intersection of its annulus boxes) culls whole blocks
+// of 32 consecutive leaves by their bounding boxes, and the 32 candidates
+// of each surviving block are tested by the 32 lanes.  Product mode (short
+// lists): lanes take consecutive (parent, candidate) positions of the
+// flattened product so small lists still fill the warp.
 
 struct PairState {
-    // per level
     int64_t lvl_off[32];
+    int64_t blk_off[32];
     int32_t lvl_cnt[32];
     int32_t tkey[32];
     int32_t order[32];
@@ -598,7 +1030,17 @@ struct PairState {
     int32_t cnt[32];
     int32_t par[32];
     int32_t cnd[32];
-    int32_t rowbase[32];
+    int32_t tile[32];
+    // chain of the parent being expanded in block mode
+    float4 cxyz[32];
+    float4 cthr[32];
+    int32_t cpos[32];
+};
+
+template <typename PosT>
+struct __align__(4) Entry {
+    PosT pos;
+    uint16_t parent;
 };
 
 // Exact FP64 annulus test of the reference (_Annulus_po,
@@ -626,8 +1068,8 @@ __device__ __forceinline__ bool annulus64(const double *c, const double *x, cons
 // point inside every annulus box is never pruned; for a point that passes
 // the annulus tests but lies outside B (possible only within rounding of a
 // box face) walk the implicit tree to its leaf as the reference would.
-__device__ bool kd_path_reaches(const int32_t *leaf_atom, int m, int rank, const double *xyz,
-                                const double *Bmin, const double *Bmax) {
+__device__ __noinline__ bool kd_path_reaches(const int32_t *leaf_atom, int m, int rank, const double *xyz,
+                                             const double *Bmin, const double *Bmax) {
     int q = m - 1 - rank;
     int lo = 0, hi = m;
     while (hi - lo > 1) {
@@ -664,18 +1106,49 @@ __device__ __forceinline__ bool check_pair(int32_t kj, int32_t kn, int32_t tj, i
     return true;
 }
 
-template <typename RowT, bool FP32>
+// FP64 decision for one candidate whose FP32 test was inconclusive against
+// at least one chain atom (`exact_mask`), or for every chain atom in FP64
+// mode: the reference's annulus arithmetic, then the kd path check when the
+// point lies outside an annulus box.
+__device__ __noinline__ bool decide_fp64(unsigned exact_mask, int lev, const int32_t *atoms, int32_t an,
+                                         const double *xyz, const AnnulusParam *prm, const int32_t *order,
+                                         int n, int qn, const int32_t *leaf_atom_list, int mc, int cr) {
+    bool need_path = false;
+    const double *x = xyz + 3 * (int64_t)an;
+    for (int j = 0; j <= lev; j++) {
+        if (!((exact_mask >> j) & 1u)) continue;
+        bool inb;
+        if (!annulus64(xyz + 3 * (int64_t)atoms[j], x, prm[order[j] * n + qn], &inb)) return false;
+        if (!inb) need_path = true;
+    }
+    if (!need_path) return true;
+    double Bmin[3] = {-INFINITY, -INFINITY, -INFINITY};
+    double Bmax[3] = {INFINITY, INFINITY, INFINITY};
+    for (int j = 0; j <= lev; j++) {
+        const double *cj = xyz + 3 * (int64_t)atoms[j];
+        double bj = prm[order[j] * n + qn].b;
+        for (int i = 0; i < 3; i++) {
+            double lo = __dsub_rn(cj[i], bj), hi = __dadd_rn(cj[i], bj);
+            Bmin[i] = Bmin[i] > lo ? Bmin[i] : lo;
+            Bmax[i] = Bmax[i] < hi ? Bmax[i] : hi;
+        }
+    }
+    return kd_path_reaches(leaf_atom_list, mc, cr, xyz, Bmin, Bmax);
+}
+
+template <typename PosT, bool FP32>
 __global__ void __launch_bounds__(SEARCH_WARPS * 32)
     k_search(ChunkView cv, TemplateView tv, CandView cd, SearchArgs sa, int32_t *pair_counter,
              const int32_t *scanned, CompleteRows out, unsigned long long *counters) {
     extern __shared__ __align__(16) unsigned char smem[];
+    using E = Entry<PosT>;
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
     unsigned char *wbase = smem + (size_t)wib * sa.warp_smem;
     PairState &st = *reinterpret_cast<PairState *>(wbase);
     const size_t o2 = (sizeof(PairState) + 15) & ~size_t(15);
-    RowT *rows = reinterpret_cast<RowT *>(wbase + o2);
-    const int64_t row_units = (int64_t)(sa.warp_smem - o2) / (int64_t)sizeof(RowT);
+    E *tiles = reinterpret_cast<E *>(wbase + o2);
+    const int64_t tile_units = (int64_t)(sa.warp_smem - o2) / (int64_t)sizeof(E);
     const int T = tv.n_templates;
     const int G = cd.n_sigs;
     // wall-time budget: every warp stops taking work, and stops the pair it
@@ -711,10 +1184,9 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
 
         // ---- candidate-list lengths, empty-set skip, statistics
         int k = lane;
-        int64_t lw = 0;
         int c = INT_MAX, sc = 0;
         if (k < n) {
-            lw = (int64_t)s * G + tv.sig[ab + k];
+            int64_t lw = (int64_t)s * G + tv.sig[ab + k];
             c = cd.count[lw];
             sc = scanned[lw];
         }
@@ -748,44 +1220,89 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
                 if (cj < c || (cj == c && j < k)) rank++;
             }
         }
+        __syncwarp();
         if (k < n) st.order[rank] = k;
         __syncwarp();
+        // tile capacity: equal entry count for levels 0..n-2
+        int cap = n >= 2 ? (int)min((int64_t)4096, tile_units / (n - 1)) : 0;
         if (lane < n) {
             int tk = st.order[lane];
             int64_t w2 = (int64_t)s * G + tv.sig[ab + tk];
             st.lvl_off[lane] = cd.offset[w2];
+            st.blk_off[lane] = cd.blk_offset[w2];
             st.lvl_cnt[lane] = cd.count[w2];
             st.tkey[lane] = tv.key[ab + tk];
             st.F[lane] = 0;
             st.cnt[lane] = 0;
             st.par[lane] = 0;
             st.cnd[lane] = 0;
+            st.tile[lane] = cap * lane;
         }
-        // annulus parameters of template atoms (p, q): prm[p * n + q]
-        const AnnulusParam *prm = tv.params + tv.param_begin[t];
-        // tile capacity: equal row count for levels 0..n-2
-        int cap = 0;
-        if (n >= 2) {
-            int64_t units = (int64_t)(n - 1) * n / 2;
-            int64_t c2 = row_units / units;
-            cap = (int)(c2 > 4096 ? 4096 : c2);
-        }
-        if (lane < n) st.rowbase[lane] = cap * (lane * (lane + 1) / 2);
         __syncwarp();
-        if (n >= 2 && cap < 1) {
+        if (n >= 2 && cap < 32) {
             if (lane == 0) atomicMax(&counters[C_ERROR], 2ull);
             continue;
         }
+        // annulus parameters of template atoms (p, q): prm[p * n + q]
+        const AnnulusParam *prm = tv.params + tv.param_begin[t];
 
         int64_t emitted = 0;
         unsigned long long rechecks = 0;
         const int m0 = st.lvl_cnt[0];
         const int64_t off0 = st.lvl_off[0];
 
-        // emit complete rows: `pass` lanes with their level positions
-        auto emit = [&](bool pass, const RowT *prow, int lastpos, double rm) -> void {
+        // atom of level j at list position pos
+        auto level_atom = [&](int j, int pos) -> int32_t {
+            return j == 0 ? cd.cand_atom[off0 + pos] : cd.leaf_atom[st.lvl_off[j] + pos];
+        };
+        auto level_xyz = [&](int j, int pos) -> float4 {
+            return j == 0 ? cd.cand_xyz[off0 + pos] : cd.leaf_xyz[st.lvl_off[j] + pos];
+        };
+
+        bool stop = false;
+        int64_t cut_base = 0;
+        const int64_t stop_at = (sa.best_match && sa.max_candidates >= 0) ? (int64_t)sa.max_candidates + 2 : -1;
+
+        // emit complete rows: lanes with `pass`, level positions in pos[]
+        // (levels 0..n-2) and the last level's position `lastpos`
+        auto emit = [&](bool pass, const int32_t *pos, int lastpos) -> void {
             unsigned m = __ballot_sync(FULL_MASK, pass);
             if (!m) return;
+            double rm = 0.0;
+            int32_t at[32];
+            if (pass) {
+                for (int j = 0; j < n - 1; j++) at[st.order[j]] = level_atom(j, pos[j]);
+                at[st.order[n - 1]] = level_atom(n - 1, lastpos);
+            }
+            if (sa.cut_inline) {
+                // Query.__next__'s max_candidates cut, applied while
+                // searching: the candidate whose distance from the last hit
+                // (or the template start) reaches M+1 ends the template's
+                // stream after it has been considered
+                bool hitf = false;
+                if (pass) {
+                    rm = lane_rmsd(n, at, xyz64, tv.pos + 3 * (int64_t)ab);
+                    hitf = rm <= sa.rmsd_threshold && n >= 3;
+                }
+                unsigned hl = __ballot_sync(FULL_MASK, hitf);
+                unsigned mm = m;
+                int r = 0, keep = 32;
+                while (mm) {
+                    int ln = __ffs(mm) - 1;
+                    mm &= mm - 1;
+                    int64_t q = emitted + r;
+                    if (q - cut_base == (int64_t)sa.max_candidates + 1) {
+                        keep = r;
+                        stop = true;
+                        break;
+                    }
+                    if ((hl >> ln) & 1u) cut_base = q + 1;
+                    r++;
+                }
+                int myrank = __popc(m & ((1u << lane) - 1u));
+                pass = pass && myrank <= keep;
+                m = __ballot_sync(FULL_MASK, pass);
+            }
             int np = __popc(m);
             int64_t base = 0;
             if (lane == 0) base = (int64_t)atomicAdd(out.count, (unsigned long long)np);
@@ -795,49 +1312,44 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
                 int64_t ri = base + rk;
                 if (ri < out.capacity) {
                     int32_t *dst = out.atoms + ri * out.stride;
-                    for (int j = 0; j < n - 1; j++) {
-                        int pos = (int)prow[j];
-                        int32_t at = (j == 0) ? cd.cand_atom[off0 + pos] : cd.leaf_atom[st.lvl_off[j] + pos];
-                        dst[st.order[j]] = at;
-                    }
-                    int32_t at = (n == 1) ? cd.cand_atom[off0 + lastpos]
-                                          : cd.leaf_atom[st.lvl_off[n - 1] + lastpos];
-                    dst[st.order[n - 1]] = at;
+                    for (int j = 0; j < n; j++) dst[j] = at[j];
                     out.pair[ri] = pair;
                     out.ordinal[ri] = emitted + rk;
                     if (out.rmsd) out.rmsd[ri] = rm;
                 }
             }
             emitted += np;
+            if (stop_at >= 0 && emitted >= stop_at) stop = true;
         };
-
-        bool stop = false;
-        int64_t cut_base = 0;
-        const int64_t stop_at = (sa.best_match && sa.max_candidates >= 0) ? (int64_t)sa.max_candidates + 2 : -1;
 
         if (n == 1) {
             // Scanner_next with one level advances the seed index before
             // reporting (patches/Scanner.c.patch:244-263): seeds 1..m0-1
             for (int b = 1; b < m0 && !stop; b += 32) {
                 int p = b + lane;
-                emit(p < m0, nullptr, p, 0.0);
-                if (stop_at >= 0 && emitted >= stop_at) stop = true;
+                emit(p < m0, nullptr, p);
                 if (over_budget()) stop = true;
             }
-            if (lane == 0) {
-                st.F[0] = m0;
-            }
+            if (lane == 0) st.F[0] = m0;
         } else {
             int root = 0;
             int lev = -1;
+            int chain_lev = -1, chain_par = -1;
+            float box_lo[3], box_hi[3];
             while (!stop) {
                 if (over_budget()) break;
                 if (lev < 0) {
                     if (root >= m0) break;
                     int kk = min(cap, m0 - root);
-                    RowT *r0 = rows + st.rowbase[0];
-                    for (int i = lane; i < kk; i += 32) r0[i] = (RowT)(root + i);
+                    E *t0 = tiles + st.tile[0];
+                    for (int i = lane; i < kk; i += 32) {
+                        E e;
+                        e.pos = (PosT)(root + i);
+                        e.parent = 0;
+                        t0[i] = e;
+                    }
                     root += kk;
+                    __syncwarp();
                     if (lane == 0) {
                         st.F[0] += kk;
                         st.cnt[0] = kk;
@@ -846,98 +1358,210 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
                     }
                     __syncwarp();
                     lev = 0;
+                    chain_lev = -1;
                     continue;
                 }
+                const int child = lev + 1;
+                const bool last = (child == n - 1);
                 const int pcnt = st.cnt[lev];
-                int ppar = st.par[lev];
+                const int ppar = st.par[lev];
+                const int ccnt = last ? 0 : st.cnt[child];
                 if (ppar >= pcnt) {
                     __syncwarp();
+                    if (!last && ccnt > 0) {
+                        if (lane == 0) {
+                            st.par[child] = 0;
+                            st.cnd[child] = 0;
+                        }
+                        __syncwarp();
+                        lev = child;
+                        continue;
+                    }
                     if (lane == 0) st.cnt[lev] = 0;
                     __syncwarp();
                     lev--;
                     continue;
                 }
-                const int child = lev + 1;
                 const int mc = st.lvl_cnt[child];
-                const bool last = (child == n - 1);
-                int ccnt = last ? 0 : st.cnt[child];
-                int batch = last ? 32 : min(32, cap - ccnt);
-                if (batch <= 0) {
-                    __syncwarp();
-                    if (lane == 0) {
-                        st.par[child] = 0;
-                        st.cnd[child] = 0;
-                    }
-                    __syncwarp();
-                    lev = child;
-                    continue;
-                }
-                // lane -> (parent p, candidate rank cr)
-                int pcnd = st.cnd[lev];
-                int tt = pcnd + lane;
-                int p = ppar + tt / mc;
-                int cr = tt % mc;
-                bool valid = lane < batch && p < pcnt;
+                const int qn = st.order[child];
+                const int32_t tn = st.tkey[child];
+                const int64_t coff = st.lvl_off[child];
+                const E *ptile = tiles + st.tile[lev];
+                E *ctile = tiles + st.tile[child];
                 bool pass = false;
-                const RowT *prow = rows + st.rowbase[lev] + (int64_t)p * (lev + 1);
-                if (valid) {
-                    const int64_t coff = st.lvl_off[child];
-                    float4 xc = cd.leaf_xyz[coff + cr];
-                    int32_t kn = __float_as_int(xc.w);
-                    int32_t tn = st.tkey[child];
-                    const int qn = st.order[child];
-                    pass = true;
-                    bool need_path = false;
-                    for (int j = 0; j <= lev && pass; j++) {
-                        int pos = (int)prow[j];
-                        float4 xj = (j == 0) ? cd.cand_xyz[off0 + pos] : cd.leaf_xyz[st.lvl_off[j] + pos];
-                        if (!check_pair(__float_as_int(xj.w), kn, st.tkey[j], tn, sa.ignore_chain)) {
-                            pass = false;
+                int cr = 0;
+                int my_parent = 0;      // product mode: this lane's parent entry
+                int32_t chainpos[32];   // product mode: this lane's parent chain
+                if (mc >= 32) {
+                    // ---------------- block mode ----------------
+                    if (!last && cap - ccnt < 32) {
+                        __syncwarp();
+                        if (lane == 0) {
+                            st.par[child] = 0;
+                            st.cnd[child] = 0;
+                        }
+                        __syncwarp();
+                        lev = child;
+                        continue;
+                    }
+                    if (chain_lev != lev || chain_par != ppar) {
+                        // positions of the parent's chain, by walking the tiles
+                        __syncwarp();
+                        if (lane == 0) {
+                            int idx = ppar;
+                            for (int j = lev; j >= 0; j--) {
+                                E e = tiles[st.tile[j] + idx];
+                                st.cpos[j] = (int)e.pos;
+                                idx = e.parent;
+                            }
+                        }
+                        __syncwarp();
+                        float lo[3] = {-INFINITY, -INFINITY, -INFINITY}, hi[3] = {INFINITY, INFINITY, INFINITY};
+                        if (lane <= lev) {
+                            float4 cj = level_xyz(lane, st.cpos[lane]);
+                            float4 th = prm[st.order[lane] * n + qn].thr;
+                            st.cxyz[lane] = cj;
+                            st.cthr[lane] = th;
+                            float rb = sqrtf(fmaxf(th.w, 0.f)) * 1.000001f + 1e-3f;
+                            lo[0] = cj.x - rb;
+                            lo[1] = cj.y - rb;
+                            lo[2] = cj.z - rb;
+                            hi[0] = cj.x + rb;
+                            hi[1] = cj.y + rb;
+                            hi[2] = cj.z + rb;
+                        }
+                        for (int i = 0; i < 3; i++) {
+                            for (int off = 16; off; off >>= 1) {
+                                lo[i] = fmaxf(lo[i], __shfl_xor_sync(FULL_MASK, lo[i], off));
+                                hi[i] = fminf(hi[i], __shfl_xor_sync(FULL_MASK, hi[i], off));
+                            }
+                            box_lo[i] = lo[i];
+                            box_hi[i] = hi[i];
+                        }
+                        chain_lev = lev;
+                        chain_par = ppar;
+                        __syncwarp();
+                    }
+                    // next block >= cursor whose bounding box meets the join box
+                    const int nblk = (mc + 31) >> 5;
+                    int found = -1;
+                    for (int g0 = st.cnd[lev]; g0 < nblk; g0 += 32) {
+                        int b = g0 + lane;
+                        bool hit = false;
+                        if (b < nblk) {
+                            float4 bl = cd.blk_lo[st.blk_off[child] + b];
+                            float4 bh = cd.blk_hi[st.blk_off[child] + b];
+                            hit = !(bl.x > box_hi[0] || bh.x < box_lo[0] || bl.y > box_hi[1] || bh.y < box_lo[1] ||
+                                    bl.z > box_hi[2] || bh.z < box_lo[2]);
+                        }
+                        unsigned hm = __ballot_sync(FULL_MASK, hit);
+                        if (hm) {
+                            found = g0 + __ffs(hm) - 1;
                             break;
                         }
-                        const AnnulusParam &PA = prm[st.order[j] * n + qn];
-                        bool exact = !FP32;
-                        if (FP32) {
-                            float dx = xj.x - xc.x, dy = xj.y - xc.y, dz = xj.z - xc.z;
-                            float d2 = dx * dx + dy * dy + dz * dz;
-                            float4 th = PA.thr;
-                            if (d2 < th.x || d2 > th.w) {
-                                pass = false;
-                                break;
-                            }
-                            if (!(d2 >= th.y && d2 <= th.z)) exact = true;
-                        }
-                        if (exact) {
-                            if (FP32) rechecks++;
-                            int32_t aj = (j == 0) ? cd.cand_atom[off0 + pos] : cd.leaf_atom[st.lvl_off[j] + pos];
-                            int32_t an = cd.leaf_atom[coff + cr];
-                            bool inb;
-                            if (!annulus64(xyz64 + 3 * (int64_t)aj, xyz64 + 3 * (int64_t)an, PA, &inb)) {
-                                pass = false;
-                                break;
-                            }
-                            if (!inb) need_path = true;
-                        }
                     }
-                    if (pass && need_path) {
-                        double Bmin[3] = {-INFINITY, -INFINITY, -INFINITY};
-                        double Bmax[3] = {INFINITY, INFINITY, INFINITY};
+                    __syncwarp();
+                    if (found < 0) {
+                        if (lane == 0) {
+                            st.par[lev] = ppar + 1;
+                            st.cnd[lev] = 0;
+                        }
+                        __syncwarp();
+                        continue;
+                    }
+                    cr = found * 32 + lane;
+                    if (cr < mc) {
+                        float4 xc = cd.leaf_xyz[coff + cr];
+                        int32_t kn = __float_as_int(xc.w);
+                        pass = true;
+                        unsigned exact = 0;
                         for (int j = 0; j <= lev; j++) {
-                            int pos = (int)prow[j];
-                            int32_t aj = (j == 0) ? cd.cand_atom[off0 + pos] : cd.leaf_atom[st.lvl_off[j] + pos];
-                            const double *cj = xyz64 + 3 * (int64_t)aj;
-                            double bj = prm[st.order[j] * n + qn].b;
-                            for (int i = 0; i < 3; i++) {
-                                double lo = __dsub_rn(cj[i], bj), hi = __dadd_rn(cj[i], bj);
-                                Bmin[i] = Bmin[i] > lo ? Bmin[i] : lo;
-                                Bmax[i] = Bmax[i] < hi ? Bmax[i] : hi;
+                            float4 xj = st.cxyz[j];
+                            if (!check_pair(__float_as_int(xj.w), kn, st.tkey[j], tn, sa.ignore_chain)) {
+                                pass = false;
+                                break;
+                            }
+                            if (FP32) {
+                                float dx = xj.x - xc.x, dy = xj.y - xc.y, dz = xj.z - xc.z;
+                                float d2 = dx * dx + dy * dy + dz * dz;
+                                float4 th = st.cthr[j];
+                                if (d2 < th.x || d2 > th.w) {
+                                    pass = false;
+                                    break;
+                                }
+                                if (!(d2 >= th.y && d2 <= th.z)) exact |= 1u << j;
+                            } else {
+                                exact |= 1u << j;
                             }
                         }
-                        pass = kd_path_reaches(cd.leaf_atom + coff, mc, cr, xyz64, Bmin, Bmax);
+                        if (pass && exact) {
+                            if (FP32) rechecks += __popc(exact);
+                            int32_t atoms[32];
+                            for (int j = 0; j <= lev; j++) atoms[j] = level_atom(j, st.cpos[j]);
+                            pass = decide_fp64(exact, lev, atoms, cd.leaf_atom[coff + cr], xyz64, prm, st.order, n,
+                                               qn, cd.leaf_atom + coff, mc, cr);
+                        }
                     }
-                }
-                // advance the parent cursor by `batch` product positions
-                {
+                    __syncwarp();
+                    if (lane == 0) st.cnd[lev] = found + 1;
+                    __syncwarp();
+                } else {
+                    // ---------------- product mode ----------------
+                    int batch = last ? 32 : min(32, cap - ccnt);
+                    if (batch <= 0) {
+                        __syncwarp();
+                        if (lane == 0) {
+                            st.par[child] = 0;
+                            st.cnd[child] = 0;
+                        }
+                        __syncwarp();
+                        lev = child;
+                        continue;
+                    }
+                    const int pcnd = st.cnd[lev];
+                    const int tt = pcnd + lane;
+                    const int p = ppar + tt / mc;
+                    cr = tt % mc;
+                    const bool valid = lane < batch && p < pcnt;
+                    if (valid) {
+                        int idx = p;
+                        for (int j = lev; j >= 0; j--) {
+                            E e = tiles[st.tile[j] + idx];
+                            chainpos[j] = (int)e.pos;
+                            idx = e.parent;
+                        }
+                        float4 xc = cd.leaf_xyz[coff + cr];
+                        int32_t kn = __float_as_int(xc.w);
+                        pass = true;
+                        unsigned exact = 0;
+                        for (int j = 0; j <= lev; j++) {
+                            float4 xj = level_xyz(j, chainpos[j]);
+                            if (!check_pair(__float_as_int(xj.w), kn, st.tkey[j], tn, sa.ignore_chain)) {
+                                pass = false;
+                                break;
+                            }
+                            if (FP32) {
+                                float dx = xj.x - xc.x, dy = xj.y - xc.y, dz = xj.z - xc.z;
+                                float d2 = dx * dx + dy * dy + dz * dz;
+                                float4 th = prm[st.order[j] * n + qn].thr;
+                                if (d2 < th.x || d2 > th.w) {
+                                    pass = false;
+                                    break;
+                                }
+                                if (!(d2 >= th.y && d2 <= th.z)) exact |= 1u << j;
+                            } else {
+                                exact |= 1u << j;
+                            }
+                        }
+                        if (pass && exact) {
+                            if (FP32) rechecks += __popc(exact);
+                            int32_t atoms[32];
+                            for (int j = 0; j <= lev; j++) atoms[j] = level_atom(j, chainpos[j]);
+                            pass = decide_fp64(exact, lev, atoms, cd.leaf_atom[coff + cr], xyz64, prm, st.order, n,
+                                               qn, cd.leaf_atom + coff, mc, cr);
+                        }
+                    }
+                    // advance the parent cursor by `batch` product positions
                     int nt = pcnd + batch;
                     int np2 = ppar + nt / mc;
                     int nc2 = nt % mc;
@@ -950,58 +1574,31 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
                         st.par[lev] = np2;
                         st.cnd[lev] = nc2;
                     }
-                    ppar = np2;
+                    __syncwarp();
+                    my_parent = p;
                 }
+                // ---- children / complete rows
+                const bool block_mode = mc >= 32;
+                unsigned m = __ballot_sync(FULL_MASK, pass);
                 if (last) {
-                    unsigned m = __ballot_sync(FULL_MASK, pass);
-                    double rm = 0.0;
-                    if (sa.cut_inline && m) {
-                        // Query.__next__'s max_candidates cut, applied while
-                        // searching: the candidate whose distance from the last
-                        // hit (or the template start) reaches M+1 ends the
-                        // template's stream after it has been considered
-                        bool hitf = false;
-                        if (pass) {
-                            int32_t at[32];
-                            for (int j = 0; j < n - 1; j++) {
-                                int pos = (int)prow[j];
-                                at[st.order[j]] = (j == 0) ? cd.cand_atom[off0 + pos] : cd.leaf_atom[st.lvl_off[j] + pos];
-                            }
-                            at[st.order[n - 1]] = cd.leaf_atom[st.lvl_off[n - 1] + cr];
-                            rm = lane_rmsd(n, at, xyz64, tv.pos + 3 * (int64_t)ab);
-                            hitf = rm <= sa.rmsd_threshold && n >= 3;
-                        }
-                        unsigned hl = __ballot_sync(FULL_MASK, hitf);
-                        unsigned mm = m;
-                        int r = 0, keep = 32;
-                        while (mm) {
-                            int ln = __ffs(mm) - 1;
-                            mm &= mm - 1;
-                            int64_t q = emitted + r;
-                            if (q - cut_base == (int64_t)sa.max_candidates + 1) {
-                                keep = r;
-                                stop = true;
-                                break;
-                            }
-                            if ((hl >> ln) & 1u) cut_base = q + 1;
-                            r++;
-                        }
-                        int myrank = __popc(m & ((1u << lane) - 1u));
-                        pass = pass && myrank <= keep;
-                        m = __ballot_sync(FULL_MASK, pass);
+                    if (block_mode) {
+                        int32_t pos[32];
+                        for (int j = 0; j <= lev; j++) pos[j] = st.cpos[j];
+                        emit(pass, pos, cr);
+                    } else {
+                        emit(pass, chainpos, cr);
                     }
-                    emit(pass, prow, cr, rm);
                     __syncwarp();
                     if (lane == 0) st.F[child] += __popc(m);
-                    if (stop_at >= 0 && emitted >= stop_at) stop = true;
                     __syncwarp();
+                    if (!block_mode) chain_lev = -1;
                 } else {
-                    unsigned m = __ballot_sync(FULL_MASK, pass);
                     if (pass) {
                         int ci = ccnt + __popc(m & ((1u << lane) - 1u));
-                        RowT *crow = rows + st.rowbase[child] + (int64_t)ci * (child + 1);
-                        for (int j = 0; j <= lev; j++) crow[j] = prow[j];
-                        crow[child] = (RowT)cr;
+                        E e;
+                        e.pos = (PosT)cr;
+                        e.parent = (uint16_t)(block_mode ? ppar : my_parent);
+                        ctile[ci] = e;
                     }
                     int ncnt = ccnt + __popc(m);
                     __syncwarp();
@@ -1010,8 +1607,18 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
                         st.F[child] += __popc(m);
                     }
                     __syncwarp();
-                    bool parent_done = ppar >= pcnt;
-                    if (ncnt > 0 && (cap - ncnt < min(32, cap) || parent_done)) {
+                    if (!block_mode) {
+                        chain_lev = -1;
+                        bool parent_done = st.par[lev] >= pcnt;
+                        if (ncnt > 0 && (cap - ncnt < 32 || parent_done)) {
+                            if (lane == 0) {
+                                st.par[child] = 0;
+                                st.cnd[child] = 0;
+                            }
+                            __syncwarp();
+                            lev = child;
+                        }
+                    } else if (cap - ncnt < 32) {
                         if (lane == 0) {
                             st.par[child] = 0;
                             st.cnd[child] = 0;
@@ -1141,9 +1748,33 @@ void launch_scan_add(cudaStream_t st, int64_t *out, int64_t n, const int64_t *ti
 }
 
 void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t n_sigs, const int32_t *count,
-                       const int64_t *offset, const int32_t *cand_atom, const float4 *cand_xyz,
-                       int32_t *leaf_atom, float4 *leaf_xyz) {
-    k_leaf_order<<<blocks, 128, 0, st>>>(cv, n_sigs, count, offset, cand_atom, cand_xyz, leaf_atom, leaf_xyz);
+                       const int64_t *offset, const int64_t *blk_offset, const int32_t *cand_atom,
+                       const float4 *cand_xyz, int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
+                       int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters) {
+    cudaMemsetAsync(exact_count, 0, sizeof(unsigned long long), st);
+    k_leaf_order<<<blocks, LEAF_WARPS * 32, 0, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, cand_xyz,
+                                                    leaf_atom, leaf_xyz, blk_lo, blk_hi, exact_list, exact_count,
+                                                    counters);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // lists up to 1024 entries: 16 KB a warp, 4 warps a block
+    constexpr int SM1 = 1024 * 16 * 4;
+    cudaFuncSetAttribute(k_leaf_exact<1024, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM1);
+    k_leaf_exact<1024, 0><<<sms * 3, 128, SM1, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, cand_xyz,
+                                                    leaf_atom, leaf_xyz, blk_lo, blk_hi, exact_list, exact_count,
+                                                    counters);
+    // longer lists: 64 KB a warp, one warp a block (beyond EXACT_MAX: one
+    // thread replays the list from global memory)
+    constexpr int SM2 = EXACT_MAX * 16;
+    cudaFuncSetAttribute(k_leaf_exact<EXACT_MAX, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM2);
+    k_leaf_exact<EXACT_MAX, 1024><<<sms * 3, 32, SM2, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom,
+                                                           cand_xyz, leaf_atom, leaf_xyz, blk_lo, blk_hi,
+                                                           exact_list, exact_count, counters);
+}
+
+void launch_block_counts(cudaStream_t st, int64_t n, const int32_t *count, int32_t *nblk) {
+    if (n > 0) k_block_counts<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, count, nblk);
 }
 
 template <typename RowT, bool FP32>
@@ -1153,6 +1784,13 @@ static cudaError_t search_variant(cudaStream_t st, int grid, const ChunkView &cv
     size_t smem = (size_t)sa.warp_smem * SEARCH_WARPS;
     cudaError_t e = cudaFuncSetAttribute(k_search<RowT, FP32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    // persistent grid: as many blocks as can be resident at once
+    int per_sm = 0, dev = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<RowT, FP32>, SEARCH_WARPS * 32, smem);
+    if (e != cudaSuccess) return e;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (per_sm > 0 && sms > 0) grid = per_sm * sms;
     k_search<RowT, FP32><<<grid, SEARCH_WARPS * 32, smem, st>>>(cv, tv, cd, sa, pair_counter, scanned, out, counters);
     return cudaGetLastError();
 }

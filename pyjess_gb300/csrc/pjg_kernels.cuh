@@ -9,7 +9,10 @@
 
 namespace pjg {
 
-constexpr int SEARCH_WARPS = 4;        // warps per block of k_search
+constexpr int SEARCH_WARPS = 8;        // warps per block of k_search
+constexpr int LEAF_WARPS = 4;          // warps per block of k_leaf_order (shared memory: 8.5 KB a warp)
+constexpr int LEAF_FAST_MAX = 384;     // longest list ordered in shared memory
+constexpr int EXACT_MAX = 4096;        // longest list replayed warp-parallel
 
 struct SearchArgs {
     int32_t n_pairs;                   // chunk structures x templates
@@ -72,8 +75,12 @@ void launch_scan_tiles_i64(cudaStream_t st, const int64_t *in, int64_t n, int64_
 void launch_scan_add(cudaStream_t st, int64_t *out, int64_t n, const int64_t *tile_offsets);
 
 void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t n_sigs, const int32_t *count,
-                       const int64_t *offset, const int32_t *cand_atom, const float4 *cand_xyz,
-                       int32_t *leaf_atom, float4 *leaf_xyz);
+                       const int64_t *offset, const int64_t *blk_offset, const int32_t *cand_atom,
+                       const float4 *cand_xyz, int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
+                       int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters);
+
+// blocks of 32 leaves per list: ceil(count / 32)
+void launch_block_counts(cudaStream_t st, int64_t n, const int32_t *count, int32_t *nblk);
 
 // k_search variant: wide = 32-bit frontier entries (structures above 65535
 // atoms), fp32 = guarded FP32 distance tests (else exact FP64 throughout)
