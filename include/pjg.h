@@ -216,6 +216,35 @@ pjg_status pjg_results_stats(const pjg_results *r, pjg_stats *stats);
 
 void pjg_results_destroy(pjg_results *r);
 
+/* Allocation-free superposition --------------------------------------------
+ *
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they run (work recorded into a CUDA graph, real-time loops
+ * that must not block on the allocator, applications whose memory manager
+ * owns every device allocation).  It superposes n_rows candidate assignments
+ * of one template: row r's molecule atoms are mol_xyz[(r*n_atoms + k)*3 + d],
+ * the template's atoms tpl_xyz[3k + d] (k = template atom, 1 <= n_atoms <=
+ * 32), all device pointers.  It writes, per row, rmsd[r], rotation[9r..]
+ * (row major, molecule -> template) and centres[6r..] (molecule centroid,
+ * template centroid), then pass_rows[0 .. *pass_count) = the rows with
+ * rmsd <= rmsd_threshold (and a defined rotation, n_atoms >= 3) in row order.
+ * Kernels are enqueued on `stream` (a cudaStream_t, NULL for the default
+ * stream); the call returns without waiting.
+ *
+ * It allocates nothing: its scratch is a static device array of
+ * PJG_NOALLOC_MAX_ROWS (2^20) row flags (4 MiB) that every GPU loading the
+ * library keeps until the process exits.  More rows than that, or a bad
+ * argument, return PJG_ERR_INVALID with a message from
+ * pjg_noalloc_last_error().  The first call on each device looks up that
+ * array's device address with the device current; make that first call
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race, so serialise them. */
+#define PJG_NOALLOC_MAX_ROWS (1 << 20)
+pjg_status pjg_superpose_noalloc(const double *mol_xyz, const double *tpl_xyz, int32_t n_rows, int32_t n_atoms,
+                                 double rmsd_threshold, double *rmsd, double *rotation, double *centres,
+                                 int32_t *pass_rows, int32_t *pass_count, void *stream);
+const char *pjg_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,7 +28,8 @@ EXPORTED = (
     "pjg_init", "pjg_last_error", "pjg_templates_create", "pjg_templates_destroy",
     "pjg_structures_create", "pjg_structures_destroy", "pjg_query", "pjg_results_count",
     "pjg_results_atom_count", "pjg_results_copy", "pjg_results_warning_count",
-    "pjg_results_warnings", "pjg_results_stats", "pjg_results_destroy",
+    "pjg_results_warnings", "pjg_results_stats", "pjg_results_destroy", "pjg_superpose_noalloc",
+    "pjg_noalloc_last_error",
 )
 
 _lib = None

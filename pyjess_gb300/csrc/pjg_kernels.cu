@@ -20,6 +20,8 @@
 #include <cfloat>
 #include <climits>
 #include <cstdint>
+#include <cstdio>
+#include <algorithm>
 
 #include "pjg_common.cuh"
 #include "pjg_kernels.cuh"
@@ -1811,4 +1813,166 @@ void launch_superpose(cudaStream_t st, int blocks, const ChunkView &cv, const Te
     k_superpose<<<blocks, 256, 0, st>>>(cv, tv, sa, in, out, counters);
 }
 
+// ---------------------------------------------------------------------------
+// Superposition without allocation (pjg_superpose_noalloc).
+//
+// For callers that cannot allocate device memory while they run -- code
+// recorded into a CUDA graph, a real-time loop that must not block on the
+// allocator, or a host application whose memory manager owns every device
+// allocation -- this variant of k_superpose takes the assignments' molecule
+// coordinates and the template's coordinates directly from the caller,
+// writes the caller's output arrays, and keeps its only scratch (one pass
+// flag per row, for the order-preserving compaction of the rows under the
+// rmsd threshold) in the static array below.  The array is part of the
+// library image: every GPU that loads the library holds it until the process
+// exits.  Every call shares it, so calls that overlap on the GPU (other
+// streams, other host threads) race and must be serialised by the caller.
+// Each call writes the flag of every row it later reads, so nothing carries
+// over from one call to the next.
+
+static __device__ __align__(256) int32_t g_noalloc_flags[PJG_NOALLOC_MAX_ROWS];
+
+__global__ void k_superpose_rows(const double *mol_xyz, const double *tpl_xyz, int32_t n_rows, int32_t n,
+                                 double rmsd_threshold, double *rmsd_out, double *rot_out, double *cen_out,
+                                 int32_t *flags) {
+    const int lane = lane_id();
+    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = warp; i < n_rows; i += nwarps) {
+        double a[3] = {0, 0, 0}, b[3] = {0, 0, 0};
+        if (lane < n) {
+            for (int d = 0; d < 3; d++) {
+                a[d] = mol_xyz[(i * n + lane) * 3 + d];
+                b[d] = tpl_xyz[3 * lane + d];
+            }
+        }
+        double ca[3], cb[3];
+        for (int d = 0; d < 3; d++) {
+            ca[d] = warp_sum(a[d]) / (double)n;
+            cb[d] = warp_sum(b[d]) / (double)n;
+        }
+        double ac[3] = {0, 0, 0}, bc[3] = {0, 0, 0};
+        if (lane < n)
+            for (int d = 0; d < 3; d++) {
+                ac[d] = a[d] - ca[d];
+                bc[d] = b[d] - cb[d];
+            }
+        double sumA = warp_sum(ac[0] * ac[0] + ac[1] * ac[1] + ac[2] * ac[2]);
+        double sumB = warp_sum(bc[0] * bc[0] + bc[1] * bc[1] + bc[2] * bc[2]);
+        double S[9];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) S[3 * r + c] = warp_sum(ac[r] * bc[c]);
+        if (lane == 0) {
+            double rmsd = 0.0, R[9];
+            bool bad = false;
+            quaternion_fit(S, 0.5 * (sumA + sumB), n, &rmsd, R, &bad);
+            rmsd_out[i] = rmsd;
+            for (int q = 0; q < 9; q++) rot_out[9 * i + q] = R[q];
+            for (int d = 0; d < 3; d++) {
+                cen_out[6 * i + d] = ca[d];
+                cen_out[6 * i + 3 + d] = cb[d];
+            }
+            flags[i] = (rmsd <= rmsd_threshold && !bad) ? 1 : 0;
+        }
+    }
+}
+
+// one block: rows whose flag is set, in row order, and their count
+__global__ void k_compact_rows(const int32_t *flags, int32_t n_rows, int32_t *pass_rows, int32_t *pass_count) {
+    __shared__ int32_t warp_tot[32];
+    const int lane = lane_id(), wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int32_t base = 0;
+    for (int32_t t0 = 0; t0 < n_rows; t0 += blockDim.x) {
+        const int32_t i = t0 + threadIdx.x;
+        const bool f = i < n_rows && flags[i] != 0;
+        const unsigned m = __ballot_sync(FULL_MASK, f);
+        if (lane == 0) warp_tot[wid] = __popc(m);
+        __syncthreads();
+        int32_t before = 0, total = 0;
+        for (int w = 0; w < nw; w++) {
+            if (w < wid) before += warp_tot[w];
+            total += warp_tot[w];
+        }
+        if (f) pass_rows[base + before + __popc(m & ((1u << lane) - 1u))] = i;
+        base += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *pass_count = base;
+}
+
 }  // namespace pjg
+
+// ---------------------------------------------------------------------------
+// C entry point of the allocation-free superposition
+
+#include <mutex>
+
+#include "../../include/pjg.h"
+
+namespace {
+std::mutex g_noalloc_mutex;
+void *g_noalloc_ptr[64] = {};  // device address of g_noalloc_flags, per device
+thread_local char g_noalloc_err[256];
+}  // namespace
+
+extern "C" const char *pjg_noalloc_last_error(void) { return g_noalloc_err; }
+
+// No counterpart in the reference: see include/pjg.h.
+extern "C" pjg_status pjg_superpose_noalloc(const double *mol_xyz, const double *tpl_xyz, int32_t n_rows,
+                                            int32_t n_atoms, double rmsd_threshold, double *rmsd, double *rotation,
+                                            double *centres, int32_t *pass_rows, int32_t *pass_count,
+                                            void *stream) {
+    g_noalloc_err[0] = 0;
+    if (n_rows < 0 || n_rows > PJG_NOALLOC_MAX_ROWS) {
+        snprintf(g_noalloc_err, sizeof g_noalloc_err,
+                 "pjg_superpose_noalloc: %d rows requested, the static scratch holds at most %d", n_rows,
+                 PJG_NOALLOC_MAX_ROWS);
+        return PJG_ERR_INVALID;
+    }
+    if (n_atoms < 1 || n_atoms > 32) {
+        snprintf(g_noalloc_err, sizeof g_noalloc_err, "pjg_superpose_noalloc: %d atoms per row (1 to 32 allowed)",
+                 n_atoms);
+        return PJG_ERR_INVALID;
+    }
+    if (!pass_count || (n_rows > 0 && (!mol_xyz || !tpl_xyz || !rmsd || !rotation || !centres || !pass_rows))) {
+        snprintf(g_noalloc_err, sizeof g_noalloc_err, "pjg_superpose_noalloc: null pointer argument");
+        return PJG_ERR_INVALID;
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 64) {
+        snprintf(g_noalloc_err, sizeof g_noalloc_err, "pjg_superpose_noalloc: no current device (%s)",
+                 cudaGetErrorString(e));
+        return PJG_ERR_NO_DEVICE;
+    }
+    void *flags = nullptr;
+    {
+        // once per device, with that device current: the device address of
+        // the static scratch (host code must not pass the symbol itself)
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_ptr[dev]) {
+            void *p = nullptr;
+            e = cudaGetSymbolAddress(&p, pjg::g_noalloc_flags);
+            if (e != cudaSuccess || !p) {
+                snprintf(g_noalloc_err, sizeof g_noalloc_err, "pjg_superpose_noalloc: cudaGetSymbolAddress: %s",
+                         cudaGetErrorString(e));
+                return PJG_ERR_CUDA;
+            }
+            g_noalloc_ptr[dev] = p;
+        }
+        flags = g_noalloc_ptr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n_rows > 0) {
+        int blocks = (int)std::min<int64_t>(((int64_t)n_rows + 7) / 8, 4096);
+        pjg::k_superpose_rows<<<blocks, 256, 0, st>>>(mol_xyz, tpl_xyz, n_rows, n_atoms, rmsd_threshold, rmsd,
+                                                      rotation, centres, (int32_t *)flags);
+    }
+    pjg::k_compact_rows<<<1, 1024, 0, st>>>((const int32_t *)flags, n_rows, pass_rows, pass_count);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        snprintf(g_noalloc_err, sizeof g_noalloc_err, "pjg_superpose_noalloc: launch: %s", cudaGetErrorString(e));
+        return PJG_ERR_CUDA;
+    }
+    return PJG_OK;
+}

@@ -9,6 +9,11 @@
 
 namespace pjg {
 
+// rows one call of pjg_superpose_noalloc may take (its static scratch)
+#ifndef PJG_NOALLOC_MAX_ROWS
+#define PJG_NOALLOC_MAX_ROWS (1 << 20)
+#endif
+
 constexpr int SEARCH_WARPS = 8;        // warps per block of k_search
 constexpr int LEAF_WARPS = 4;          // warps per block of k_leaf_order (shared memory: 8.5 KB a warp)
 constexpr int LEAF_FAST_MAX = 384;     // longest list ordered in shared memory
