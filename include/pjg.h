@@ -219,9 +219,9 @@ void pjg_results_destroy(pjg_results *r);
 /* Allocation-free superposition --------------------------------------------
  *
  * No counterpart in the reference.  For callers that cannot allocate device
- * memory while they run (work recorded into a CUDA graph, real-time loops
- * that must not block on the allocator, applications whose memory manager
- * owns every device allocation).  It superposes n_rows candidate assignments
+ * memory while they run (real-time loops that must not block on the
+ * allocator, applications whose memory manager owns every device
+ * allocation).  It superposes n_rows candidate assignments
  * of one template: row r's molecule atoms are mol_xyz[(r*n_atoms + k)*3 + d],
  * the template's atoms tpl_xyz[3k + d] (k = template atom, 1 <= n_atoms <=
  * 32), all device pointers.  It writes, per row, rmsd[r], rotation[9r..]

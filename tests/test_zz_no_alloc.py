@@ -1,9 +1,9 @@
 """pjg_superpose_noalloc: the allocation-free superposition entry point.
 
-Callers that cannot allocate device memory while they run (a CUDA graph
-being recorded, a real-time loop, an application whose memory manager owns
-every device allocation) pass their own input and output buffers; the entry
-point's only scratch is a static device array inside the library.  This test
+Callers that cannot allocate device memory while they run (a real-time
+loop, an application whose memory manager owns every device allocation) pass
+their own input and output buffers; the entry point's only scratch is a
+static device array inside the library.  This test
 calls it through the C ABI on the hits of a normal `pjg_query` and checks that
 it reproduces that query's rmsd, rotations and centroids, twice in a row
 (the second call reuses the static scratch left by the first).  The file is
