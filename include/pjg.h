@@ -125,6 +125,8 @@ typedef struct {
     int64_t hits;                    /* after the automaton                */
     int64_t fp64_rechecks;           /* guard-band rechecks (FP32 mode)    */
     int64_t leaf_exact;              /* lists ordered by the exact replay  */
+    int64_t leaf_sorted;             /* lists ordered by sorted axes       */
+    int64_t leaf_replays;            /* kd nodes replayed there (ties)     */
     int64_t bytes_candidates;        /* algorithmic bytes, candidate stage */
     int64_t bytes_expansion;         /* algorithmic bytes, expansion stage */
     int64_t bytes_superposition;     /* algorithmic bytes, superposition   */

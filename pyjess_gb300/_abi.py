@@ -61,6 +61,8 @@ class Stats(C.Structure):
         ("hits", C.c_int64),
         ("fp64_rechecks", C.c_int64),
         ("leaf_exact", C.c_int64),
+        ("leaf_sorted", C.c_int64),
+        ("leaf_replays", C.c_int64),
         ("bytes_candidates", C.c_int64),
         ("bytes_expansion", C.c_int64),
         ("bytes_superposition", C.c_int64),

@@ -150,6 +150,8 @@ struct pjg_structures {
     int32_t *d_sorted = nullptr;
     int32_t *d_bucket_begin = nullptr, *d_bucket_lo = nullptr, *d_bucket_hi = nullptr;
     uint32_t *d_bucket_name = nullptr;
+    uint32_t *d_lrank = nullptr, *d_urank = nullptr;  // [3][N] axis ranks
+    uint8_t *d_special = nullptr;                     // [S] NaN coordinate
     int device = 0;
 };
 
@@ -437,6 +439,25 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
     if (e == cudaSuccess) e = upload(&h->d_bucket_name, bucket_name);
     if (e == cudaSuccess) e = upload(&h->d_bucket_lo, bucket_lo);
     if (e == cudaSuccess) e = upload(&h->d_bucket_hi, bucket_hi);
+    if (e == cudaSuccess) {
+        // axis ranks of every atom (the leaf-order sorted-axis path)
+        const size_t n3 = 3 * (size_t)std::max<int64_t>(N, 1);
+        unsigned long long *tile_key = nullptr;
+        uint16_t *tile_idx = nullptr;
+        e = cudaMalloc((void **)&h->d_lrank, n3 * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_urank, n3 * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_special, std::max(S, 1));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&tile_key, n3 * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&tile_idx, n3 * sizeof(uint16_t));
+        if (e == cudaSuccess) {
+            launch_axis_ranks(0, S, h->d_atom_base, h->d_atom_count, h->d_xyz64, N, tile_key, tile_idx, h->d_lrank,
+                              h->d_urank, h->d_special);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        }
+        if (tile_key) cudaFree(tile_key);
+        if (tile_idx) cudaFree(tile_idx);
+    }
     if (e != cudaSuccess) {
         pjg_status st = fail(e == cudaErrorMemoryAllocation ? PJG_ERR_OOM : PJG_ERR_CUDA, "structure upload: %s",
                              cudaGetErrorString(e));
@@ -450,7 +471,8 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
 void pjg_structures_destroy(pjg_structures *h) {
     if (!h) return;
     void *ptrs[] = {h->d_atom_base, h->d_atom_count, h->d_xyz64, h->d_xyz32, h->d_name, h->d_resname,
-                    h->d_sorted, h->d_bucket_begin, h->d_bucket_name, h->d_bucket_lo, h->d_bucket_hi};
+                    h->d_sorted, h->d_bucket_begin, h->d_bucket_name, h->d_bucket_lo, h->d_bucket_hi,
+                    h->d_lrank, h->d_urank, h->d_special};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete h;
@@ -526,8 +548,8 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     DBuf<int32_t> d_count, d_scanned, d_cand_atom, d_leaf_atom, d_pair_counter;
     DBuf<int64_t> d_offset, d_totals, d_boff;
     DBuf<int32_t> d_nblk;
-    DBuf<int64_t> d_exact_list;
-    DBuf<unsigned long long> d_exact_count;
+    DBuf<int64_t> d_exact_list, d_sorted_list;
+    DBuf<unsigned long long> d_exact_count, d_sorted_count;
     DBuf<float4> d_blk_lo, d_blk_hi;
     DBuf<float4> d_cand_xyz, d_leaf_xyz;
     DBuf<unsigned long long> d_counters, d_ccount, d_pcount;
@@ -588,7 +610,8 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
         CUDA_TRY(dalloc(d_scanned, (size_t)W, st));
         CUDA_TRY(dalloc(d_totals, (size_t)S, st));
         ChunkView cv{S, sp->d_atom_base, sp->d_atom_count, sp->d_xyz64, sp->d_xyz32, sp->d_name, sp->d_resname,
-                     sp->d_sorted, sp->d_bucket_begin, sp->d_bucket_name, sp->d_bucket_lo, sp->d_bucket_hi};
+                     sp->d_sorted, sp->d_bucket_begin, sp->d_bucket_name, sp->d_bucket_lo, sp->d_bucket_hi,
+                     sp->N, sp->d_lrank, sp->d_urank, sp->d_special};
         SigView sv{G, tp->d_code, tp->d_rule, tp->d_mainchain, tp->d_name_begin, tp->d_names, tp->d_res_begin,
                    tp->d_resnames, tp->d_partner_begin, tp->d_partner_res, tp->d_partner_name};
         int blocks = (int)std::min<int64_t>((W + 7) / 8, (int64_t)sm_count() * 32);
@@ -623,7 +646,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             const int64_t Wc = (int64_t)Sc * G;
             ChunkView cv{Sc, sp->d_atom_base + s0, sp->d_atom_count + s0, sp->d_xyz64, sp->d_xyz32, sp->d_name,
                          sp->d_resname, sp->d_sorted, sp->d_bucket_begin + s0, sp->d_bucket_name, sp->d_bucket_lo,
-                         sp->d_bucket_hi};
+                         sp->d_bucket_hi, sp->N, sp->d_lrank, sp->d_urank, sp->d_special + s0};
             SigView sv{G, tp->d_code, tp->d_rule, tp->d_mainchain, tp->d_name_begin, tp->d_names, tp->d_res_begin,
                        tp->d_resnames, tp->d_partner_begin, tp->d_partner_res, tp->d_partner_name};
             int32_t *cnt_c = d_count.p + (int64_t)s0 * G;
@@ -658,10 +681,13 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 int lb = (int)std::min<int64_t>((Wc + LEAF_WARPS - 1) / LEAF_WARPS, (int64_t)sm_count() * 32);
                 CUDA_TRY(dalloc(d_exact_list, (size_t)Wc, st));
                 CUDA_TRY(dalloc(d_exact_count, 1, st));
+                CUDA_TRY(dalloc(d_sorted_list, 3 * (size_t)Wc, st));
+                CUDA_TRY(dalloc(d_sorted_count, 3, st));
                 launch_leaf_order(st, std::max(lb, 1), cv, G, cnt_c, d_offset.p, d_boff.p, d_cand_atom.p,
-                                  d_cand_xyz.p, d_leaf_atom.p, d_leaf_xyz.p, d_blk_lo.p, d_blk_hi.p, d_exact_list.p,
-                                  d_exact_count.p, d_counters.p);
-                launches += 6;
+                                  d_cand_xyz.p, d_leaf_atom.p, d_leaf_xyz.p, d_blk_lo.p, d_blk_hi.p,
+                                  d_sorted_list.p, d_sorted_count.p, Wc, d_exact_list.p, d_exact_count.p,
+                                  d_counters.p);
+                launches += 9;
                 CUDA_TRY(cudaGetLastError());
             }
             CUDA_TRY(cudaEventRecord(ev[2], st));
@@ -806,8 +832,11 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
         goto done;
     }
     if (counters[C_ERROR]) {
-        status = fail(PJG_ERR_CAPACITY, "search kernel reported error %llu (template too large for the frontier tile)",
-                      counters[C_ERROR]);
+        const unsigned long long c = counters[C_ERROR];
+        status = fail(PJG_ERR_CAPACITY, "kernel reported error %llu (%s)", c,
+                      c == 1 ? "template over 32 atoms" : c == 2 ? "template too large for the frontier tile"
+                      : c == 4 ? "leaf order: too many small subtrees" : c == 5 ? "leaf order: partition did not converge"
+                      : "leaf order: inconsistent node partition");
         goto done;
     }
 
@@ -896,6 +925,8 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     res->stats.hits = (int64_t)res->rmsd.size();
     res->stats.fp64_rechecks = (int64_t)counters[C_RECHECK];
     res->stats.leaf_exact = (int64_t)counters[C_LEAF_EXACT];
+    res->stats.leaf_sorted = (int64_t)counters[C_LEAF_SORTED];
+    res->stats.leaf_replays = (int64_t)counters[C_LEAF_REPLAY];
     res->stats.bytes_candidates = (int64_t)counters[C_BYTES_CAND];
     res->stats.bytes_expansion = (int64_t)counters[C_BYTES_EXP];
     {
@@ -919,7 +950,8 @@ done:
         dfree(d_pcount, st); dfree(d_c_pair, st); dfree(d_c_atoms, st); dfree(d_p_pair, st);
         dfree(d_p_nan, st); dfree(d_p_atoms, st); dfree(d_c_ord, st); dfree(d_p_row, st);
         dfree(d_p_ord, st); dfree(d_p_rmsd, st); dfree(d_c_rmsd, st); dfree(d_boff, st); dfree(d_nblk, st);
-        dfree(d_blk_lo, st); dfree(d_blk_hi, st); dfree(d_exact_list, st); dfree(d_exact_count, st); dfree(d_p_rot, st); dfree(d_p_cen, st);
+        dfree(d_blk_lo, st); dfree(d_blk_hi, st); dfree(d_exact_list, st); dfree(d_exact_count, st);
+        dfree(d_sorted_list, st); dfree(d_sorted_count, st); dfree(d_p_rot, st); dfree(d_p_cen, st);
         for (auto &b : scan_tmp) dfree(b, st);
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);

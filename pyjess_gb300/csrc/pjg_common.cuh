@@ -67,6 +67,10 @@ struct ChunkView {
     const uint32_t *bucket_name;
     const int32_t *bucket_lo;     // structure-local positions into sorted
     const int32_t *bucket_hi;
+    int64_t n_atoms;              // atoms of the whole structure set
+    const uint32_t *lrank;        // [3][n_atoms] strict-lower axis rank
+    const uint32_t *urank;        // [3][n_atoms] unique axis rank
+    const uint8_t *special;       // [S] a NaN coordinate (exact leaf order only)
 };
 
 struct SigView {
@@ -122,8 +126,12 @@ enum Counter : int {
     C_OVERFLOW,       // complete-row buffer overflow (rows dropped)
     C_PASS_OVERFLOW,  // passing-row buffer overflow
     C_LEAF_EXACT,     // lists ordered by the exact sequential replay
+    C_LEAF_SORTED,    // lists ordered by sorted axes
+    C_LEAF_REPLAY,    // kd nodes replayed by qselect in the sorted-axis path
     C_ERROR,          // error code: 1 template > 32 atoms, 2 frontier tile too
-                      // small, 3 time budget exhausted (0 = none)
+                      // small, 3 time budget exhausted, 4 leaf order: too many
+                      // small subtrees, 5 a partition did not converge, 6 an
+                      // inconsistent node partition (0 = none)
     C_NUM
 };
 

@@ -21,6 +21,7 @@
 #include <climits>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <algorithm>
 
 #include "pjg_common.cuh"
@@ -259,15 +260,17 @@ __global__ void k_scan_add(int64_t *out, int64_t n, const int64_t *tile_offsets)
 // leaf order is the partitioned index array read backwards.  Pruning only
 // removes subtrees, so accepted leaves always come out in this order.
 //
-// Fast path (warp per list, shared memory): when no node has a tie at its
+// Fast paths (warp per list, shared memory): when no node has a tie at its
 // median boundary (equal axis values on both sides of position n/2), each
 // node's left/right sets are the n/2 smallest / the rest whatever the
-// arrangement qselect leaves behind, so the leaf order follows from a
-// rank-based recursive median split computed by all lanes.  The FP32
+// arrangement qselect leaves behind, so the leaf order follows from any
+// recursive median split computed by all lanes.  Short lists use ranks
+// (O(m^2) a level); longer ones sort each axis once and partition the three
+// sorted arrays stably at every level (O(m) a level).  The FP32
 // centroid-relative keys are a monotone rounding of the FP64 coordinates, so
 // a tie there only sends the list to the exact path.  Exact path: the
-// literal sequential qselect replay on the FP64 coordinates.  Each list also
-// gets the bounding boxes of its blocks of 32 consecutive leaves (the
+// literal qselect replay on the FP64 coordinates (k_leaf_exact).  Each list
+// also gets the bounding boxes of its blocks of 32 consecutive leaves (the
 // search culls whole blocks against a parent's join box).
 
 __device__ __forceinline__ int axis_cmp(double c, double d) { return c < d ? -1 : c > d ? 1 : 0; }
@@ -355,26 +358,68 @@ struct LeafWarp {
     uint16_t seg_n[LEAF_FAST_MAX];
 };
 
+// Leaf order of a list from its partitioned candidate array `order`
+// (read backwards: the right subtree is visited first), plus the bounding
+// boxes of its blocks of 32 consecutive leaves.
+__device__ void write_leaves(const uint16_t *order, int m, int64_t o, const int32_t *ca, const float4 *cand_xyz,
+                             int32_t *leaf_atom, float4 *leaf_xyz, int64_t bo, float4 *blk_lo, float4 *blk_hi) {
+    const int lane = lane_id();
+    for (int r = lane; r < m; r += 32) {
+        int e = order[m - 1 - r];
+        leaf_atom[o + r] = ca[e];
+        leaf_xyz[o + r] = cand_xyz[o + e];
+    }
+    __syncwarp();
+    for (int b = 0; b * 32 < m; b++) {
+        int r = b * 32 + lane;
+        float4 p = leaf_xyz[o + (r < m ? r : b * 32)];
+        float mnx = p.x, mny = p.y, mnz = p.z, mxx = p.x, mxy = p.y, mxz = p.z;
+        for (int off = 16; off; off >>= 1) {
+            mnx = fminf(mnx, __shfl_xor_sync(FULL_MASK, mnx, off));
+            mny = fminf(mny, __shfl_xor_sync(FULL_MASK, mny, off));
+            mnz = fminf(mnz, __shfl_xor_sync(FULL_MASK, mnz, off));
+            mxx = fmaxf(mxx, __shfl_xor_sync(FULL_MASK, mxx, off));
+            mxy = fmaxf(mxy, __shfl_xor_sync(FULL_MASK, mxy, off));
+            mxz = fmaxf(mxz, __shfl_xor_sync(FULL_MASK, mxz, off));
+        }
+        if (lane == 0) {
+            blk_lo[bo + b] = make_float4(mnx, mny, mnz, 0.f);
+            blk_hi[bo + b] = make_float4(mxx, mxy, mxz, 0.f);
+        }
+    }
+    __syncwarp();
+}
+
+// Short lists (at most rank_max entries) without a tie: rank method, one
+// warp per list.  Longer or tied lists go to k_leaf_sorted's worklist (up
+// to LEAF_SORTED_MAX entries), the rest -- and every list of a structure
+// with a NaN coordinate -- to k_leaf_exact's.
 __global__ void __launch_bounds__(LEAF_WARPS * 32)
     k_leaf_order(ChunkView cv, int32_t n_sigs, const int32_t *count, const int64_t *offset,
                  const int64_t *blk_offset, const int32_t *cand_atom, const float4 *cand_xyz,
-                 int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
-                 int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters) {
+                 int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi, int64_t *sorted_list,
+                 unsigned long long *sorted_count, int64_t list_cap, int64_t *exact_list,
+                 unsigned long long *exact_count, unsigned long long *counters, int rank_max) {
     __shared__ LeafWarp sh[LEAF_WARPS];
     const int lane = lane_id();
     LeafWarp &L = sh[threadIdx.x >> 5];
     int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     int64_t total = (int64_t)cv.n_structures * n_sigs;
-    unsigned long long slow = 0;
+    unsigned long long n_exact = 0, n_sorted = 0;
     for (int64_t w = warp; w < total; w += nwarps) {
         const int m = count[w];
         if (m <= 0) continue;
+        const int s = (int)(w / n_sigs);
+        if (cv.special[s]) {
+            n_exact++;
+            if (lane == 0) exact_list[atomicAdd(exact_count, 1ull)] = w;
+            continue;
+        }
         const int64_t o = offset[w];
-        const int32_t *ca = cand_atom + o;
-        bool exact = m > LEAF_FAST_MAX;
+        bool tie = m > rank_max;
         int src = 0;
-        if (!exact) {
+        if (!tie) {
             for (int i = lane; i < m; i += 32) {
                 float4 p = cand_xyz[o + i];
                 L.v[0][i] = p.x;
@@ -391,7 +436,7 @@ __global__ void __launch_bounds__(LEAF_WARPS * 32)
             for (int d = 0; d < levels; d++) {
                 const uint16_t *A = L.ord[src];
                 uint16_t *B = L.ord[src ^ 1];
-                bool tie = false;
+                bool t = false;
                 for (int p = lane; p < m; p += 32) {
                     const int lo = L.seg_lo[p], n = L.seg_n[p];
                     const int e = A[p];
@@ -409,12 +454,12 @@ __global__ void __launch_bounds__(LEAF_WARPS * 32)
                         before += (y < x) | ((y == x) & (q < p));
                     }
                     const int k = n / 2;
-                    if (less < k && less + eq > k) tie = true;
+                    if (less < k && less + eq > k) t = true;
                     B[lo + before] = (uint16_t)e;
                 }
                 __syncwarp();
-                if (__any_sync(FULL_MASK, tie)) {
-                    exact = true;
+                if (__any_sync(FULL_MASK, t)) {
+                    tie = true;
                     break;
                 }
                 const int nax = (d + 1) % 3;
@@ -434,44 +479,23 @@ __global__ void __launch_bounds__(LEAF_WARPS * 32)
                 __syncwarp();
             }
         }
-        if (exact) {
-            // a tie at some median boundary (or a long list): the exact
-            // replay runs in k_leaf_exact, one thread per list
-            slow++;
-            if (lane == 0) exact_list[atomicAdd(exact_count, 1ull)] = w;
+        if (tie) {
+            if (m <= LEAF_SORTED_MAX) {
+                // size classes of k_leaf_sorted: up to 512, 1024, 2048 entries
+                const int c = m <= 512 ? 0 : m <= 1024 ? 1 : 2;
+                n_sorted++;
+                if (lane == 0) sorted_list[c * list_cap + (int64_t)atomicAdd(&sorted_count[c], 1ull)] = w;
+            } else {
+                n_exact++;
+                if (lane == 0) exact_list[atomicAdd(exact_count, 1ull)] = w;
+            }
+            __syncwarp();
             continue;
         }
-        {
-            const uint16_t *A = L.ord[src];
-            for (int r = lane; r < m; r += 32) {
-                int e = A[m - 1 - r];
-                leaf_atom[o + r] = ca[e];
-                leaf_xyz[o + r] = cand_xyz[o + e];
-            }
-        }
-        __syncwarp();
-        // bounding boxes of blocks of 32 consecutive leaves
-        const int64_t bo = blk_offset[w];
-        for (int b = 0; b * 32 < m; b++) {
-            int r = b * 32 + lane;
-            float4 p = leaf_xyz[o + (r < m ? r : b * 32)];
-            float mnx = p.x, mny = p.y, mnz = p.z, mxx = p.x, mxy = p.y, mxz = p.z;
-            for (int off = 16; off; off >>= 1) {
-                mnx = fminf(mnx, __shfl_xor_sync(FULL_MASK, mnx, off));
-                mny = fminf(mny, __shfl_xor_sync(FULL_MASK, mny, off));
-                mnz = fminf(mnz, __shfl_xor_sync(FULL_MASK, mnz, off));
-                mxx = fmaxf(mxx, __shfl_xor_sync(FULL_MASK, mxx, off));
-                mxy = fmaxf(mxy, __shfl_xor_sync(FULL_MASK, mxy, off));
-                mxz = fmaxf(mxz, __shfl_xor_sync(FULL_MASK, mxz, off));
-            }
-            if (lane == 0) {
-                blk_lo[bo + b] = make_float4(mnx, mny, mnz, 0.f);
-                blk_hi[bo + b] = make_float4(mxx, mxy, mxz, 0.f);
-            }
-        }
-        __syncwarp();
+        write_leaves(L.ord[src], m, o, cand_atom + o, cand_xyz, leaf_atom, leaf_xyz, blk_offset[w], blk_lo, blk_hi);
     }
-    if (lane == 0 && slow) atomicAdd(&counters[C_LEAF_EXACT], slow);
+    if (lane == 0 && n_exact) atomicAdd(&counters[C_LEAF_EXACT], n_exact);
+    if (lane == 0 && n_sorted) atomicAdd(&counters[C_LEAF_SORTED], n_sorted);
 }
 
 // Exact replay for the lists k_leaf_order could not order by ranks (a tie
@@ -496,7 +520,17 @@ struct ExactShared {
     uint16_t *PTR;    // append -> earlier append it copies
 };
 
-__device__ int warp_partition(const ExactShared &S, int L0, int R0, int piv, unsigned long long *fallback) {
+// One Lomuto partition of A[L0..R0] around A[piv] (moved to R0 first) by
+// the whole warp; key[e] is element e's axis value ("<=" in the sense of
+// axis_cmp: a NaN compares equal).  X, VAL and PTR are scratch of at least
+// R0 - L0 entries.  Returns the pivot's final position.
+template <typename KeyT>
+__device__ int warp_lomuto(uint16_t *A, const KeyT *key, uint16_t *X, uint16_t *VAL, uint16_t *PTR, int L0, int R0,
+                           int piv, unsigned long long *fallback) {
+    struct {
+        uint16_t *A, *X, *VAL, *PTR;
+        const KeyT *key;
+    } S{A, X, VAL, PTR, key};
     const int lane = lane_id();
     const unsigned lt = (1u << lane) - 1u;
     __syncwarp();
@@ -507,7 +541,7 @@ __device__ int warp_partition(const ExactShared &S, int L0, int R0, int piv, uns
     }
     __syncwarp();
     const uint16_t P = S.A[R0];
-    const double pv = S.key[P];
+    const KeyT pv = S.key[P];
     const int L = R0 - L0;
     int cf = 0, cpush = 0, crot = 0, capp = 0;
     for (int c0 = 0; c0 < L; c0 += 32) {
@@ -517,7 +551,7 @@ __device__ int warp_partition(const ExactShared &S, int L0, int R0, int piv, uns
         bool f = false;
         if (valid) {
             xi = S.A[L0 + i];
-            f = S.key[xi] <= pv;
+            f = !(S.key[xi] > pv);
         }
         const unsigned mf = __ballot_sync(FULL_MASK, valid && f);
         const unsigned mp = __ballot_sync(FULL_MASK, valid && !f);
@@ -558,7 +592,7 @@ __device__ int warp_partition(const ExactShared &S, int L0, int R0, int piv, uns
         }
         __syncwarp();
         if (!__any_sync(FULL_MASK, open)) break;
-        if (round == 19 && lane == 0) atomicAdd(fallback, 1ull);
+        if (round == 19 && lane == 0) atomicMax(fallback, 5ull);
     }
     const int C = cf, G = cpush, R = crot;
     for (int i = lane; i < C; i += 32) S.A[L0 + i] = S.X[i];
@@ -569,6 +603,10 @@ __device__ int warp_partition(const ExactShared &S, int L0, int R0, int piv, uns
     if (lane == 0) S.A[L0 + C] = P;
     __syncwarp();
     return L0 + C;
+}
+
+__device__ int warp_partition(const ExactShared &S, int L0, int R0, int piv, unsigned long long *fallback) {
+    return warp_lomuto<double>(S.A, S.key, S.X, S.VAL, S.PTR, L0, R0, piv, fallback);
 }
 
 // sequential qselect_r on positions A[0..n) with their FP64 axis values in
@@ -641,7 +679,7 @@ __global__ void k_leaf_exact(ChunkView cv, int32_t n_sigs, const int32_t *count,
     for (int64_t i = warp; i < total; i += nwarps) {
         const int64_t w = exact_list[i];
         const int m = count[w];
-        if (m <= MINN) continue;
+        if (m <= MINN || (m > MAXN && MAXN != EXACT_MAX)) continue;
         const int s = (int)(w / n_sigs);
         const int64_t o = offset[w];
         const int32_t *ca = cand_atom + o;
@@ -771,6 +809,435 @@ __global__ void k_leaf_exact(ChunkView cv, int32_t n_sigs, const int32_t *count,
         }
         __syncwarp();
     }
+}
+
+// ---------------------------------------------------------------------------
+// Axis ranks of every structure atom (once per structure set, at upload).
+//
+// For atom i and axis a: lrank = number of the structure's atoms whose
+// coordinate on a is strictly smaller, so lranks compare exactly as the FP64
+// coordinates do (equal coordinates share one); urank = number of atoms
+// before i in (coordinate, index) order, a permutation of 0..n-1.  A
+// coordinate that is NaN has no place in that order: the structure is
+// flagged in `special` and its lists take the exact replay.  One block per
+// (structure, axis): the atoms are sorted in tiles of RANK_TILE in shared
+// memory, each tile is stored, and every atom's ranks are sums of binary
+// searches over the sorted tiles.
+
+constexpr int RANK_TILE = 2048;
+constexpr int RANK_THREADS = 512;
+
+__device__ __forceinline__ unsigned long long order_key(double x) {
+    if (x == 0.0) x = 0.0;  // -0 and +0 compare equal
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__global__ void __launch_bounds__(RANK_THREADS)
+    k_axis_ranks(const int64_t *atom_base, const int32_t *atom_count, const double *xyz64, int64_t n_atoms,
+                 unsigned long long *tile_key, uint16_t *tile_idx, uint32_t *lrank, uint32_t *urank,
+                 uint8_t *special) {
+    __shared__ unsigned long long key[RANK_TILE];
+    __shared__ uint16_t idx[RANK_TILE];
+    const int s = blockIdx.x, a = blockIdx.y;
+    const int64_t b0 = atom_base[s];
+    const int n = atom_count[s];
+    const int tiles = (n + RANK_TILE - 1) / RANK_TILE;
+    unsigned long long *gk = tile_key + a * n_atoms + b0;
+    uint16_t *gi = tile_idx + a * n_atoms + b0;
+    int nan = 0;
+    for (int t = 0; t < tiles; t++) {
+        const int t0 = t * RANK_TILE, tn = min(RANK_TILE, n - t0);
+        for (int i = threadIdx.x; i < RANK_TILE; i += blockDim.x) {
+            if (i < tn) {
+                const double x = xyz64[3 * (b0 + t0 + i) + a];
+                nan |= x != x;
+                key[i] = order_key(x);
+            } else {
+                key[i] = ~0ull;
+            }
+            idx[i] = (uint16_t)i;
+        }
+        __syncthreads();
+        // bitonic sort by (key, idx)
+        for (int k = 2; k <= RANK_TILE; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                const int lj = __ffs(j) - 1;
+                for (int q = threadIdx.x; q < RANK_TILE / 2; q += blockDim.x) {
+                    const int i = ((q >> lj) << (lj + 1)) | (q & (j - 1));
+                    const int l = i | j;
+                    const bool asc = (i & k) == 0;
+                    const unsigned long long ki = key[i], kl = key[l];
+                    const uint16_t ii = idx[i], il = idx[l];
+                    const bool gt = ki > kl || (ki == kl && ii > il);
+                    if (gt == asc) {
+                        key[i] = kl;
+                        key[l] = ki;
+                        idx[i] = il;
+                        idx[l] = ii;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (int i = threadIdx.x; i < tn; i += blockDim.x) {
+            gk[t0 + i] = key[i];
+            gi[t0 + i] = idx[i];
+        }
+        __syncthreads();
+    }
+    if (__syncthreads_or(nan) && threadIdx.x == 0) special[s] = 1;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const unsigned long long ki = order_key(xyz64[3 * (b0 + i) + a]);
+        const int ti = i / RANK_TILE;
+        const uint16_t li = (uint16_t)(i % RANK_TILE);
+        uint32_t lr = 0, ur = 0;
+        for (int t = 0; t < tiles; t++) {
+            const unsigned long long *tk = gk + t * RANK_TILE;
+            const int tn = min(RANK_TILE, n - t * RANK_TILE);
+            int lo = 0, hi = tn;
+            while (lo < hi) {  // first key >= ki
+                const int mid = (lo + hi) >> 1;
+                if (tk[mid] < ki) lo = mid + 1;
+                else hi = mid;
+            }
+            lr += lo;
+            if (t < ti) {  // earlier atoms: equal keys come before i
+                int l2 = lo, h2 = tn;
+                while (l2 < h2) {
+                    const int mid = (l2 + h2) >> 1;
+                    if (tk[mid] <= ki) l2 = mid + 1;
+                    else h2 = mid;
+                }
+                ur += l2;
+            } else if (t == ti) {  // i's own tile: (key, index) order
+                const uint16_t *tix = gi + t * RANK_TILE;
+                int l2 = lo, h2 = tn;
+                while (l2 < h2) {
+                    const int mid = (l2 + h2) >> 1;
+                    if (tk[mid] < ki || (tk[mid] == ki && tix[mid] < li)) l2 = mid + 1;
+                    else h2 = mid;
+                }
+                ur += l2;
+            } else {
+                ur += lo;
+            }
+        }
+        lrank[a * n_atoms + b0 + i] = lr;
+        urank[a * n_atoms + b0 + i] = ur;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Sorted-axis leaf order (lists longer than the rank method's, or tied).
+//
+// One warp per list.  (1) Each axis order of the list comes from the atoms'
+// unique axis ranks: set one bit per element in a bitmap over the
+// structure's ranks (windows of SORT_WINDOW_BITS), prefix-count the words,
+// and each element's position is the count of set bits below its own.
+// Each element also gets its coordinate's dense rank within the list per
+// axis (`run`), so that equal coordinates are exactly equal keys.  (2) The
+// tree is split level by level: a node's left child is the first n/2
+// entries of its range in the split axis's order, and the other orders are
+// partitioned stably within each node by one prefix count per level.  (3)
+// A node with a tie at its median boundary (equal keys on both sides of
+// position n/2) keeps the elements qselect_r would leave on each side,
+// which depends on the arrangement its ancestors' qselects leave behind:
+// those ancestors and the node are replayed (median-of-3 pivots and Lomuto
+// partitions, as in k_leaf_exact) on the arrangement array A, top down and
+// each node at most once, and the node's children take their members from
+// A.  Untied nodes need no arrangement: their children are the n/2
+// smallest and the rest whatever the arrangement.  Lists whose tied nodes
+// or replays exceed the small per-warp tables go to k_leaf_exact.
+
+constexpr int SORT_WINDOW_WORDS = 512;
+constexpr int SORT_WINDOW_BITS = 32 * SORT_WINDOW_WORDS;
+constexpr int LEAF_MAX_TIED = 32;     // tied nodes per level
+constexpr int LEAF_MAX_REPLAY = 64;   // replayed nodes per list
+
+template <int M>
+struct SortedWarp {
+    uint16_t buf[4][M];  // the three axis orders and a spare (ping-pong)
+    uint16_t run[3][M];  // dense coordinate rank of each element per axis
+    union {
+        struct {
+            uint32_t bits[SORT_WINDOW_WORDS];
+            uint16_t wpre[SORT_WINDOW_WORDS];  // set bits before each word
+            uint32_t ur[M];                    // unique rank of each element
+        } so;
+        struct {
+            uint16_t F[M];    // left-flag prefix counts (VAL of a replay)
+            uint16_t PTR[M];  // replay scratch
+            uint16_t A[M];    // qselect arrangement of replayed nodes
+            uint32_t seg[M];  // node of each position: lo | n << 16
+            uint8_t flag[M];  // element goes to the left child
+            uint32_t done[LEAF_MAX_REPLAY];
+            uint16_t tied[LEAF_MAX_TIED];
+        } sp;
+    } u;
+};
+
+// qselect_r's k = n/2 selection on A[lo..lo+n) with keys K (see k_leaf_exact)
+__device__ void warp_qselect(uint16_t *A, const uint16_t *K, uint16_t *X, uint16_t *VAL, uint16_t *PTR, int lo,
+                             int n, unsigned long long *err) {
+    const int k = n / 2;
+    int left = 0, right = n - 1;
+    while (left != right) {
+        const int L0 = lo + left, R0 = lo + right;
+        const int mid = (L0 + R0 + 1) / 2;
+        const int l = K[A[L0]], r = K[A[R0]], mm = K[A[mid]];
+        int piv;
+        if ((l > mm) != (l > r)) piv = L0;
+        else if ((mm < l) != (mm < r)) piv = mid;
+        else piv = R0;
+        const int store = warp_lomuto<uint16_t>(A, K, X, VAL, PTR, L0, R0, piv, err) - lo;
+        if (store == k) break;
+        if (k < store) right = store - 1;
+        else left = store + 1;
+    }
+}
+
+template <int M, int MINN, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, 1)
+    k_leaf_sorted(ChunkView cv, int32_t n_sigs, const int32_t *count, const int64_t *offset,
+                  const int64_t *blk_offset, const int32_t *cand_atom, const float4 *cand_xyz, int32_t *leaf_atom,
+                  float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi, const int64_t *sorted_list,
+                  const unsigned long long *sorted_count, int64_t *exact_list, unsigned long long *exact_count,
+                  unsigned long long *counters) {
+    extern __shared__ __align__(16) unsigned char sorted_smem[];
+    SortedWarp<M> &L = reinterpret_cast<SortedWarp<M> *>(sorted_smem)[threadIdx.x >> 5];
+    const int lane = lane_id();
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t total = (int64_t)*sorted_count;
+    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned long long n_exact = 0, n_replay = 0;
+    for (int64_t i = warp; i < total; i += nwarps) {
+        const int64_t w = sorted_list[i];
+        const int m = count[w];
+        if (m <= MINN || m > M) continue;
+        const int s = (int)(w / n_sigs);
+        const int64_t gbase = cv.atom_base[s];
+        const int natoms = cv.atom_count[s];
+        const int64_t o = offset[w];
+        const int32_t *ca = cand_atom + o;
+
+        // (1) axis orders and dense ranks
+        bool complete = true;
+        for (int a = 0; a < 3; a++) {
+            const uint32_t *ur = cv.urank + a * cv.n_atoms + gbase;
+            const uint32_t *lrk = cv.lrank + a * cv.n_atoms + gbase;
+            uint16_t *Sa = L.buf[a];
+#pragma unroll 4
+            for (int e = lane; e < m; e += 32) L.u.so.ur[e] = ur[ca[e]];
+            int placed = 0;
+            for (int wb = 0; wb < natoms; wb += SORT_WINDOW_BITS) {
+                const int nwords = min(SORT_WINDOW_WORDS, (natoms - wb + 31) >> 5);
+                if (wb == 0)
+                    for (int q = lane; q < nwords; q += 32) L.u.so.bits[q] = 0u;
+                __syncwarp();
+                for (int e = lane; e < m; e += 32) {
+                    const uint32_t u = L.u.so.ur[e] - (uint32_t)wb;
+                    if (u < (uint32_t)SORT_WINDOW_BITS) atomicOr(&L.u.so.bits[u >> 5], 1u << (u & 31));
+                }
+                __syncwarp();
+                int carry = placed;
+                for (int w0 = 0; w0 < nwords; w0 += 32) {
+                    const int wd = w0 + lane;
+                    const int c = wd < nwords ? __popc(L.u.so.bits[wd]) : 0;
+                    int incl = c;
+                    for (int off = 1; off < 32; off <<= 1) {
+                        const int y = __shfl_up_sync(FULL_MASK, incl, off);
+                        if (lane >= off) incl += y;
+                    }
+                    if (wd < nwords) L.u.so.wpre[wd] = (uint16_t)(carry - placed + incl - c);
+                    carry += __shfl_sync(FULL_MASK, incl, 31);
+                }
+                __syncwarp();
+                for (int e = lane; e < m; e += 32) {
+                    const uint32_t u = L.u.so.ur[e] - (uint32_t)wb;
+                    if (u < (uint32_t)SORT_WINDOW_BITS) {
+                        const uint32_t word = L.u.so.bits[u >> 5];
+                        Sa[placed + L.u.so.wpre[u >> 5] + __popc(word & ((1u << (u & 31)) - 1u))] = (uint16_t)e;
+                    }
+                }
+                __syncwarp();
+                for (int e = lane; e < m; e += 32) {
+                    const uint32_t u = L.u.so.ur[e] - (uint32_t)wb;
+                    if (u < (uint32_t)SORT_WINDOW_BITS) L.u.so.bits[u >> 5] = 0u;
+                }
+                __syncwarp();
+                placed = carry;
+            }
+            if (placed != m) {  // an atom twice in the list: not a permutation
+                complete = false;
+                break;
+            }
+            // dense ranks: a new run wherever the strict-lower rank changes
+            int c0 = 0;
+            uint32_t prev = 0;
+#pragma unroll 2
+            for (int p0 = 0; p0 < m; p0 += 32) {
+                const int p = p0 + lane;
+                const int e = p < m ? Sa[p] : 0;
+                const uint32_t l = p < m ? lrk[ca[e]] : 0u;
+                uint32_t before = __shfl_up_sync(FULL_MASK, l, 1);
+                if (lane == 0) before = prev;
+                const bool chg = p < m && (p == 0 || l != before);
+                const unsigned mask = __ballot_sync(FULL_MASK, chg);
+                if (p < m) L.run[a][e] = (uint16_t)(c0 + __popc(mask & (lt | (1u << lane))) - 1);
+                c0 += __popc(mask);
+                prev = __shfl_sync(FULL_MASK, l, 31);
+            }
+            __syncwarp();
+        }
+
+        // (2) level-by-level median splits
+        bool bail = !complete;
+        for (int p = lane; p < m; p += 32) L.u.sp.seg[p] = (uint32_t)m << 16;
+        __syncwarp();
+        int cur0 = 0, cur1 = 1, cur2 = 2, spare = 3;
+        int nd = 0;
+        int levels = 0;
+        while ((1 << levels) < m) levels++;
+        for (int d = 0; d < levels && !bail; d++) {
+            const int a = d % 3;
+            const int ca_buf = a == 0 ? cur0 : a == 1 ? cur1 : cur2;
+            const uint16_t *Sa = L.buf[ca_buf];
+            const uint16_t *Ra = L.run[a];
+            int ntied = 0;
+            for (int p0 = 0; p0 < m; p0 += 32) {
+                const int p = p0 + lane;
+                bool tie = false;
+                int lo = 0;
+                if (p < m) {
+                    const uint32_t sg = L.u.sp.seg[p];
+                    lo = (int)(sg & 0xFFFFu);
+                    const int n = (int)(sg >> 16), k = n >> 1;
+                    const int e = Sa[p];
+                    L.u.sp.flag[e] = (uint8_t)(n >= 2 && p < lo + k);
+                    if (n >= 2 && p == lo + k) tie = Ra[Sa[p - 1]] == Ra[e];
+                }
+                const unsigned mask = __ballot_sync(FULL_MASK, tie);
+                if (tie) {
+                    const int slot = ntied + __popc(mask & lt);
+                    if (slot < LEAF_MAX_TIED) L.u.sp.tied[slot] = (uint16_t)lo;
+                }
+                ntied += __popc(mask);
+            }
+            __syncwarp();
+            if (ntied > LEAF_MAX_TIED) {
+                bail = true;
+                break;
+            }
+            for (int t = 0; t < ntied && !bail; t++) {
+                const int tlo = L.u.sp.tied[t];
+                const int tn = (int)(L.u.sp.seg[tlo] >> 16);
+                int lj = 0, nj = m;
+                for (int j = 0; j <= d; j++) {
+                    if (j > 0) {
+                        // child of the level j-1 node (lj, nj) holding tlo
+                        const int k = nj >> 1;
+                        if (tlo < lj + k) nj = k;
+                        else {
+                            lj += k;
+                            nj -= k;
+                        }
+                    }
+                    const uint32_t tag = ((uint32_t)j << 16) | (uint32_t)lj;
+                    bool seen = false;
+                    for (int q = lane; q < nd; q += 32) seen |= L.u.sp.done[q] == tag;
+                    if (__any_sync(FULL_MASK, seen)) continue;
+                    if (nd == LEAF_MAX_REPLAY) {
+                        bail = true;
+                        break;
+                    }
+                    if (nd == 0) {
+                        for (int p = lane; p < m; p += 32) L.u.sp.A[p] = (uint16_t)p;
+                        __syncwarp();
+                    }
+                    warp_qselect(L.u.sp.A, L.run[j % 3], L.buf[spare], L.u.sp.F, L.u.sp.PTR, lj, nj,
+                                 &counters[C_ERROR]);
+                    if (lane == 0) L.u.sp.done[nd] = tag;
+                    nd++;
+                    n_replay++;
+                    __syncwarp();
+                }
+                if (bail) break;
+                // the tied node's members from its qselect arrangement
+                for (int p = tlo + lane; p < tlo + tn; p += 32)
+                    L.u.sp.flag[L.u.sp.A[p]] = (uint8_t)(p < tlo + (tn >> 1));
+                __syncwarp();
+            }
+            if (bail) break;
+            // stable partition of the orders within each node
+            bool bad = false;
+            for (int b = 0; b < 3; b++) {
+                if (b == a && ntied == 0) continue;
+                const int cb = b == 0 ? cur0 : b == 1 ? cur1 : cur2;
+                const uint16_t *src = L.buf[cb];
+                uint16_t *dst = L.buf[spare];
+                int carry = 0;
+                for (int p0 = 0; p0 < m; p0 += 32) {
+                    const int p = p0 + lane;
+                    const bool valid = p < m;
+                    const int e = valid ? src[p] : 0;
+                    const bool f = valid && L.u.sp.flag[e];
+                    const unsigned mask = __ballot_sync(FULL_MASK, f);
+                    const int Fp = carry + __popc(mask & lt);
+                    if (valid) L.u.sp.F[p] = (uint16_t)Fp;
+                    carry += __popc(mask);
+                    __syncwarp();
+                    if (valid) {
+                        const uint32_t sg = L.u.sp.seg[p];
+                        const int lo = (int)(sg & 0xFFFFu), n = (int)(sg >> 16);
+                        int to = p;
+                        if (n >= 2) {
+                            const int k = n >> 1;
+                            const int lb = Fp - L.u.sp.F[lo];
+                            to = f ? lo + lb : lo + k + (p - lo) - lb;
+                            // inside the node by construction (exactly k
+                            // left members); checked all the same
+                            if (to < lo || to >= lo + n) {
+                                bad = true;
+                                to = p;
+                            }
+                        }
+                        dst[to] = (uint16_t)e;
+                    }
+                }
+                __syncwarp();
+                if (b == 0) cur0 = spare;
+                else if (b == 1) cur1 = spare;
+                else cur2 = spare;
+                spare = cb;
+            }
+            if (__any_sync(FULL_MASK, bad)) {
+                if (lane == 0) atomicMax(&counters[C_ERROR], 6ull);
+                bail = true;
+                break;
+            }
+            for (int p = lane; p < m; p += 32) {
+                const uint32_t sg = L.u.sp.seg[p];
+                const int lo = (int)(sg & 0xFFFFu), n = (int)(sg >> 16);
+                if (n >= 2) {
+                    const int k = n >> 1;
+                    L.u.sp.seg[p] = p < lo + k ? ((uint32_t)lo | ((uint32_t)k << 16))
+                                               : ((uint32_t)(lo + k) | ((uint32_t)(n - k) << 16));
+                }
+            }
+            __syncwarp();
+        }
+        if (bail) {
+            n_exact++;
+            if (lane == 0) exact_list[atomicAdd(exact_count, 1ull)] = w;
+            __syncwarp();
+            continue;
+        }
+        write_leaves(L.buf[cur0], m, o, ca, cand_xyz, leaf_atom, leaf_xyz, blk_offset[w], blk_lo, blk_hi);
+    }
+    if (lane == 0 && n_exact) atomicAdd(&counters[C_LEAF_EXACT], n_exact);
+    if (lane == 0 && n_replay) atomicAdd(&counters[C_LEAF_REPLAY], n_replay);
 }
 
 __global__ void k_block_counts(int64_t n, const int32_t *count, int32_t *nblk) {
@@ -1752,15 +2219,43 @@ void launch_scan_add(cudaStream_t st, int64_t *out, int64_t n, const int64_t *ti
 void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t n_sigs, const int32_t *count,
                        const int64_t *offset, const int64_t *blk_offset, const int32_t *cand_atom,
                        const float4 *cand_xyz, int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
+                       int64_t *sorted_list, unsigned long long *sorted_count, int64_t list_cap,
                        int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters) {
+    cudaMemsetAsync(sorted_count, 0, 3 * sizeof(unsigned long long), st);
     cudaMemsetAsync(exact_count, 0, sizeof(unsigned long long), st);
+    // lists longer than rank_max take the sorted-axis split (the rank
+    // method costs O(m^2) a level); PJG_LEAF_RANK_MAX overrides the crossover
+    static const int rank_max = [] {
+        const char *v = getenv("PJG_LEAF_RANK_MAX");
+        int r = v ? atoi(v) : LEAF_RANK_MAX;
+        return r < 1 ? 1 : r > LEAF_FAST_MAX ? LEAF_FAST_MAX : r;
+    }();
     k_leaf_order<<<blocks, LEAF_WARPS * 32, 0, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, cand_xyz,
-                                                    leaf_atom, leaf_xyz, blk_lo, blk_hi, exact_list, exact_count,
-                                                    counters);
+                                                    leaf_atom, leaf_xyz, blk_lo, blk_hi, sorted_list, sorted_count,
+                                                    list_cap, exact_list, exact_count, counters, rank_max);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    // lists up to 1024 entries: 16 KB a warp, 4 warps a block
+    // sorted-axis split, one worklist per size class: up to 512 entries
+    // 13 KB a warp (4 warps a block), up to 1024 25 KB (2 a block), up to
+    // LEAF_SORTED_MAX 50 KB (1 a block)
+    constexpr int SS0 = (int)sizeof(SortedWarp<512>) * 4;
+    cudaFuncSetAttribute(k_leaf_sorted<512, 0, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, SS0);
+    k_leaf_sorted<512, 0, 4><<<sms * 4, 128, SS0, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, cand_xyz,
+                                                       leaf_atom, leaf_xyz, blk_lo, blk_hi, sorted_list,
+                                                       sorted_count, exact_list, exact_count, counters);
+    constexpr int SS1 = (int)sizeof(SortedWarp<1024>) * 2;
+    cudaFuncSetAttribute(k_leaf_sorted<1024, 512, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, SS1);
+    k_leaf_sorted<1024, 512, 2><<<sms * 4, 64, SS1, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom,
+                                                         cand_xyz, leaf_atom, leaf_xyz, blk_lo, blk_hi,
+                                                         sorted_list + list_cap, sorted_count + 1, exact_list,
+                                                         exact_count, counters);
+    constexpr int SS2 = (int)sizeof(SortedWarp<LEAF_SORTED_MAX>);
+    cudaFuncSetAttribute(k_leaf_sorted<LEAF_SORTED_MAX, 1024, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SS2);
+    k_leaf_sorted<LEAF_SORTED_MAX, 1024, 1><<<sms * 4, 32, SS2, st>>>(
+        cv, n_sigs, count, offset, blk_offset, cand_atom, cand_xyz, leaf_atom, leaf_xyz, blk_lo, blk_hi,
+        sorted_list + 2 * list_cap, sorted_count + 2, exact_list, exact_count, counters);
+    // exact replay: lists up to 1024 entries 16 KB a warp, 4 warps a block
     constexpr int SM1 = 1024 * 16 * 4;
     cudaFuncSetAttribute(k_leaf_exact<1024, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM1);
     k_leaf_exact<1024, 0><<<sms * 3, 128, SM1, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, cand_xyz,
@@ -1773,6 +2268,15 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
     k_leaf_exact<EXACT_MAX, 1024><<<sms * 3, 32, SM2, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom,
                                                            cand_xyz, leaf_atom, leaf_xyz, blk_lo, blk_hi,
                                                            exact_list, exact_count, counters);
+}
+
+void launch_axis_ranks(cudaStream_t st, int32_t n_structures, const int64_t *atom_base, const int32_t *atom_count,
+                       const double *xyz64, int64_t n_atoms, unsigned long long *tile_key, uint16_t *tile_idx,
+                       uint32_t *lrank, uint32_t *urank, uint8_t *special) {
+    if (n_structures <= 0) return;
+    cudaMemsetAsync(special, 0, (size_t)n_structures, st);
+    k_axis_ranks<<<dim3((unsigned)n_structures, 3), RANK_THREADS, 0, st>>>(atom_base, atom_count, xyz64, n_atoms,
+                                                                          tile_key, tile_idx, lrank, urank, special);
 }
 
 void launch_block_counts(cudaStream_t st, int64_t n, const int32_t *count, int32_t *nblk) {
@@ -1816,10 +2320,9 @@ void launch_superpose(cudaStream_t st, int blocks, const ChunkView &cv, const Te
 // ---------------------------------------------------------------------------
 // Superposition without allocation (pjg_superpose_noalloc).
 //
-// For callers that cannot allocate device memory while they run -- code
-// recorded into a CUDA graph, a real-time loop that must not block on the
-// allocator, or a host application whose memory manager owns every device
-// allocation -- this variant of k_superpose takes the assignments' molecule
+// For callers that cannot allocate device memory while they run -- a
+// real-time loop that must not block on the allocator, or a host
+// application whose memory manager owns every device allocation -- this variant of k_superpose takes the assignments' molecule
 // coordinates and the template's coordinates directly from the caller,
 // writes the caller's output arrays, and keeps its only scratch (one pass
 // flag per row, for the order-preserving compaction of the rows under the

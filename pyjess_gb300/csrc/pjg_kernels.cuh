@@ -15,8 +15,11 @@ namespace pjg {
 #endif
 
 constexpr int SEARCH_WARPS = 8;        // warps per block of k_search
-constexpr int LEAF_WARPS = 4;          // warps per block of k_leaf_order (shared memory: 8.5 KB a warp)
-constexpr int LEAF_FAST_MAX = 384;     // longest list ordered in shared memory
+constexpr int LEAF_WARPS = 4;          // warps per block of k_leaf_order
+constexpr int LEAF_FAST_MAX = 256;     // capacity of the rank method's buffers
+constexpr int LEAF_RANK_MAX = 128;     // default: longest list ordered by the rank method
+constexpr int LEAF_SORTED_MAX = 2048;  // longest list ordered by sorted axes
+constexpr int LEAF_SORT_MAX = 1024;    // longest list ordered by presorted axes
 constexpr int EXACT_MAX = 4096;        // longest list replayed warp-parallel
 
 struct SearchArgs {
@@ -82,7 +85,15 @@ void launch_scan_add(cudaStream_t st, int64_t *out, int64_t n, const int64_t *ti
 void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t n_sigs, const int32_t *count,
                        const int64_t *offset, const int64_t *blk_offset, const int32_t *cand_atom,
                        const float4 *cand_xyz, int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
+                       int64_t *sorted_list, unsigned long long *sorted_count, int64_t list_cap,
                        int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters);
+
+// per-structure axis ranks (lrank, urank: [3][n_atoms], structure-local
+// values; special[s] = 1 for a structure with a NaN coordinate); tile_key /
+// tile_idx: scratch of 3 * n_atoms entries
+void launch_axis_ranks(cudaStream_t st, int32_t n_structures, const int64_t *atom_base, const int32_t *atom_count,
+                       const double *xyz64, int64_t n_atoms, unsigned long long *tile_key, uint16_t *tile_idx,
+                       uint32_t *lrank, uint32_t *urank, uint8_t *special);
 
 // blocks of 32 leaves per list: ceil(count / 32)
 void launch_block_counts(cudaStream_t st, int64_t n, const int32_t *count, int32_t *nblk);
