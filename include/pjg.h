@@ -169,7 +169,10 @@ void pjg_templates_destroy(pjg_templates *t);
 /* Replaces Molecule creation + ResIndex_create (patches/ResIndex.c.patch
  * :24-119, src/pyjess/_jess.pyx:632-684): sorts each structure's atoms by
  * (residue name, serial), builds the residue buckets and the FP64 and
- * centroid-relative FP32 coordinate arrays, and uploads them. */
+ * centroid-relative FP32 coordinate arrays, uploads them and ranks every
+ * atom along each axis on the device (the kd leaf order's sorted-axis path).
+ * A non-finite coordinate returns PJG_ERR_INVALID (the reference accepts
+ * one: there a NaN atom passes every distance test). */
 pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **out);
 
 /* Replaces Molecule_free. */

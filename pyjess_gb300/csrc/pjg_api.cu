@@ -151,7 +151,6 @@ struct pjg_structures {
     int32_t *d_bucket_begin = nullptr, *d_bucket_lo = nullptr, *d_bucket_hi = nullptr;
     uint32_t *d_bucket_name = nullptr;
     uint32_t *d_lrank = nullptr, *d_urank = nullptr;  // [3][N] axis ranks
-    uint8_t *d_special = nullptr;                     // [S] NaN coordinate
     int device = 0;
 };
 
@@ -381,6 +380,12 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
             return fail(PJG_ERR_INVALID, "structure %d too large", s);
         }
         int n = (int)(b1 - b0);
+        for (int64_t i = 3 * b0; i < 3 * b1; i++)
+            if (!std::isfinite(set->xyz[i])) {
+                delete h;
+                return fail(PJG_ERR_INVALID, "structure %d atom %lld: non-finite coordinate", s,
+                            (long long)(i / 3 - b0));
+            }
         base[s] = b0;
         count[s] = n;
         h->max_atoms = std::max(h->max_atoms, n);
@@ -446,12 +451,11 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
         uint16_t *tile_idx = nullptr;
         e = cudaMalloc((void **)&h->d_lrank, n3 * sizeof(uint32_t));
         if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_urank, n3 * sizeof(uint32_t));
-        if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_special, std::max(S, 1));
         if (e == cudaSuccess) e = cudaMalloc((void **)&tile_key, n3 * sizeof(unsigned long long));
         if (e == cudaSuccess) e = cudaMalloc((void **)&tile_idx, n3 * sizeof(uint16_t));
         if (e == cudaSuccess) {
             launch_axis_ranks(0, S, h->d_atom_base, h->d_atom_count, h->d_xyz64, N, tile_key, tile_idx, h->d_lrank,
-                              h->d_urank, h->d_special);
+                              h->d_urank);
             e = cudaGetLastError();
             if (e == cudaSuccess) e = cudaDeviceSynchronize();
         }
@@ -472,7 +476,7 @@ void pjg_structures_destroy(pjg_structures *h) {
     if (!h) return;
     void *ptrs[] = {h->d_atom_base, h->d_atom_count, h->d_xyz64, h->d_xyz32, h->d_name, h->d_resname,
                     h->d_sorted, h->d_bucket_begin, h->d_bucket_name, h->d_bucket_lo, h->d_bucket_hi,
-                    h->d_lrank, h->d_urank, h->d_special};
+                    h->d_lrank, h->d_urank};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete h;
@@ -611,7 +615,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
         CUDA_TRY(dalloc(d_totals, (size_t)S, st));
         ChunkView cv{S, sp->d_atom_base, sp->d_atom_count, sp->d_xyz64, sp->d_xyz32, sp->d_name, sp->d_resname,
                      sp->d_sorted, sp->d_bucket_begin, sp->d_bucket_name, sp->d_bucket_lo, sp->d_bucket_hi,
-                     sp->N, sp->d_lrank, sp->d_urank, sp->d_special};
+                     sp->N, sp->d_lrank, sp->d_urank};
         SigView sv{G, tp->d_code, tp->d_rule, tp->d_mainchain, tp->d_name_begin, tp->d_names, tp->d_res_begin,
                    tp->d_resnames, tp->d_partner_begin, tp->d_partner_res, tp->d_partner_name};
         int blocks = (int)std::min<int64_t>((W + 7) / 8, (int64_t)sm_count() * 32);
@@ -646,7 +650,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             const int64_t Wc = (int64_t)Sc * G;
             ChunkView cv{Sc, sp->d_atom_base + s0, sp->d_atom_count + s0, sp->d_xyz64, sp->d_xyz32, sp->d_name,
                          sp->d_resname, sp->d_sorted, sp->d_bucket_begin + s0, sp->d_bucket_name, sp->d_bucket_lo,
-                         sp->d_bucket_hi, sp->N, sp->d_lrank, sp->d_urank, sp->d_special + s0};
+                         sp->d_bucket_hi, sp->N, sp->d_lrank, sp->d_urank};
             SigView sv{G, tp->d_code, tp->d_rule, tp->d_mainchain, tp->d_name_begin, tp->d_names, tp->d_res_begin,
                        tp->d_resnames, tp->d_partner_begin, tp->d_partner_res, tp->d_partner_name};
             int32_t *cnt_c = d_count.p + (int64_t)s0 * G;

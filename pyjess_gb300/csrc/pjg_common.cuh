@@ -70,7 +70,6 @@ struct ChunkView {
     int64_t n_atoms;              // atoms of the whole structure set
     const uint32_t *lrank;        // [3][n_atoms] strict-lower axis rank
     const uint32_t *urank;        // [3][n_atoms] unique axis rank
-    const uint8_t *special;       // [S] a NaN coordinate (exact leaf order only)
 };
 
 struct SigView {

@@ -358,18 +358,9 @@ struct LeafWarp {
     uint16_t seg_n[LEAF_FAST_MAX];
 };
 
-// Leaf order of a list from its partitioned candidate array `order`
-// (read backwards: the right subtree is visited first), plus the bounding
-// boxes of its blocks of 32 consecutive leaves.
-__device__ void write_leaves(const uint16_t *order, int m, int64_t o, const int32_t *ca, const float4 *cand_xyz,
-                             int32_t *leaf_atom, float4 *leaf_xyz, int64_t bo, float4 *blk_lo, float4 *blk_hi) {
+// Bounding boxes of the blocks of 32 consecutive leaves of a list.
+__device__ void write_boxes(int m, int64_t o, const float4 *leaf_xyz, int64_t bo, float4 *blk_lo, float4 *blk_hi) {
     const int lane = lane_id();
-    for (int r = lane; r < m; r += 32) {
-        int e = order[m - 1 - r];
-        leaf_atom[o + r] = ca[e];
-        leaf_xyz[o + r] = cand_xyz[o + e];
-    }
-    __syncwarp();
     for (int b = 0; b * 32 < m; b++) {
         int r = b * 32 + lane;
         float4 p = leaf_xyz[o + (r < m ? r : b * 32)];
@@ -390,10 +381,23 @@ __device__ void write_leaves(const uint16_t *order, int m, int64_t o, const int3
     __syncwarp();
 }
 
+// Leaf order of a list from its partitioned candidate array `order`
+// (read backwards: the right subtree is visited first), plus its block boxes.
+__device__ void write_leaves(const uint16_t *order, int m, int64_t o, const int32_t *ca, const float4 *cand_xyz,
+                             int32_t *leaf_atom, float4 *leaf_xyz, int64_t bo, float4 *blk_lo, float4 *blk_hi) {
+    const int lane = lane_id();
+    for (int r = lane; r < m; r += 32) {
+        int e = order[m - 1 - r];
+        leaf_atom[o + r] = ca[e];
+        leaf_xyz[o + r] = cand_xyz[o + e];
+    }
+    __syncwarp();
+    write_boxes(m, o, leaf_xyz, bo, blk_lo, blk_hi);
+}
+
 // Short lists (at most rank_max entries) without a tie: rank method, one
-// warp per list.  Longer or tied lists go to k_leaf_sorted's worklist (up
-// to LEAF_SORTED_MAX entries), the rest -- and every list of a structure
-// with a NaN coordinate -- to k_leaf_exact's.
+// warp per list.  Longer or tied lists go to k_leaf_sorted's worklists (up
+// to LEAF_SORTED_MAX entries), the rest to k_leaf_exact's.
 __global__ void __launch_bounds__(LEAF_WARPS * 32)
     k_leaf_order(ChunkView cv, int32_t n_sigs, const int32_t *count, const int64_t *offset,
                  const int64_t *blk_offset, const int32_t *cand_atom, const float4 *cand_xyz,
@@ -410,12 +414,6 @@ __global__ void __launch_bounds__(LEAF_WARPS * 32)
     for (int64_t w = warp; w < total; w += nwarps) {
         const int m = count[w];
         if (m <= 0) continue;
-        const int s = (int)(w / n_sigs);
-        if (cv.special[s]) {
-            n_exact++;
-            if (lane == 0) exact_list[atomicAdd(exact_count, 1ull)] = w;
-            continue;
-        }
         const int64_t o = offset[w];
         bool tie = m > rank_max;
         int src = 0;
@@ -789,25 +787,7 @@ __global__ void k_leaf_exact(ChunkView cv, int32_t n_sigs, const int32_t *count,
             }
         }
         __syncwarp();
-        const int64_t bo = blk_offset[w];
-        for (int b = 0; b * 32 < m; b++) {
-            int r = b * 32 + lane;
-            float4 p = leaf_xyz[o + (r < m ? r : b * 32)];
-            float mnx = p.x, mny = p.y, mnz = p.z, mxx = p.x, mxy = p.y, mxz = p.z;
-            for (int off = 16; off; off >>= 1) {
-                mnx = fminf(mnx, __shfl_xor_sync(FULL_MASK, mnx, off));
-                mny = fminf(mny, __shfl_xor_sync(FULL_MASK, mny, off));
-                mnz = fminf(mnz, __shfl_xor_sync(FULL_MASK, mnz, off));
-                mxx = fmaxf(mxx, __shfl_xor_sync(FULL_MASK, mxx, off));
-                mxy = fmaxf(mxy, __shfl_xor_sync(FULL_MASK, mxy, off));
-                mxz = fmaxf(mxz, __shfl_xor_sync(FULL_MASK, mxz, off));
-            }
-            if (lane == 0) {
-                blk_lo[bo + b] = make_float4(mnx, mny, mnz, 0.f);
-                blk_hi[bo + b] = make_float4(mxx, mxy, mxz, 0.f);
-            }
-        }
-        __syncwarp();
+        write_boxes(m, o, leaf_xyz, blk_offset[w], blk_lo, blk_hi);
     }
 }
 
@@ -817,9 +797,9 @@ __global__ void k_leaf_exact(ChunkView cv, int32_t n_sigs, const int32_t *count,
 // For atom i and axis a: lrank = number of the structure's atoms whose
 // coordinate on a is strictly smaller, so lranks compare exactly as the FP64
 // coordinates do (equal coordinates share one); urank = number of atoms
-// before i in (coordinate, index) order, a permutation of 0..n-1.  A
-// coordinate that is NaN has no place in that order: the structure is
-// flagged in `special` and its lists take the exact replay.  One block per
+// before i in (coordinate, index) order, a permutation of 0..n-1
+// (coordinates are finite: pjg_structures_create rejects others).  One
+// block per
 // (structure, axis): the atoms are sorted in tiles of RANK_TILE in shared
 // memory, each tile is stored, and every atom's ranks are sums of binary
 // searches over the sorted tiles.
@@ -835,8 +815,7 @@ __device__ __forceinline__ unsigned long long order_key(double x) {
 
 __global__ void __launch_bounds__(RANK_THREADS)
     k_axis_ranks(const int64_t *atom_base, const int32_t *atom_count, const double *xyz64, int64_t n_atoms,
-                 unsigned long long *tile_key, uint16_t *tile_idx, uint32_t *lrank, uint32_t *urank,
-                 uint8_t *special) {
+                 unsigned long long *tile_key, uint16_t *tile_idx, uint32_t *lrank, uint32_t *urank) {
     __shared__ unsigned long long key[RANK_TILE];
     __shared__ uint16_t idx[RANK_TILE];
     const int s = blockIdx.x, a = blockIdx.y;
@@ -845,14 +824,11 @@ __global__ void __launch_bounds__(RANK_THREADS)
     const int tiles = (n + RANK_TILE - 1) / RANK_TILE;
     unsigned long long *gk = tile_key + a * n_atoms + b0;
     uint16_t *gi = tile_idx + a * n_atoms + b0;
-    int nan = 0;
     for (int t = 0; t < tiles; t++) {
         const int t0 = t * RANK_TILE, tn = min(RANK_TILE, n - t0);
         for (int i = threadIdx.x; i < RANK_TILE; i += blockDim.x) {
             if (i < tn) {
-                const double x = xyz64[3 * (b0 + t0 + i) + a];
-                nan |= x != x;
-                key[i] = order_key(x);
+                key[i] = order_key(xyz64[3 * (b0 + t0 + i) + a]);
             } else {
                 key[i] = ~0ull;
             }
@@ -886,7 +862,6 @@ __global__ void __launch_bounds__(RANK_THREADS)
         }
         __syncthreads();
     }
-    if (__syncthreads_or(nan) && threadIdx.x == 0) special[s] = 1;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const unsigned long long ki = order_key(xyz64[3 * (b0 + i) + a]);
         const int ti = i / RANK_TILE;
@@ -2272,11 +2247,10 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
 
 void launch_axis_ranks(cudaStream_t st, int32_t n_structures, const int64_t *atom_base, const int32_t *atom_count,
                        const double *xyz64, int64_t n_atoms, unsigned long long *tile_key, uint16_t *tile_idx,
-                       uint32_t *lrank, uint32_t *urank, uint8_t *special) {
+                       uint32_t *lrank, uint32_t *urank) {
     if (n_structures <= 0) return;
-    cudaMemsetAsync(special, 0, (size_t)n_structures, st);
     k_axis_ranks<<<dim3((unsigned)n_structures, 3), RANK_THREADS, 0, st>>>(atom_base, atom_count, xyz64, n_atoms,
-                                                                          tile_key, tile_idx, lrank, urank, special);
+                                                                          tile_key, tile_idx, lrank, urank);
 }
 
 void launch_block_counts(cudaStream_t st, int64_t n, const int32_t *count, int32_t *nblk) {

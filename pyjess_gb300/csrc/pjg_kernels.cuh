@@ -89,11 +89,10 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
                        int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters);
 
 // per-structure axis ranks (lrank, urank: [3][n_atoms], structure-local
-// values; special[s] = 1 for a structure with a NaN coordinate); tile_key /
-// tile_idx: scratch of 3 * n_atoms entries
+// values); tile_key / tile_idx: scratch of 3 * n_atoms entries
 void launch_axis_ranks(cudaStream_t st, int32_t n_structures, const int64_t *atom_base, const int32_t *atom_count,
                        const double *xyz64, int64_t n_atoms, unsigned long long *tile_key, uint16_t *tile_idx,
-                       uint32_t *lrank, uint32_t *urank, uint8_t *special);
+                       uint32_t *lrank, uint32_t *urank);
 
 // blocks of 32 leaves per list: ceil(count / 32)
 void launch_block_counts(cudaStream_t st, int64_t n, const int32_t *count, int32_t *nblk);
