@@ -272,16 +272,23 @@ def main():
             "atom_offset", "code", "res_seq", "chain", "xyz", "dist_weight", "name_offset", "names",
             "resname_offset", "resnames", "dim"))
         times, d2h = [], 0
+        phases = {"templates_create": 0.0, "structures_create": 0.0, "query": 0.0, "results_copy": 0.0}
         for i in range(args.warmup + args.steps):
             t1 = time.perf_counter()
             tp2 = _native.Templates(wl.templates)
+            t2 = time.perf_counter()
             st2 = _native.Structures(wl.structures)
+            t3 = time.perf_counter()
             r2 = _native.query(tp2, st2, P)
+            t4 = time.perf_counter()
             a2 = r2.arrays()
+            t5 = time.perf_counter()
             del tp2, st2
             dt = time.perf_counter() - t1
             if i >= args.warmup:
                 times.append(dt)
+                for k, v in zip(phases, (t2 - t1, t3 - t2, t4 - t3, t5 - t4)):
+                    phases[k] += 1e3 * v / args.steps
             d2h = sum(v.nbytes for k, v in a2.items() if hasattr(v, "nbytes"))
         tot = sum(times)
         if dist:
@@ -291,7 +298,7 @@ def main():
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             tot = float(t.item())
         e2e = {"value": pairs_step * world * args.steps / tot, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h)}
+               "d2h_bytes_per_step": int(d2h), "phases_ms": {k: round(v, 1) for k, v in phases.items()}}
 
     # ---- CPU baseline (rank 0, N=1)
     cpu = None

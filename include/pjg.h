@@ -184,8 +184,9 @@ void pjg_structures_destroy(pjg_structures *s);
  * JessQuery_superposition + the Query.__next__ automaton
  * (patches/Jess.c.patch:74-216, patches/Scanner.c.patch:110-336,
  * src/pyjess/_jess.pyx:2197-2283) for every structure of `s` against every
- * template of `t`.  Results are ordered by structure, then by template in
- * reverse index order, then by the reference's candidate order. */
+ * template of `t`, all on the device.  Results are ordered by structure,
+ * then by template in reverse index order, then by the reference's
+ * candidate order. */
 pjg_status pjg_query(const pjg_templates *t, const pjg_structures *s,
                      const pjg_query_params *params, pjg_results **out);
 
@@ -195,7 +196,8 @@ int64_t pjg_results_count(const pjg_results *r);
 /* Sum over hits of the template atom count (size of the atom index array). */
 int64_t pjg_results_atom_count(const pjg_results *r);
 
-/* Copy the hits out.  Each array may be NULL to skip it.
+/* Copy the hits out (host arrays; the hits stay on the device until
+ * pjg_results_destroy).  Each array may be NULL to skip it.
  *   structure[i], template_index[i]    which pair hit i belongs to
  *   ordinal[i]     position of hit i in its pair's candidate stream
  *   rmsd[i]        Superposition_rmsd

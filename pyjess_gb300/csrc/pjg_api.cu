@@ -24,7 +24,9 @@
 #include <cstring>
 #include <map>
 #include <numeric>
+#include <atomic>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/pjg.h"
@@ -154,25 +156,91 @@ struct pjg_structures {
     int device = 0;
 };
 
-struct HitRec {
-    int32_t s, t;
-    int64_t ordinal;
-    double rmsd;
-    int32_t nan_rot;
-    double rot[9], centres[6];
-    int64_t atom_at;  // into atom store
+// Hits and warnings of a query, on the device: contiguous arrays that grow
+// (doubling) as chunks append to them.
+struct HitStore {
+    int64_t hits = 0, atoms = 0, warns = 0;           // in use
+    int64_t cap_h = 0, cap_a = 0, cap_w = 0;          // allocated
+    int32_t *structure = nullptr, *tpl = nullptr, *atoms_ = nullptr, *warn_structure = nullptr;
+    int64_t *ordinal = nullptr, *atom_offset = nullptr, *warn_before = nullptr;
+    double *rmsd = nullptr, *rot = nullptr, *centres = nullptr;
+
+    template <typename T>
+    static cudaError_t grow(T **p, int64_t used, int64_t cap, int64_t width, cudaStream_t st) {
+        T *q = nullptr;
+        cudaError_t e = cudaMalloc((void **)&q, (size_t)std::max<int64_t>(cap, 1) * width * sizeof(T));
+        if (e != cudaSuccess) return e;
+        if (*p && used > 0) e = cudaMemcpyAsync(q, *p, (size_t)used * width * sizeof(T), cudaMemcpyDeviceToDevice, st);
+        if (*p) {
+            cudaStreamSynchronize(st);
+            cudaFree(*p);
+        }
+        *p = q;
+        return e;
+    }
+    // room for `h` more hits, `a` more atoms, `w` more warnings
+    cudaError_t reserve(int64_t h, int64_t a, int64_t w, cudaStream_t st) {
+        cudaError_t e = cudaSuccess;
+        if (hits + h > cap_h) {
+            int64_t c = std::max<int64_t>(hits + h, 2 * cap_h);
+            if (e == cudaSuccess) e = grow(&structure, hits, c, 1, st);
+            if (e == cudaSuccess) e = grow(&tpl, hits, c, 1, st);
+            if (e == cudaSuccess) e = grow(&ordinal, hits, c, 1, st);
+            if (e == cudaSuccess) e = grow(&atom_offset, hits, c + 1, 1, st);
+            if (e == cudaSuccess) e = grow(&rmsd, hits, c, 1, st);
+            if (e == cudaSuccess) e = grow(&rot, hits, c, 9, st);
+            if (e == cudaSuccess) e = grow(&centres, hits, c, 6, st);
+            if (e == cudaSuccess) cap_h = c;
+        }
+        if (atoms + a > cap_a && e == cudaSuccess) {
+            int64_t c = std::max<int64_t>(atoms + a, 2 * cap_a);
+            e = grow(&atoms_, atoms, c, 1, st);
+            if (e == cudaSuccess) cap_a = c;
+        }
+        if (warns + w > cap_w && e == cudaSuccess) {
+            int64_t c = std::max<int64_t>(warns + w, 2 * cap_w);
+            e = grow(&warn_structure, warns, c, 1, st);
+            if (e == cudaSuccess) e = grow(&warn_before, warns, c, 1, st);
+            if (e == cudaSuccess) cap_w = c;
+        }
+        return e;
+    }
+    // the segment view at the current ends
+    HitSegment tail() const {
+        return HitSegment{structure + hits, tpl + hits, ordinal + hits, rmsd + hits, rot + 9 * hits,
+                          centres + 6 * hits, atom_offset + hits, atoms_ + atoms, warn_structure + warns,
+                          warn_before + warns};
+    }
+    ~HitStore() {
+        void *ptrs[] = {structure, tpl, atoms_, warn_structure, ordinal, atom_offset, warn_before, rmsd, rot, centres};
+        for (void *p : ptrs)
+            if (p) cudaFree(p);
+    }
 };
 
 struct pjg_results {
-    std::vector<int32_t> structure, tpl;
-    std::vector<int64_t> ordinal;
-    std::vector<double> rmsd, rot, centres;
-    std::vector<int64_t> atom_offset{0};
-    std::vector<int32_t> atoms;
-    std::vector<int32_t> warn_structure;
-    std::vector<int64_t> warn_before;
+    HitStore store;
     pjg_stats stats{};
+    int device = 0;
 };
+
+namespace {
+
+// Device-to-host copy into caller memory: pinned for the duration of the
+// copy when it is large (one DMA at full link speed), plain otherwise.
+cudaError_t copy_out(void *dst, const void *src, size_t bytes) {
+    if (!dst || bytes == 0) return cudaSuccess;
+    bool reg = false;
+    if (bytes >= (16u << 20)) {
+        reg = cudaHostRegister(dst, bytes, cudaHostRegisterDefault) == cudaSuccess;
+        if (!reg) cudaGetLastError();  // not pinnable here: plain copy
+    }
+    cudaError_t e = cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost);
+    if (reg) cudaHostUnregister(dst);
+    return e;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -379,7 +447,6 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
             delete h;
             return fail(PJG_ERR_INVALID, "structure %d too large", s);
         }
-        int n = (int)(b1 - b0);
         for (int64_t i = 3 * b0; i < 3 * b1; i++)
             if (!std::isfinite(set->xyz[i])) {
                 delete h;
@@ -387,8 +454,22 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
                             (long long)(i / 3 - b0));
             }
         base[s] = b0;
-        count[s] = n;
-        h->max_atoms = std::max(h->max_atoms, n);
+        count[s] = (int)(b1 - b0);
+        h->max_atoms = std::max(h->max_atoms, count[s]);
+    }
+    // per structure, on host threads: centroid-relative FP32 coordinates
+    // with the residue key, packed names, and the ResIndex order (stable by
+    // residue name, then serial) with its residue-name buckets
+    struct Buckets {
+        std::vector<uint32_t> name;
+        std::vector<int32_t> lo, hi;
+        double radius = 0.0;
+    };
+    std::vector<Buckets> bk(std::max(S, 0));
+    auto prepare = [&](int s) {
+        const int64_t b0 = base[s];
+        const int n = count[s];
+        Buckets &B = bk[s];
         double c[3] = {0, 0, 0};
         for (int i = 0; i < n; i++)
             for (int d = 0; d < 3; d++) c[d] += set->xyz[3 * (b0 + i) + d];
@@ -398,7 +479,7 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
             int64_t a = b0 + i;
             double dx = set->xyz[3 * a] - c[0], dy = set->xyz[3 * a + 1] - c[1], dz = set->xyz[3 * a + 2] - c[2];
             double r = std::sqrt(dx * dx + dy * dy + dz * dz);
-            if (r > h->max_radius) h->max_radius = r;
+            if (r > B.radius) B.radius = r;
             int32_t k = make_key(set->res_seq[a], set->chain[2 * a + 1]);
             float kf;
             std::memcpy(&kf, &k, 4);
@@ -421,21 +502,39 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
         for (int i = 0; i < n; i++) {
             sorted[b0 + i] = idx[i];
             uint32_t rn = resname[b0 + idx[i]];
-            if (i == 0 || rn != bucket_name.back()) {
-                if (i > 0) bucket_hi.push_back(i);
-                bucket_name.push_back(rn);
-                bucket_lo.push_back(i);
+            if (i == 0 || rn != B.name.back()) {
+                if (i > 0) B.hi.push_back(i);
+                B.name.push_back(rn);
+                B.lo.push_back(i);
             }
         }
-        if (n > 0) bucket_hi.push_back(n);
+        if (n > 0) B.hi.push_back(n);
+    };
+    {
+        const int nthreads = (int)std::max<unsigned>(1, std::min<unsigned>(32, std::thread::hardware_concurrency()));
+        std::atomic<int> next{0};
+        auto worker = [&]() {
+            for (int s; (s = next.fetch_add(1)) < S;) prepare(s);
+        };
+        std::vector<std::thread> pool;
+        for (int i = 1; i < std::min(nthreads, S); i++) pool.emplace_back(worker);
+        worker();
+        for (auto &th : pool) th.join();
+    }
+    for (int s = 0; s < S; s++) {
+        const Buckets &B = bk[s];
+        h->max_radius = std::max(h->max_radius, B.radius);
+        bucket_name.insert(bucket_name.end(), B.name.begin(), B.name.end());
+        bucket_lo.insert(bucket_lo.end(), B.lo.begin(), B.lo.end());
+        bucket_hi.insert(bucket_hi.end(), B.hi.begin(), B.hi.end());
         bucket_begin.push_back((int32_t)bucket_name.size());
     }
     h->atom_base = base;
-    std::vector<double> xyz64(set->xyz, set->xyz + 3 * N);
-    cudaError_t e = cudaSuccess;
+    cudaError_t e = cudaMalloc((void **)&h->d_xyz64, std::max<size_t>(3 * (size_t)N, 1) * sizeof(double));
+    if (e == cudaSuccess && N > 0)
+        e = cudaMemcpy(h->d_xyz64, set->xyz, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = upload(&h->d_atom_base, base);
     if (e == cudaSuccess) e = upload(&h->d_atom_count, count);
-    if (e == cudaSuccess) e = upload(&h->d_xyz64, xyz64);
     if (e == cudaSuccess) e = upload(&h->d_xyz32, xyz32);
     if (e == cudaSuccess) e = upload(&h->d_name, name);
     if (e == cudaSuccess) e = upload(&h->d_resname, resname);
@@ -544,6 +643,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
         return fail(PJG_ERR_INVALID, "non-finite distance parameters");
 
     pjg_results *res = new pjg_results;
+    cudaGetDevice(&res->device);
     const int T = tp->T, S = sp->S, G = tp->G;
     const bool fp32 = P->mode == PJG_MODE_BATCHED_FP32;
     cudaStream_t st = nullptr;
@@ -556,14 +656,16 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     DBuf<unsigned long long> d_exact_count, d_sorted_count;
     DBuf<float4> d_blk_lo, d_blk_hi;
     DBuf<float4> d_cand_xyz, d_leaf_xyz;
-    DBuf<unsigned long long> d_counters, d_ccount, d_pcount;
-    DBuf<int32_t> d_c_pair, d_c_atoms, d_p_pair, d_p_nan, d_p_atoms;
-    DBuf<int64_t> d_c_ord, d_p_row, d_p_ord;
+    DBuf<unsigned long long> d_counters, d_ccount, d_rtotals;
+    DBuf<int32_t> d_c_pair, d_c_atoms, d_pair_rows, d_cnt_q;
+    DBuf<int64_t> d_c_ord, d_off_q;
     DBuf<double> d_c_rmsd;
-    DBuf<double> d_p_rmsd, d_p_rot, d_p_cen;
+    // per complete row, in reference order
+    DBuf<double> d_r_rmsd, d_r_rot, d_r_cen;
+    DBuf<int32_t> d_r_nan, d_r_hit, d_r_warn, d_r_hatoms;
+    DBuf<int64_t> d_r_src, d_r_hidx, d_r_widx, d_r_aidx;
     std::vector<DBuf<int64_t>> scan_tmp;
-    std::vector<HitRec> recs;
-    std::vector<int32_t> rec_atoms;
+    int64_t passing = 0;
     const int stride = std::max(tp->nmax, 1);
     unsigned long long counters[C_NUM] = {};
     float ms = 0.f;
@@ -605,7 +707,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     CUDA_TRY(cudaMemsetAsync(d_counters.p, 0, C_NUM * sizeof(unsigned long long), st));
     CUDA_TRY(dalloc(d_pair_counter, 1, st));
     CUDA_TRY(dalloc(d_ccount, 1, st));
-    CUDA_TRY(dalloc(d_pcount, 1, st));
+    CUDA_TRY(dalloc(d_rtotals, 4, st));
 
     {
         // pass 1: list lengths for every (structure, signature)
@@ -632,7 +734,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
         const int64_t ENTRY_BUDGET = 48ll << 20;
         const int max_chunk = P->mode == PJG_MODE_PLAIN_FP64 ? 1 : 4096;
         int s0 = 0;
-        int64_t c_cap = 1 << 20, p_cap = 1 << 18;
+        int64_t c_cap = 1 << 20;
         CUDA_TRY(dalloc(d_c_pair, c_cap, st));
         CUDA_TRY(dalloc(d_c_ord, c_cap, st));
         CUDA_TRY(dalloc(d_c_atoms, (size_t)c_cap * stride, st));
@@ -730,11 +832,14 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             unsigned long long snap[C_NUM];
             CUDA_TRY(cudaMemcpyAsync(snap, d_counters.p, sizeof snap, cudaMemcpyDeviceToHost, st));
             CUDA_TRY(cudaStreamSynchronize(st));
+            const int64_t n_pairs = (int64_t)Sc * T;
+            CUDA_TRY(dalloc(d_pair_rows, (size_t)n_pairs, st));
             for (int attempt = 0; attempt < 8; attempt++) {
                 CUDA_TRY(cudaMemsetAsync(d_pair_counter.p, 0, sizeof(int32_t), st));
                 CUDA_TRY(cudaMemsetAsync(d_ccount.p, 0, sizeof(unsigned long long), st));
+                CUDA_TRY(cudaMemsetAsync(d_pair_rows.p, 0, (size_t)n_pairs * sizeof(int32_t), st));
                 CompleteRows cr{d_ccount.p, c_cap, stride, d_c_pair.p, d_c_ord.p, d_c_atoms.p,
-                                cut_inline ? d_c_rmsd.p : nullptr};
+                                cut_inline ? d_c_rmsd.p : nullptr, d_pair_rows.p};
                 int grid = sm_count() * 8;
                 CUDA_TRY(launch_search(st, grid, wide, fp32, cv, tv, cd, sa, d_pair_counter.p, scn_c, cr, d_counters.p));
                 launches++;
@@ -754,68 +859,60 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             }
             CUDA_TRY(cudaEventRecord(ev[3], st));
             {
+                // superposition of every complete row into its slot in
+                // reference order, Query.__next__ per pair, compaction of
+                // the hits and warnings into this chunk's segment
                 unsigned long long nc = 0;
                 CUDA_TRY(cudaMemcpyAsync(&nc, d_ccount.p, sizeof nc, cudaMemcpyDeviceToHost, st));
                 CUDA_TRY(cudaStreamSynchronize(st));
+                const int64_t rows = (int64_t)nc;
                 CompleteRows cr{d_ccount.p, c_cap, stride, d_c_pair.p, d_c_ord.p, d_c_atoms.p,
-                                cut_inline ? d_c_rmsd.p : nullptr};
-                int64_t need = std::max<int64_t>((int64_t)nc, 1);
-                if (need > p_cap) p_cap = need;
-                CUDA_TRY(dalloc(d_p_row, p_cap, st));
-                CUDA_TRY(dalloc(d_p_pair, p_cap, st));
-                CUDA_TRY(dalloc(d_p_ord, p_cap, st));
-                CUDA_TRY(dalloc(d_p_rmsd, p_cap, st));
-                CUDA_TRY(dalloc(d_p_nan, p_cap, st));
-                CUDA_TRY(dalloc(d_p_rot, (size_t)p_cap * 9, st));
-                CUDA_TRY(dalloc(d_p_cen, (size_t)p_cap * 6, st));
-                CUDA_TRY(dalloc(d_p_atoms, (size_t)p_cap * stride, st));
-                CUDA_TRY(cudaMemsetAsync(d_pcount.p, 0, sizeof(unsigned long long), st));
-                PassRows pr{d_pcount.p, p_cap, stride, d_p_row.p, d_p_pair.p, d_p_ord.p, d_p_rmsd.p,
-                            d_p_nan.p, d_p_rot.p, d_p_cen.p, d_p_atoms.p};
-                SuperArgs su{P->rmsd_threshold};
-                TemplateView tv2 = tv;
-                if (nc > 0) {
-                    int blocks = (int)std::min<int64_t>(((int64_t)nc + 7) / 8, (int64_t)sm_count() * 32);
-                    launch_superpose(st, blocks, cv, tv2, su, cr, pr, d_counters.p);
-                    launches++;
-                    CUDA_TRY(cudaGetLastError());
+                                cut_inline ? d_c_rmsd.p : nullptr, d_pair_rows.p};
+                if (rows > 0) {
+                    CUDA_TRY(dalloc(d_cnt_q, (size_t)n_pairs, st));
+                    CUDA_TRY(dalloc(d_off_q, (size_t)n_pairs, st));
+                    launch_order_counts(st, n_pairs, T, d_pair_rows.p, d_cnt_q.p);
+                    CUDA_TRY(scan_exclusive(d_cnt_q.p, n_pairs, d_off_q.p, scan_tmp, st));
+                    CUDA_TRY(dalloc(d_r_rmsd, (size_t)rows, st));
+                    CUDA_TRY(dalloc(d_r_rot, (size_t)rows * 9, st));
+                    CUDA_TRY(dalloc(d_r_cen, (size_t)rows * 6, st));
+                    CUDA_TRY(dalloc(d_r_nan, (size_t)rows, st));
+                    CUDA_TRY(dalloc(d_r_src, (size_t)rows, st));
+                    CUDA_TRY(dalloc(d_r_hit, (size_t)rows, st));
+                    CUDA_TRY(dalloc(d_r_warn, (size_t)rows, st));
+                    CUDA_TRY(dalloc(d_r_hatoms, (size_t)rows, st));
+                    CUDA_TRY(dalloc(d_r_hidx, (size_t)rows, st));
+                    CUDA_TRY(dalloc(d_r_widx, (size_t)rows, st));
+                    CUDA_TRY(dalloc(d_r_aidx, (size_t)rows, st));
+                    RowResults rr{d_off_q.p, T, d_r_rmsd.p, d_r_nan.p, d_r_rot.p, d_r_cen.p, d_r_src.p};
+                    int blocks = (int)std::min<int64_t>((rows + 7) / 8, (int64_t)sm_count() * 32);
+                    launch_superpose(st, blocks, cv, tv, cr, rr);
+                    CUDA_TRY(cudaMemsetAsync(d_rtotals.p, 0, 4 * sizeof(unsigned long long), st));
+                    launch_automaton(st, n_pairs, T, tp->d_atom_begin, d_cnt_q.p, d_off_q.p, rr, P->max_candidates,
+                                     P->best_match, P->rmsd_threshold, d_r_hit.p, d_r_warn.p, d_r_hatoms.p,
+                                     d_rtotals.p);
+                    CUDA_TRY(scan_exclusive(d_r_hit.p, rows, d_r_hidx.p, scan_tmp, st));
+                    CUDA_TRY(scan_exclusive(d_r_warn.p, rows, d_r_widx.p, scan_tmp, st));
+                    CUDA_TRY(scan_exclusive(d_r_hatoms.p, rows, d_r_aidx.p, scan_tmp, st));
+                    unsigned long long tot[4] = {};
+                    CUDA_TRY(cudaMemcpyAsync(tot, d_rtotals.p, sizeof tot, cudaMemcpyDeviceToHost, st));
+                    CUDA_TRY(cudaStreamSynchronize(st));
+                    passing += (int64_t)tot[3];
+                    if (tot[0] + tot[1] > 0) {
+                        HitStore &hs = res->store;
+                        CUDA_TRY(hs.reserve((int64_t)tot[0], (int64_t)tot[2], (int64_t)tot[1], st));
+                        launch_gather_hits(st, rows, T, s0, hs.atoms, tp->d_atom_begin, cr, rr, d_r_hit.p,
+                                           d_r_warn.p, d_r_hidx.p, d_r_widx.p, d_r_aidx.p, P->best_match, hs.tail());
+                        CUDA_TRY(cudaGetLastError());
+                        hs.hits += (int64_t)tot[0];
+                        hs.atoms += (int64_t)tot[2];
+                        hs.warns += (int64_t)tot[1];
+                    }
+                    launches += 8;
                 }
                 CUDA_TRY(cudaEventRecord(ev[4], st));
-                unsigned long long np = 0;
-                CUDA_TRY(cudaMemcpyAsync(&np, d_pcount.p, sizeof np, cudaMemcpyDeviceToHost, st));
-                CUDA_TRY(cudaStreamSynchronize(st));
-                if ((int64_t)np > p_cap) {
-                    status = fail(PJG_ERR_CAPACITY, "passing-row buffer overflow");
-                    goto done;
-                }
-                std::vector<int32_t> pair(np), nan(np), atoms((size_t)np * stride);
-                std::vector<int64_t> ord(np);
-                std::vector<double> rm(np), rot((size_t)np * 9), cen((size_t)np * 6);
-                if (np > 0) {
-                    CUDA_TRY(cudaMemcpyAsync(pair.data(), d_p_pair.p, np * 4, cudaMemcpyDeviceToHost, st));
-                    CUDA_TRY(cudaMemcpyAsync(nan.data(), d_p_nan.p, np * 4, cudaMemcpyDeviceToHost, st));
-                    CUDA_TRY(cudaMemcpyAsync(ord.data(), d_p_ord.p, np * 8, cudaMemcpyDeviceToHost, st));
-                    CUDA_TRY(cudaMemcpyAsync(rm.data(), d_p_rmsd.p, np * 8, cudaMemcpyDeviceToHost, st));
-                    CUDA_TRY(cudaMemcpyAsync(rot.data(), d_p_rot.p, np * 72, cudaMemcpyDeviceToHost, st));
-                    CUDA_TRY(cudaMemcpyAsync(cen.data(), d_p_cen.p, np * 48, cudaMemcpyDeviceToHost, st));
-                    CUDA_TRY(cudaMemcpyAsync(atoms.data(), d_p_atoms.p, (size_t)np * stride * 4, cudaMemcpyDeviceToHost, st));
-                    CUDA_TRY(cudaStreamSynchronize(st));
-                }
-                for (unsigned long long i = 0; i < np; i++) {
-                    HitRec r;
-                    r.s = s0 + pair[i] / T;
-                    r.t = pair[i] % T;
-                    r.ordinal = ord[i];
-                    r.rmsd = rm[i];
-                    r.nan_rot = nan[i];
-                    std::memcpy(r.rot, &rot[9 * i], 72);
-                    std::memcpy(r.centres, &cen[6 * i], 48);
-                    r.atom_at = (int64_t)rec_atoms.size();
-                    int n = tp->atom_begin[r.t + 1] - tp->atom_begin[r.t];
-                    rec_atoms.insert(rec_atoms.end(), &atoms[(size_t)i * stride], &atoms[(size_t)i * stride] + n);
-                    recs.push_back(r);
-                }
                 float m1 = 0, m2 = 0, m3 = 0;
+                CUDA_TRY(cudaEventSynchronize(ev[4]));
                 cudaEventElapsedTime(&m1, ev[1], ev[2]);
                 cudaEventElapsedTime(&m2, ev[2], ev[3]);
                 cudaEventElapsedTime(&m3, ev[3], ev[4]);
@@ -844,101 +941,20 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
         goto done;
     }
 
-    {
-        // order: structure, template in reverse index order (the reference's
-        // prepend list, patches/Jess.c.patch:63-72), stream ordinal
-        std::vector<size_t> idx(recs.size());
-        std::iota(idx.begin(), idx.end(), 0);
-        std::sort(idx.begin(), idx.end(), [&](size_t a, size_t b) {
-            const HitRec &x = recs[a], &y = recs[b];
-            if (x.s != y.s) return x.s < y.s;
-            if (x.t != y.t) return x.t > y.t;
-            return x.ordinal < y.ordinal;
-        });
-        // automaton of Query.__next__ per pair (closed form):
-        //  best_match: over rows with ordinal <= M+1 (M = max_candidates),
-        //    keep the first strict minimum; a NaN rotation that would have
-        //    improved the minimum raises a warning instead.
-        //  otherwise: every passing row is a hit, except that the template's
-        //    stream is cut at the first candidate whose distance from the
-        //    previous hit (or from the template start) is M+1.
-        const int M = P->max_candidates;
-        int cur_s = -1;
-        int64_t hits_in_s = 0;
-        size_t i = 0;
-        while (i < idx.size()) {
-            size_t j = i;
-            const HitRec &h0 = recs[idx[i]];
-            while (j < idx.size() && recs[idx[j]].s == h0.s && recs[idx[j]].t == h0.t) j++;
-            if (h0.s != cur_s) {
-                cur_s = h0.s;
-                hits_in_s = 0;
-            }
-            auto push_hit = [&](const HitRec &h) {
-                res->structure.push_back(h.s);
-                res->tpl.push_back(h.t);
-                res->ordinal.push_back(h.ordinal);
-                res->rmsd.push_back(h.rmsd);
-                res->rot.insert(res->rot.end(), h.rot, h.rot + 9);
-                res->centres.insert(res->centres.end(), h.centres, h.centres + 6);
-                int n = tp->atom_begin[h.t + 1] - tp->atom_begin[h.t];
-                res->atoms.insert(res->atoms.end(), rec_atoms.begin() + h.atom_at, rec_atoms.begin() + h.atom_at + n);
-                res->atom_offset.push_back((int64_t)res->atoms.size());
-                hits_in_s++;
-            };
-            if (P->best_match) {
-                double cur = INFINITY;
-                const HitRec *best = nullptr;
-                for (size_t q = i; q < j; q++) {
-                    const HitRec &h = recs[idx[q]];
-                    if (M >= 0 && h.ordinal > (int64_t)M + 1) break;
-                    if (h.rmsd < cur) {
-                        if (h.nan_rot) {
-                            res->warn_structure.push_back(h.s);
-                            res->warn_before.push_back(hits_in_s);
-                        } else {
-                            cur = h.rmsd;
-                            best = &h;
-                        }
-                    }
-                }
-                if (best) push_hit(*best);
-            } else {
-                int64_t base = 0;
-                for (size_t q = i; q < j; q++) {
-                    const HitRec &h = recs[idx[q]];
-                    if (M >= 0 && h.ordinal > base + M + 1) break;
-                    if (h.nan_rot) {
-                        res->warn_structure.push_back(h.s);
-                        res->warn_before.push_back(hits_in_s);
-                    } else {
-                        push_hit(h);
-                    }
-                    if (M >= 0 && h.ordinal == base + M + 1) break;
-                    if (!h.nan_rot) base = h.ordinal + 1;
-                }
-            }
-            i = j;
-        }
-    }
     res->stats.pairs = (int64_t)counters[C_PAIRS];
     res->stats.candidate_entries = (int64_t)counters[C_CAND];
     res->stats.partials = (int64_t)counters[C_PARTIALS];
     res->stats.complete = (int64_t)counters[C_COMPLETE];
-    res->stats.passing = (int64_t)recs.size();
-    res->stats.hits = (int64_t)res->rmsd.size();
+    res->stats.passing = passing;
+    res->stats.hits = res->store.hits;
     res->stats.fp64_rechecks = (int64_t)counters[C_RECHECK];
     res->stats.leaf_exact = (int64_t)counters[C_LEAF_EXACT];
     res->stats.leaf_sorted = (int64_t)counters[C_LEAF_SORTED];
     res->stats.leaf_replays = (int64_t)counters[C_LEAF_REPLAY];
     res->stats.bytes_candidates = (int64_t)counters[C_BYTES_CAND];
     res->stats.bytes_expansion = (int64_t)counters[C_BYTES_EXP];
-    {
-        int64_t hb = 0;
-        for (size_t q = 0; q < res->rmsd.size(); q++)
-            hb += 4 * (res->atom_offset[q + 1] - res->atom_offset[q]) + 8 + 72 + 48;
-        res->stats.bytes_superposition = hb;
-    }
+    // per hit: its atoms, rmsd, rotation and centroids
+    res->stats.bytes_superposition = 4 * res->store.atoms + (8 + 72 + 48) * res->store.hits;
     res->stats.ms_candidates = ms_cand;
     res->stats.ms_expansion = ms_exp;
     res->stats.ms_superposition = ms_sup;
@@ -951,11 +967,13 @@ done:
         dfree(d_params, st); dfree(d_count, st); dfree(d_scanned, st); dfree(d_cand_atom, st);
         dfree(d_leaf_atom, st); dfree(d_pair_counter, st); dfree(d_offset, st); dfree(d_totals, st);
         dfree(d_cand_xyz, st); dfree(d_leaf_xyz, st); dfree(d_counters, st); dfree(d_ccount, st);
-        dfree(d_pcount, st); dfree(d_c_pair, st); dfree(d_c_atoms, st); dfree(d_p_pair, st);
-        dfree(d_p_nan, st); dfree(d_p_atoms, st); dfree(d_c_ord, st); dfree(d_p_row, st);
-        dfree(d_p_ord, st); dfree(d_p_rmsd, st); dfree(d_c_rmsd, st); dfree(d_boff, st); dfree(d_nblk, st);
-        dfree(d_blk_lo, st); dfree(d_blk_hi, st); dfree(d_exact_list, st); dfree(d_exact_count, st);
-        dfree(d_sorted_list, st); dfree(d_sorted_count, st); dfree(d_p_rot, st); dfree(d_p_cen, st);
+        dfree(d_rtotals, st); dfree(d_c_pair, st); dfree(d_c_atoms, st); dfree(d_pair_rows, st);
+        dfree(d_cnt_q, st); dfree(d_c_ord, st); dfree(d_off_q, st); dfree(d_c_rmsd, st); dfree(d_boff, st);
+        dfree(d_nblk, st); dfree(d_blk_lo, st); dfree(d_blk_hi, st); dfree(d_exact_list, st);
+        dfree(d_exact_count, st); dfree(d_sorted_list, st); dfree(d_sorted_count, st);
+        dfree(d_r_rmsd, st); dfree(d_r_rot, st); dfree(d_r_cen, st); dfree(d_r_nan, st); dfree(d_r_hit, st);
+        dfree(d_r_warn, st); dfree(d_r_hatoms, st); dfree(d_r_src, st); dfree(d_r_hidx, st); dfree(d_r_widx, st);
+        dfree(d_r_aidx, st);
         for (auto &b : scan_tmp) dfree(b, st);
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);
@@ -972,32 +990,46 @@ done:
 
 extern "C" {
 
-int64_t pjg_results_count(const pjg_results *r) { return r ? (int64_t)r->rmsd.size() : 0; }
+int64_t pjg_results_count(const pjg_results *r) { return r ? r->store.hits : 0; }
 
-int64_t pjg_results_atom_count(const pjg_results *r) { return r ? (int64_t)r->atoms.size() : 0; }
+int64_t pjg_results_atom_count(const pjg_results *r) { return r ? r->store.atoms : 0; }
 
 pjg_status pjg_results_copy(const pjg_results *r, int32_t *structure, int32_t *template_index, int64_t *ordinal,
                             double *rmsd, double *rotation, double *centres, int64_t *atom_offset, int32_t *atoms) {
     if (!r) return fail(PJG_ERR_INVALID, "null results");
-    size_t n = r->rmsd.size();
-    if (structure) std::memcpy(structure, r->structure.data(), n * 4);
-    if (template_index) std::memcpy(template_index, r->tpl.data(), n * 4);
-    if (ordinal) std::memcpy(ordinal, r->ordinal.data(), n * 8);
-    if (rmsd) std::memcpy(rmsd, r->rmsd.data(), n * 8);
-    if (rotation) std::memcpy(rotation, r->rot.data(), n * 72);
-    if (centres) std::memcpy(centres, r->centres.data(), n * 48);
-    if (atom_offset) std::memcpy(atom_offset, r->atom_offset.data(), (n + 1) * 8);
-    if (atoms) std::memcpy(atoms, r->atoms.data(), r->atoms.size() * 4);
+    const HitStore &hs = r->store;
+    const size_t n = (size_t)hs.hits;
+    if (atom_offset) atom_offset[n] = hs.atoms;
+    if (n == 0) return PJG_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (prev != r->device) cudaSetDevice(r->device);
+    cudaError_t e = copy_out(structure, hs.structure, 4 * n);
+    if (e == cudaSuccess) e = copy_out(template_index, hs.tpl, 4 * n);
+    if (e == cudaSuccess) e = copy_out(ordinal, hs.ordinal, 8 * n);
+    if (e == cudaSuccess) e = copy_out(rmsd, hs.rmsd, 8 * n);
+    if (e == cudaSuccess) e = copy_out(rotation, hs.rot, 72 * n);
+    if (e == cudaSuccess) e = copy_out(centres, hs.centres, 48 * n);
+    if (e == cudaSuccess) e = copy_out(atom_offset, hs.atom_offset, 8 * n);
+    if (e == cudaSuccess) e = copy_out(atoms, hs.atoms_, 4 * (size_t)hs.atoms);
+    if (prev != r->device) cudaSetDevice(prev);
+    if (e != cudaSuccess) return fail(PJG_ERR_CUDA, "results copy: %s", cudaGetErrorString(e));
     return PJG_OK;
 }
 
-int64_t pjg_results_warning_count(const pjg_results *r) { return r ? (int64_t)r->warn_structure.size() : 0; }
+int64_t pjg_results_warning_count(const pjg_results *r) { return r ? r->store.warns : 0; }
 
 pjg_status pjg_results_warnings(const pjg_results *r, int32_t *structure, int64_t *hits_before) {
     if (!r) return fail(PJG_ERR_INVALID, "null results");
-    size_t n = r->warn_structure.size();
-    if (structure) std::memcpy(structure, r->warn_structure.data(), n * 4);
-    if (hits_before) std::memcpy(hits_before, r->warn_before.data(), n * 8);
+    const HitStore &hs = r->store;
+    if (hs.warns == 0) return PJG_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (prev != r->device) cudaSetDevice(r->device);
+    cudaError_t e = copy_out(structure, hs.warn_structure, 4 * (size_t)hs.warns);
+    if (e == cudaSuccess) e = copy_out(hits_before, hs.warn_before, 8 * (size_t)hs.warns);
+    if (prev != r->device) cudaSetDevice(prev);
+    if (e != cudaSuccess) return fail(PJG_ERR_CUDA, "warnings copy: %s", cudaGetErrorString(e));
     return PJG_OK;
 }
 
@@ -1007,6 +1039,14 @@ pjg_status pjg_results_stats(const pjg_results *r, pjg_stats *stats) {
     return PJG_OK;
 }
 
-void pjg_results_destroy(pjg_results *r) { delete r; }
+void pjg_results_destroy(pjg_results *r) {
+    if (!r) return;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    const bool other = r->store.cap_h + r->store.cap_w > 0 && prev != r->device;
+    if (other) cudaSetDevice(r->device);
+    delete r;
+    if (other) cudaSetDevice(prev);
+}
 
 }  // extern "C"

@@ -2074,6 +2074,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
             }
         }
         __syncwarp();
+        if (lane == 0 && emitted > 0) out.pair_rows[pair] = (int32_t)emitted;
         // ---- statistics of the pair
         for (int o = 16; o; o >>= 1) rechecks += __shfl_xor_sync(FULL_MASK, rechecks, o);
         if (lane == 0) {
@@ -2091,8 +2092,9 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
 }
 
 
-__global__ void k_superpose(ChunkView cv, TemplateView tv, SuperArgs sa, CompleteRows in, PassRows out,
-                            unsigned long long *counters) {
+// Superposition of every complete row (warp per row), written to the row's
+// slot in reference order.
+__global__ void k_superpose(ChunkView cv, TemplateView tv, CompleteRows in, RowResults out) {
     int lane = lane_id();
     int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -2106,9 +2108,8 @@ __global__ void k_superpose(ChunkView cv, TemplateView tv, SuperArgs sa, Complet
         int n = tv.atom_begin[t + 1] - ab;
         const double *xyz = cv.xyz64 + 3 * cv.atom_base[s];
         double a[3] = {0, 0, 0}, b[3] = {0, 0, 0};
-        int32_t atom = 0;
         if (lane < n) {
-            atom = in.atoms[i * in.stride + lane];
+            const int32_t atom = in.atoms[i * in.stride + lane];
             for (int d = 0; d < 3; d++) {
                 a[d] = xyz[3 * (int64_t)atom + d];
                 b[d] = tv.pos[3 * (ab + lane) + d];
@@ -2130,35 +2131,151 @@ __global__ void k_superpose(ChunkView cv, TemplateView tv, SuperArgs sa, Complet
         double S[9];
         for (int r = 0; r < 3; r++)
             for (int c = 0; c < 3; c++) S[3 * r + c] = warp_sum(ac[r] * bc[c]);
-        double rmsd = 0.0, R[9];
-        bool bad = false;
-        if (lane == 0) quaternion_fit(S, 0.5 * (sumA + sumB), n, &rmsd, R, &bad);
-        rmsd = __shfl_sync(FULL_MASK, rmsd, 0);
-        // rows whose rmsd already decided the max_candidates cut keep it, so
-        // the automaton on the host replays the same decisions
-        if (in.rmsd) rmsd = in.rmsd[i];
-        if (rmsd <= sa.rmsd_threshold) {
-            int64_t j = 0;
-            if (lane == 0) j = (int64_t)atomicAdd(out.count, 1ull);
-            j = __shfl_sync(FULL_MASK, j, 0);
-            if (j < out.capacity) {
-                if (lane == 0) {
-                    out.row[j] = i;
-                    out.pair[j] = pair;
-                    out.ordinal[j] = in.ordinal[i];
-                    out.rmsd[j] = rmsd;
-                    out.nan_rot[j] = bad ? 1 : 0;
-                    for (int q = 0; q < 9; q++) out.rot[9 * j + q] = R[q];
-                    for (int d = 0; d < 3; d++) {
-                        out.centres[6 * j + d] = ca[d];
-                        out.centres[6 * j + 3 + d] = cb[d];
-                    }
-                }
-                if (lane < n) out.atoms[j * out.stride + lane] = atom;
-            } else if (lane == 0) {
-                atomicAdd(&counters[C_PASS_OVERFLOW], 1ull);
+        if (lane == 0) {
+            double rmsd = 0.0, R[9];
+            bool bad = false;
+            quaternion_fit(S, 0.5 * (sumA + sumB), n, &rmsd, R, &bad);
+            // rows whose rmsd already decided the max_candidates cut keep it,
+            // so the automaton replays the same decisions
+            if (in.rmsd) rmsd = in.rmsd[i];
+            const int64_t d = out.off_q[(int64_t)s * T + (T - 1 - t)] + in.ordinal[i];
+            out.rmsd[d] = rmsd;
+            out.nan_rot[d] = bad ? 1 : 0;
+            out.src[d] = i;
+            for (int q = 0; q < 9; q++) out.rot[9 * d + q] = R[q];
+            for (int k = 0; k < 3; k++) {
+                out.centres[6 * d + k] = ca[k];
+                out.centres[6 * d + 3 + k] = cb[k];
             }
         }
+    }
+}
+
+__global__ void k_order_counts(int64_t n_pairs, int32_t T, const int32_t *pair_rows, int32_t *cnt_q) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_pairs) return;
+    const int64_t s = q / T;
+    const int t = T - 1 - (int)(q % T);
+    cnt_q[q] = pair_rows[s * T + t];
+}
+
+// Query.__next__ (src/pyjess/_jess.pyx:2197-2283) in closed form, one
+// thread per pair, over the pair's rows that pass the rmsd threshold:
+//  best_match: over rows with ordinal <= M+1 (M = max_candidates), the
+//    first strict minimum is the hit; a row with an undefined rotation that
+//    would have lowered the minimum raises a warning instead.
+//  otherwise: every passing row is a hit (an undefined rotation: a
+//    warning), but the template's stream ends at the first row whose
+//    ordinal is M+1 past the previous hit (or the template start).
+__global__ void k_automaton(int64_t n_pairs, int32_t T, const int32_t *atom_begin, const int32_t *cnt_q,
+                            const int64_t *off_q, RowResults rr, int32_t M, int32_t best, double thr, int32_t *hit,
+                            int32_t *warn, int32_t *hit_atoms, unsigned long long *totals) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long nh = 0, nw = 0, na = 0, np = 0;
+    if (q < n_pairs) {
+        const int t = T - 1 - (int)(q % T);
+        const int n = atom_begin[t + 1] - atom_begin[t];
+        const int64_t off = off_q[q];
+        const int64_t cnt = cnt_q[q];
+        for (int64_t k = 0; k < cnt; k++) {
+            hit[off + k] = 0;
+            warn[off + k] = 0;
+            hit_atoms[off + k] = 0;
+        }
+        if (best) {
+            double cur = INFINITY;
+            int64_t b = -1;
+            for (int64_t k = 0; k < cnt; k++) {
+                const double r = rr.rmsd[off + k];
+                if (!(r <= thr)) continue;
+                np++;
+                if (M >= 0 && k > (int64_t)M + 1) break;
+                if (r < cur) {
+                    if (rr.nan_rot[off + k]) {
+                        warn[off + k] = 1;
+                        nw++;
+                    } else {
+                        cur = r;
+                        b = k;
+                    }
+                }
+            }
+            if (b >= 0) {
+                hit[off + b] = 1;
+                hit_atoms[off + b] = n;
+                nh++;
+                na += n;
+            }
+        } else {
+            int64_t base = 0;
+            for (int64_t k = 0; k < cnt; k++) {
+                const double r = rr.rmsd[off + k];
+                if (!(r <= thr)) continue;
+                np++;
+                if (M >= 0 && k > base + M + 1) break;
+                const bool nan_rot = rr.nan_rot[off + k] != 0;
+                if (nan_rot) {
+                    warn[off + k] = 1;
+                    nw++;
+                } else {
+                    hit[off + k] = 1;
+                    hit_atoms[off + k] = n;
+                    nh++;
+                    na += n;
+                }
+                if (M >= 0 && k == base + M + 1) break;
+                if (!nan_rot) base = k + 1;
+            }
+        }
+    }
+    for (int o = 16; o; o >>= 1) {
+        nh += __shfl_xor_sync(FULL_MASK, nh, o);
+        nw += __shfl_xor_sync(FULL_MASK, nw, o);
+        na += __shfl_xor_sync(FULL_MASK, na, o);
+        np += __shfl_xor_sync(FULL_MASK, np, o);
+    }
+    if (lane_id() == 0) {
+        if (nh) atomicAdd(&totals[0], nh);
+        if (nw) atomicAdd(&totals[1], nw);
+        if (na) atomicAdd(&totals[2], na);
+        if (np) atomicAdd(&totals[3], np);
+    }
+}
+
+// Flagged rows into the chunk's HitSegment, thread per row.
+__global__ void k_gather_hits(int64_t n_rows, int32_t T, int32_t structure_base, int64_t atom_base,
+                              const int32_t *atom_begin, CompleteRows in, RowResults rr, const int32_t *hit,
+                              const int32_t *warn, const int64_t *hit_idx, const int64_t *warn_idx,
+                              const int64_t *atom_idx, int32_t best, HitSegment out) {
+    const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n_rows) return;
+    const bool h = hit[d] != 0, w = warn[d] != 0;
+    if (!h && !w) return;
+    const int64_t i = rr.src[d];
+    const int pair = in.pair[i];
+    const int s = pair / T, t = pair % T;
+    const int64_t q = (int64_t)s * T + (T - 1 - t);
+    if (h) {
+        const int64_t k = hit_idx[d];
+        out.structure[k] = structure_base + s;
+        out.tpl[k] = t;
+        out.ordinal[k] = in.ordinal[i];
+        out.rmsd[k] = rr.rmsd[d];
+        for (int c = 0; c < 9; c++) out.rot[9 * k + c] = rr.rot[9 * d + c];
+        for (int c = 0; c < 6; c++) out.centres[6 * k + c] = rr.centres[6 * d + c];
+        const int64_t a0 = atom_idx[d];
+        out.atom_offset[k] = atom_base + a0;
+        const int n = atom_begin[t + 1] - atom_begin[t];
+        for (int j = 0; j < n; j++) out.atoms[a0 + j] = in.atoms[i * in.stride + j];
+    }
+    if (w) {
+        const int64_t k = warn_idx[d];
+        // hits of the structure already reported: best_match reports a
+        // pair's hit after its rows, otherwise hits come in row order
+        const int64_t first = hit_idx[rr.off_q[(int64_t)s * T]];
+        const int64_t upto = best ? hit_idx[rr.off_q[q]] : hit_idx[d];
+        out.warn_structure[k] = structure_base + s;
+        out.warn_before[k] = upto - first;
     }
 }
 
@@ -2286,9 +2403,34 @@ cudaError_t launch_search(cudaStream_t st, int grid, bool wide, bool fp32, const
 }
 
 void launch_superpose(cudaStream_t st, int blocks, const ChunkView &cv, const TemplateView &tv,
-                      const SuperArgs &sa, const CompleteRows &in, const PassRows &out,
-                      unsigned long long *counters) {
-    k_superpose<<<blocks, 256, 0, st>>>(cv, tv, sa, in, out, counters);
+                      const CompleteRows &in, const RowResults &out) {
+    k_superpose<<<blocks, 256, 0, st>>>(cv, tv, in, out);
+}
+
+void launch_order_counts(cudaStream_t st, int64_t n_pairs, int32_t n_templates, const int32_t *pair_rows,
+                         int32_t *cnt_q) {
+    if (n_pairs > 0)
+        k_order_counts<<<(unsigned)((n_pairs + 255) / 256), 256, 0, st>>>(n_pairs, n_templates, pair_rows, cnt_q);
+}
+
+void launch_automaton(cudaStream_t st, int64_t n_pairs, int32_t n_templates, const int32_t *atom_begin,
+                      const int32_t *cnt_q, const int64_t *off_q, const RowResults &rr, int32_t max_candidates,
+                      int32_t best_match, double rmsd_threshold, int32_t *hit, int32_t *warn, int32_t *hit_atoms,
+                      unsigned long long *totals) {
+    if (n_pairs > 0)
+        k_automaton<<<(unsigned)((n_pairs + 127) / 128), 128, 0, st>>>(n_pairs, n_templates, atom_begin, cnt_q,
+                                                                      off_q, rr, max_candidates, best_match,
+                                                                      rmsd_threshold, hit, warn, hit_atoms, totals);
+}
+
+void launch_gather_hits(cudaStream_t st, int64_t n_rows, int32_t n_templates, int32_t structure_base,
+                        int64_t atom_base, const int32_t *atom_begin, const CompleteRows &in, const RowResults &rr,
+                        const int32_t *hit, const int32_t *warn, const int64_t *hit_idx, const int64_t *warn_idx,
+                        const int64_t *atom_idx, int32_t best_match, const HitSegment &out) {
+    if (n_rows > 0)
+        k_gather_hits<<<(unsigned)((n_rows + 255) / 256), 256, 0, st>>>(n_rows, n_templates, structure_base,
+                                                                        atom_base, atom_begin, in, rr, hit, warn,
+                                                                        hit_idx, warn_idx, atom_idx, best_match, out);
 }
 
 // ---------------------------------------------------------------------------

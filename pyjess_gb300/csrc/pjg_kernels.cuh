@@ -35,10 +35,6 @@ struct SearchArgs {
     uint64_t budget_ns;                // per-warp wall-time budget (globaltimer)
 };
 
-struct SuperArgs {
-    double rmsd_threshold;
-};
-
 // Complete assignments written by k_search.
 struct CompleteRows {
     unsigned long long *count;
@@ -49,21 +45,34 @@ struct CompleteRows {
     int32_t *atoms;                    // [capacity * stride], template order
     double *rmsd;                      // rmsd computed in the search (inline
                                        // cut mode), else nullptr
+    int32_t *pair_rows;                // [pairs] complete rows of each pair
 };
 
-// Complete assignments with rmsd <= threshold, written by k_superpose.
-struct PassRows {
-    unsigned long long *count;
-    int64_t capacity;
-    int32_t stride;
-    int64_t *row;
-    int32_t *pair;
+// Superposition of every complete row, in reference order: row i of pair
+// (s, t) with stream ordinal k lands at off_q[s * T + (T - 1 - t)] + k
+// (structures ascending, templates descending, then the stream).
+struct RowResults {
+    const int64_t *off_q;
+    int32_t n_templates;
+    double *rmsd;
+    int32_t *nan_rot;                  // rotation undefined (NaN entries)
+    double *rot;                       // [9 * rows]
+    double *centres;                   // [6 * rows]
+    int64_t *src;                      // complete-row index of each slot
+};
+
+// Final hits and warnings of one chunk (Query.__next__ applied on the device).
+struct HitSegment {
+    int32_t *structure;
+    int32_t *tpl;
     int64_t *ordinal;
     double *rmsd;
-    int32_t *nan_rot;
-    double *rot;                       // [9 * capacity]
-    double *centres;                   // [6 * capacity]
-    int32_t *atoms;                    // [capacity * stride]
+    double *rot;                       // [9 * hits]
+    double *centres;                   // [6 * hits]
+    int64_t *atom_offset;              // [hits] first atom of each hit (global)
+    int32_t *atoms;
+    int32_t *warn_structure;
+    int64_t *warn_before;              // hits of the structure before the warning
 };
 
 // Host-side launchers (the kernels themselves live in pjg_kernels.cu).
@@ -104,7 +113,25 @@ cudaError_t launch_search(cudaStream_t st, int grid, bool wide, bool fp32, const
                           const int32_t *scanned, const CompleteRows &out, unsigned long long *counters);
 
 void launch_superpose(cudaStream_t st, int blocks, const ChunkView &cv, const TemplateView &tv,
-                      const SuperArgs &sa, const CompleteRows &in, const PassRows &out,
-                      unsigned long long *counters);
+                      const CompleteRows &in, const RowResults &out);
+
+// reference-order list lengths: cnt_q[s * T + (T - 1 - t)] = pair_rows[s * T + t]
+void launch_order_counts(cudaStream_t st, int64_t n_pairs, int32_t n_templates, const int32_t *pair_rows,
+                         int32_t *cnt_q);
+
+// Query.__next__ per pair over its rows in reference order: hit / warning
+// flags and hit atom counts per row; totals[0..3] += hits, warnings, hit
+// atoms, passing rows
+void launch_automaton(cudaStream_t st, int64_t n_pairs, int32_t n_templates, const int32_t *atom_begin,
+                      const int32_t *cnt_q, const int64_t *off_q, const RowResults &rr, int32_t max_candidates,
+                      int32_t best_match, double rmsd_threshold, int32_t *hit, int32_t *warn, int32_t *hit_atoms,
+                      unsigned long long *totals);
+
+// compaction of the flagged rows into a HitSegment (hit_idx, warn_idx,
+// atom_idx: exclusive scans of the flags / hit atom counts)
+void launch_gather_hits(cudaStream_t st, int64_t n_rows, int32_t n_templates, int32_t structure_base,
+                        int64_t atom_base, const int32_t *atom_begin, const CompleteRows &in, const RowResults &rr,
+                        const int32_t *hit, const int32_t *warn, const int64_t *hit_idx, const int64_t *warn_idx,
+                        const int64_t *atom_idx, int32_t best_match, const HitSegment &out);
 
 }  // namespace pjg
