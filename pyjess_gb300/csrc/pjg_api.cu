@@ -885,7 +885,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                     CUDA_TRY(dalloc(d_r_widx, (size_t)rows, st));
                     CUDA_TRY(dalloc(d_r_aidx, (size_t)rows, st));
                     RowResults rr{d_off_q.p, T, d_r_rmsd.p, d_r_nan.p, d_r_rot.p, d_r_cen.p, d_r_src.p};
-                    int blocks = (int)std::min<int64_t>((rows + 7) / 8, (int64_t)sm_count() * 32);
+                    int blocks = (int)std::min<int64_t>((rows + 127) / 128, (int64_t)sm_count() * 24);
                     launch_superpose(st, blocks, cv, tv, cr, rr);
                     CUDA_TRY(cudaMemsetAsync(d_rtotals.p, 0, 4 * sizeof(unsigned long long), st));
                     launch_automaton(st, n_pairs, T, tp->d_atom_begin, d_cnt_q.p, d_off_q.p, rr, P->max_candidates,

@@ -1402,10 +1402,11 @@ __device__ void quaternion_fit(const double S[9], double E0, int n, double *rmsd
     *bad = n < 3;
 }
 
-// RMSD of one assignment computed by a single lane (sums in template atom
-// order), used where a lane needs the value while searching.
-__device__ double lane_rmsd(int n, const int32_t *atoms, const double *xyz, const double *tpos) {
-    double ca[3] = {0, 0, 0}, cb[3] = {0, 0, 0};
+// Centroids, centred covariance S = sum a b^T and E0 = (|a|^2 + |b|^2) / 2
+// of one assignment, by one thread (sums in template atom order).
+__device__ void lane_covariance(int n, const int32_t *atoms, const double *xyz, const double *tpos, double ca[3],
+                                double cb[3], double S[9], double *E0) {
+    for (int d = 0; d < 3; d++) ca[d] = cb[d] = 0.0;
     for (int k = 0; k < n; k++)
         for (int d = 0; d < 3; d++) {
             ca[d] += xyz[3 * (int64_t)atoms[k] + d];
@@ -1415,7 +1416,8 @@ __device__ double lane_rmsd(int n, const int32_t *atoms, const double *xyz, cons
         ca[d] /= (double)n;
         cb[d] /= (double)n;
     }
-    double sumA = 0, sumB = 0, S[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double sumA = 0, sumB = 0;
+    for (int q = 0; q < 9; q++) S[q] = 0.0;
     for (int k = 0; k < n; k++) {
         double a[3], b[3];
         for (int d = 0; d < 3; d++) {
@@ -1427,9 +1429,16 @@ __device__ double lane_rmsd(int n, const int32_t *atoms, const double *xyz, cons
         for (int r = 0; r < 3; r++)
             for (int c = 0; c < 3; c++) S[3 * r + c] += a[r] * b[c];
     }
+    *E0 = 0.5 * (sumA + sumB);
+}
+
+// RMSD of one assignment computed by a single thread, used where a lane
+// needs the value while searching (the same arithmetic as k_superpose).
+__device__ double lane_rmsd(int n, const int32_t *atoms, const double *xyz, const double *tpos) {
+    double ca[3], cb[3], S[9], E0;
+    lane_covariance(n, atoms, xyz, tpos, ca, cb, S, &E0);
     double K[4][4];
     key_matrix(S, K);
-    double E0 = 0.5 * (sumA + sumB);
     bool close = false;
     double lam = key_lambda(S, K, E0, &close);
     if (close) {
@@ -2092,61 +2101,37 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
 }
 
 
-// Superposition of every complete row (warp per row), written to the row's
-// slot in reference order.
+// Superposition of every complete row, one thread per row (the FP64
+// eigen-solve fills all lanes), written to the row's slot in reference
+// order.
 __global__ void k_superpose(ChunkView cv, TemplateView tv, CompleteRows in, RowResults out) {
-    int lane = lane_id();
-    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
     int64_t nrows = *in.count;
     if (nrows > in.capacity) nrows = in.capacity;
     const int T = tv.n_templates;
-    for (int64_t i = warp; i < nrows; i += nwarps) {
-        int pair = in.pair[i];
-        int s = pair / T, t = pair % T;
-        int ab = tv.atom_begin[t];
-        int n = tv.atom_begin[t + 1] - ab;
+    for (int64_t i = tid; i < nrows; i += nthreads) {
+        const int pair = in.pair[i];
+        const int s = pair / T, t = pair % T;
+        const int ab = tv.atom_begin[t];
+        const int n = tv.atom_begin[t + 1] - ab;
         const double *xyz = cv.xyz64 + 3 * cv.atom_base[s];
-        double a[3] = {0, 0, 0}, b[3] = {0, 0, 0};
-        if (lane < n) {
-            const int32_t atom = in.atoms[i * in.stride + lane];
-            for (int d = 0; d < 3; d++) {
-                a[d] = xyz[3 * (int64_t)atom + d];
-                b[d] = tv.pos[3 * (ab + lane) + d];
-            }
-        }
-        double ca[3], cb[3];
-        for (int d = 0; d < 3; d++) {
-            ca[d] = warp_sum(a[d]) / (double)n;
-            cb[d] = warp_sum(b[d]) / (double)n;
-        }
-        double ac[3] = {0, 0, 0}, bc[3] = {0, 0, 0};
-        if (lane < n)
-            for (int d = 0; d < 3; d++) {
-                ac[d] = a[d] - ca[d];
-                bc[d] = b[d] - cb[d];
-            }
-        double sumA = warp_sum(ac[0] * ac[0] + ac[1] * ac[1] + ac[2] * ac[2]);
-        double sumB = warp_sum(bc[0] * bc[0] + bc[1] * bc[1] + bc[2] * bc[2]);
-        double S[9];
-        for (int r = 0; r < 3; r++)
-            for (int c = 0; c < 3; c++) S[3 * r + c] = warp_sum(ac[r] * bc[c]);
-        if (lane == 0) {
-            double rmsd = 0.0, R[9];
-            bool bad = false;
-            quaternion_fit(S, 0.5 * (sumA + sumB), n, &rmsd, R, &bad);
-            // rows whose rmsd already decided the max_candidates cut keep it,
-            // so the automaton replays the same decisions
-            if (in.rmsd) rmsd = in.rmsd[i];
-            const int64_t d = out.off_q[(int64_t)s * T + (T - 1 - t)] + in.ordinal[i];
-            out.rmsd[d] = rmsd;
-            out.nan_rot[d] = bad ? 1 : 0;
-            out.src[d] = i;
-            for (int q = 0; q < 9; q++) out.rot[9 * d + q] = R[q];
-            for (int k = 0; k < 3; k++) {
-                out.centres[6 * d + k] = ca[k];
-                out.centres[6 * d + 3 + k] = cb[k];
-            }
+        double ca[3], cb[3], S[9], E0;
+        lane_covariance(n, in.atoms + i * in.stride, xyz, tv.pos + 3 * (int64_t)ab, ca, cb, S, &E0);
+        double rmsd = 0.0, R[9];
+        bool bad = false;
+        quaternion_fit(S, E0, n, &rmsd, R, &bad);
+        // rows whose rmsd already decided the max_candidates cut keep it, so
+        // the automaton replays the same decisions
+        if (in.rmsd) rmsd = in.rmsd[i];
+        const int64_t d = out.off_q[(int64_t)s * T + (T - 1 - t)] + in.ordinal[i];
+        out.rmsd[d] = rmsd;
+        out.nan_rot[d] = bad ? 1 : 0;
+        out.src[d] = i;
+        for (int q = 0; q < 9; q++) out.rot[9 * d + q] = R[q];
+        for (int k = 0; k < 3; k++) {
+            out.centres[6 * d + k] = ca[k];
+            out.centres[6 * d + 3 + k] = cb[k];
         }
     }
 }
@@ -2404,7 +2389,7 @@ cudaError_t launch_search(cudaStream_t st, int grid, bool wide, bool fp32, const
 
 void launch_superpose(cudaStream_t st, int blocks, const ChunkView &cv, const TemplateView &tv,
                       const CompleteRows &in, const RowResults &out) {
-    k_superpose<<<blocks, 256, 0, st>>>(cv, tv, in, out);
+    k_superpose<<<blocks, 128, 0, st>>>(cv, tv, in, out);
 }
 
 void launch_order_counts(cudaStream_t st, int64_t n_pairs, int32_t n_templates, const int32_t *pair_rows,
