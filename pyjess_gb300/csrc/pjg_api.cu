@@ -731,7 +731,19 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
 
     {
         // chunks of structures under an entry budget
-        const int64_t ENTRY_BUDGET = 48ll << 20;
+        // entries per chunk: candidate lists cost ~42 B an entry (atom and
+        // FP32 point, candidate and leaf order, block boxes); a third of the
+        // free device memory, at least 48M and at most 2G entries.  Fewer,
+        // larger chunks leave fewer kernel tails (a launch waits for its
+        // heaviest list or pair).  PJG_ENTRY_BUDGET overrides it.
+        int64_t ENTRY_BUDGET = 48ll << 20;
+        {
+            size_t free_b = 0, total_b = 0;
+            if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+                ENTRY_BUDGET = std::max<int64_t>(ENTRY_BUDGET, std::min<int64_t>(2ll << 30, (int64_t)(free_b / 3 / 42)));
+            const char *v = getenv("PJG_ENTRY_BUDGET");
+            if (v && atoll(v) > 0) ENTRY_BUDGET = atoll(v);
+        }
         const int max_chunk = P->mode == PJG_MODE_PLAIN_FP64 ? 1 : 4096;
         int s0 = 0;
         int64_t c_cap = 1 << 20;
@@ -834,6 +846,15 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             CUDA_TRY(cudaStreamSynchronize(st));
             const int64_t n_pairs = (int64_t)Sc * T;
             CUDA_TRY(dalloc(d_pair_rows, (size_t)n_pairs, st));
+            if (c_cap < 2 * n_pairs) {
+                // room for two complete rows a pair before the first attempt
+                // (a rerun of the search costs a whole chunk)
+                c_cap = 2 * n_pairs;
+                CUDA_TRY(dalloc(d_c_pair, c_cap, st));
+                CUDA_TRY(dalloc(d_c_ord, c_cap, st));
+                CUDA_TRY(dalloc(d_c_atoms, (size_t)c_cap * stride, st));
+                if (cut_inline) CUDA_TRY(dalloc(d_c_rmsd, c_cap, st));
+            }
             for (int attempt = 0; attempt < 8; attempt++) {
                 CUDA_TRY(cudaMemsetAsync(d_pair_counter.p, 0, sizeof(int32_t), st));
                 CUDA_TRY(cudaMemsetAsync(d_ccount.p, 0, sizeof(unsigned long long), st));

@@ -939,6 +939,7 @@ struct SortedWarp {
             uint32_t bits[SORT_WINDOW_WORDS];
             uint16_t wpre[SORT_WINDOW_WORDS];  // set bits before each word
             uint32_t ur[M];                    // unique rank of each element
+            uint32_t lr[M];                    // strict-lower rank of each element
         } so;
         struct {
             uint16_t F[M];    // left-flag prefix counts (VAL of a replay)
@@ -1004,7 +1005,11 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
             const uint32_t *lrk = cv.lrank + a * cv.n_atoms + gbase;
             uint16_t *Sa = L.buf[a];
 #pragma unroll 4
-            for (int e = lane; e < m; e += 32) L.u.so.ur[e] = ur[ca[e]];
+            for (int e = lane; e < m; e += 32) {
+                const int atom = ca[e];
+                L.u.so.ur[e] = ur[atom];
+                L.u.so.lr[e] = lrk[atom];
+            }
             int placed = 0;
             for (int wb = 0; wb < natoms; wb += SORT_WINDOW_BITS) {
                 const int nwords = min(SORT_WINDOW_WORDS, (natoms - wb + 31) >> 5);
@@ -1051,11 +1056,10 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
             // dense ranks: a new run wherever the strict-lower rank changes
             int c0 = 0;
             uint32_t prev = 0;
-#pragma unroll 2
             for (int p0 = 0; p0 < m; p0 += 32) {
                 const int p = p0 + lane;
                 const int e = p < m ? Sa[p] : 0;
-                const uint32_t l = p < m ? lrk[ca[e]] : 0u;
+                const uint32_t l = p < m ? L.u.so.lr[e] : 0u;
                 uint32_t before = __shfl_up_sync(FULL_MASK, l, 1);
                 if (lane == 0) before = prev;
                 const bool chg = p < m && (p == 0 || l != before);
@@ -1075,23 +1079,38 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
         int nd = 0;
         int levels = 0;
         while ((1 << levels) < m) levels++;
-        for (int d = 0; d < levels && !bail; d++) {
-            const int a = d % 3;
-            const int ca_buf = a == 0 ? cur0 : a == 1 ? cur1 : cur2;
-            const uint16_t *Sa = L.buf[ca_buf];
-            const uint16_t *Ra = L.run[a];
-            int ntied = 0;
+        // flags (element goes left) and tied nodes of level `lev`, from the
+        // axis order `Sx` and the node table; fused into the node update
+        // of the level before
+        int ntied = 0;
+        auto mark_level = [&](int lev) {
+            const int ax = lev % 3;
+            const uint16_t *Sx = L.buf[ax == 0 ? cur0 : ax == 1 ? cur1 : cur2];
+            const uint16_t *Rx = L.run[ax];
+            ntied = 0;
             for (int p0 = 0; p0 < m; p0 += 32) {
                 const int p = p0 + lane;
                 bool tie = false;
                 int lo = 0;
                 if (p < m) {
-                    const uint32_t sg = L.u.sp.seg[p];
+                    uint32_t sg = L.u.sp.seg[p];
                     lo = (int)(sg & 0xFFFFu);
-                    const int n = (int)(sg >> 16), k = n >> 1;
-                    const int e = Sa[p];
+                    int n = (int)(sg >> 16);
+                    if (lev > 0 && n >= 2) {
+                        // the node of level lev holding p (child of sg)
+                        const int k = n >> 1;
+                        if (p < lo + k) n = k;
+                        else {
+                            lo += k;
+                            n -= k;
+                        }
+                        sg = (uint32_t)lo | ((uint32_t)n << 16);
+                        L.u.sp.seg[p] = sg;
+                    }
+                    const int k = n >> 1;
+                    const int e = Sx[p];
                     L.u.sp.flag[e] = (uint8_t)(n >= 2 && p < lo + k);
-                    if (n >= 2 && p == lo + k) tie = Ra[Sa[p - 1]] == Ra[e];
+                    if (n >= 2 && p == lo + k) tie = Rx[Sx[p - 1]] == Rx[e];
                 }
                 const unsigned mask = __ballot_sync(FULL_MASK, tie);
                 if (tie) {
@@ -1100,6 +1119,11 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
                 }
                 ntied += __popc(mask);
             }
+            __syncwarp();
+        };
+        if (levels > 0) mark_level(0);
+        for (int d = 0; d < levels && !bail; d++) {
+            const int a = d % 3;
             __syncwarp();
             if (ntied > LEAF_MAX_TIED) {
                 bail = true;
@@ -1192,16 +1216,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
                 bail = true;
                 break;
             }
-            for (int p = lane; p < m; p += 32) {
-                const uint32_t sg = L.u.sp.seg[p];
-                const int lo = (int)(sg & 0xFFFFu), n = (int)(sg >> 16);
-                if (n >= 2) {
-                    const int k = n >> 1;
-                    L.u.sp.seg[p] = p < lo + k ? ((uint32_t)lo | ((uint32_t)k << 16))
-                                               : ((uint32_t)(lo + k) | ((uint32_t)(n - k) << 16));
-                }
-            }
-            __syncwarp();
+            if (d + 1 < levels) mark_level(d + 1);
         }
         if (bail) {
             n_exact++;
