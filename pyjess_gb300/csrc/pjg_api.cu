@@ -23,6 +23,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <numeric>
 #include <atomic>
 #include <string>
@@ -683,6 +684,24 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
         if (dev != tp->device || dev != sp->device) {
             delete res;
             return fail(PJG_ERR_INVALID, "templates, structures and the calling thread use different devices");
+        }
+    }
+    {
+        // keep the stream-ordered pool's memory mapped between queries (up
+        // to half the device) instead of returning it at every sync: the
+        // next query's chunk buffers then need no new mappings
+        static std::mutex m;
+        static bool done[256] = {};
+        std::lock_guard<std::mutex> g(m);
+        if (res->device >= 0 && res->device < 256 && !done[res->device]) {
+            cudaMemPool_t pool;
+            size_t fb = 0, tb = 0;
+            if (cudaDeviceGetDefaultMemPool(&pool, res->device) == cudaSuccess && cudaMemGetInfo(&fb, &tb) == cudaSuccess) {
+                uint64_t thr = tb / 2;
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+            }
+            cudaGetLastError();
+            done[res->device] = true;
         }
     }
     CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));

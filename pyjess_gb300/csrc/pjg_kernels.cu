@@ -1910,69 +1910,99 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
                         chain_par = ppar;
                         __syncwarp();
                     }
-                    // next block >= cursor whose bounding box meets the join box
+                    // every block from the cursor on whose bounding box meets
+                    // the join box, in order: its 32 candidates are tested by
+                    // the 32 lanes and the passing ones become children (or
+                    // complete rows); the parent is left early only when the
+                    // child tile cannot take another block
                     const int nblk = (mc + 31) >> 5;
-                    int found = -1;
-                    for (int g0 = st.cnd[lev]; g0 < nblk; g0 += 32) {
-                        int b = g0 + lane;
+                    int ncnt = ccnt;
+                    int resume = -1;
+                    for (int g0 = st.cnd[lev]; g0 < nblk && resume < 0 && !stop; g0 += 32) {
+                        const int b = g0 + lane;
                         bool hit = false;
                         if (b < nblk) {
-                            float4 bl = cd.blk_lo[st.blk_off[child] + b];
-                            float4 bh = cd.blk_hi[st.blk_off[child] + b];
+                            const float4 bl = cd.blk_lo[st.blk_off[child] + b];
+                            const float4 bh = cd.blk_hi[st.blk_off[child] + b];
                             hit = !(bl.x > box_hi[0] || bh.x < box_lo[0] || bl.y > box_hi[1] || bh.y < box_lo[1] ||
                                     bl.z > box_hi[2] || bh.z < box_lo[2]);
                         }
                         unsigned hm = __ballot_sync(FULL_MASK, hit);
-                        if (hm) {
-                            found = g0 + __ffs(hm) - 1;
-                            break;
+                        while (hm) {
+                            const int blk = g0 + __ffs(hm) - 1;
+                            hm &= hm - 1;
+                            cr = blk * 32 + lane;
+                            pass = false;
+                            if (cr < mc) {
+                                const float4 xc = cd.leaf_xyz[coff + cr];
+                                const int32_t kn = __float_as_int(xc.w);
+                                pass = true;
+                                unsigned exact = 0;
+                                for (int j = 0; j <= lev; j++) {
+                                    const float4 xj = st.cxyz[j];
+                                    if (!check_pair(__float_as_int(xj.w), kn, st.tkey[j], tn, sa.ignore_chain)) {
+                                        pass = false;
+                                        break;
+                                    }
+                                    if (FP32) {
+                                        const float dx = xj.x - xc.x, dy = xj.y - xc.y, dz = xj.z - xc.z;
+                                        const float d2 = dx * dx + dy * dy + dz * dz;
+                                        const float4 th = st.cthr[j];
+                                        if (d2 < th.x || d2 > th.w) {
+                                            pass = false;
+                                            break;
+                                        }
+                                        if (!(d2 >= th.y && d2 <= th.z)) exact |= 1u << j;
+                                    } else {
+                                        exact |= 1u << j;
+                                    }
+                                }
+                                if (pass && exact) {
+                                    if (FP32) rechecks += __popc(exact);
+                                    int32_t atoms[32];
+                                    for (int j = 0; j <= lev; j++) atoms[j] = level_atom(j, st.cpos[j]);
+                                    pass = decide_fp64(exact, lev, atoms, cd.leaf_atom[coff + cr], xyz64, prm, st.order,
+                                                       n, qn, cd.leaf_atom + coff, mc, cr);
+                                }
+                            }
+                            const unsigned m = __ballot_sync(FULL_MASK, pass);
+                            if (last) {
+                                int32_t pos[32];
+                                for (int j = 0; j <= lev; j++) pos[j] = st.cpos[j];
+                                emit(pass, pos, cr);
+                            } else if (pass) {
+                                E e;
+                                e.pos = (PosT)cr;
+                                e.parent = (uint16_t)ppar;
+                                ctile[ncnt + __popc(m & ((1u << lane) - 1u))] = e;
+                            }
+                            if (!last) ncnt += __popc(m);
+                            if (lane == 0) st.F[child] += __popc(m);
+                            if (stop) break;
+                            if (!last && cap - ncnt < 32) {
+                                // child tile full: finish it first, then
+                                // come back to this parent at the next block
+                                resume = blk + 1;
+                                break;
+                            }
                         }
+                        if (over_budget()) stop = true;
                     }
                     __syncwarp();
-                    if (found < 0) {
-                        if (lane == 0) {
+                    if (lane == 0) {
+                        if (!last) st.cnt[child] = ncnt;
+                        if (resume >= 0) {
+                            st.cnd[lev] = resume;
+                            st.par[child] = 0;
+                            st.cnd[child] = 0;
+                        } else {
                             st.par[lev] = ppar + 1;
                             st.cnd[lev] = 0;
                         }
-                        __syncwarp();
-                        continue;
-                    }
-                    cr = found * 32 + lane;
-                    if (cr < mc) {
-                        float4 xc = cd.leaf_xyz[coff + cr];
-                        int32_t kn = __float_as_int(xc.w);
-                        pass = true;
-                        unsigned exact = 0;
-                        for (int j = 0; j <= lev; j++) {
-                            float4 xj = st.cxyz[j];
-                            if (!check_pair(__float_as_int(xj.w), kn, st.tkey[j], tn, sa.ignore_chain)) {
-                                pass = false;
-                                break;
-                            }
-                            if (FP32) {
-                                float dx = xj.x - xc.x, dy = xj.y - xc.y, dz = xj.z - xc.z;
-                                float d2 = dx * dx + dy * dy + dz * dz;
-                                float4 th = st.cthr[j];
-                                if (d2 < th.x || d2 > th.w) {
-                                    pass = false;
-                                    break;
-                                }
-                                if (!(d2 >= th.y && d2 <= th.z)) exact |= 1u << j;
-                            } else {
-                                exact |= 1u << j;
-                            }
-                        }
-                        if (pass && exact) {
-                            if (FP32) rechecks += __popc(exact);
-                            int32_t atoms[32];
-                            for (int j = 0; j <= lev; j++) atoms[j] = level_atom(j, st.cpos[j]);
-                            pass = decide_fp64(exact, lev, atoms, cd.leaf_atom[coff + cr], xyz64, prm, st.order, n,
-                                               qn, cd.leaf_atom + coff, mc, cr);
-                        }
                     }
                     __syncwarp();
-                    if (lane == 0) st.cnd[lev] = found + 1;
-                    __syncwarp();
+                    if (resume >= 0) lev = child;
+                    continue;
                 } else {
                     // ---------------- product mode ----------------
                     int batch = last ? 32 : min(32, cap - ccnt);
