@@ -942,7 +942,8 @@ struct SortedWarp {
             uint32_t lr[M];                    // strict-lower rank of each element
         } so;
         struct {
-            uint16_t F[M];    // left-flag prefix counts (VAL of a replay)
+            uint16_t base[M]; // left members of the nodes before a position's node
+            uint16_t VAL[M];  // replay scratch
             uint16_t PTR[M];  // replay scratch
             uint16_t A[M];    // qselect arrangement of replayed nodes
             uint32_t seg[M];  // node of each position: lo | n << 16
@@ -1088,9 +1089,10 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
             const uint16_t *Sx = L.buf[ax == 0 ? cur0 : ax == 1 ? cur1 : cur2];
             const uint16_t *Rx = L.run[ax];
             ntied = 0;
+            int left_before = 0;  // left positions of the level before this chunk
             for (int p0 = 0; p0 < m; p0 += 32) {
                 const int p = p0 + lane;
-                bool tie = false;
+                bool tie = false, left = false, start = false;
                 int lo = 0;
                 if (p < m) {
                     uint32_t sg = L.u.sp.seg[p];
@@ -1109,9 +1111,16 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
                     }
                     const int k = n >> 1;
                     const int e = Sx[p];
-                    L.u.sp.flag[e] = (uint8_t)(n >= 2 && p < lo + k);
+                    left = n >= 2 && p < lo + k;
+                    start = p == lo;
+                    L.u.sp.flag[e] = (uint8_t)left;
                     if (n >= 2 && p == lo + k) tie = Rx[Sx[p - 1]] == Rx[e];
                 }
+                const unsigned lm = __ballot_sync(FULL_MASK, left);
+                if (start) L.u.sp.base[p] = (uint16_t)(left_before + __popc(lm & lt));
+                __syncwarp();
+                if (p < m && !start) L.u.sp.base[p] = L.u.sp.base[lo];
+                left_before += __popc(lm);
                 const unsigned mask = __ballot_sync(FULL_MASK, tie);
                 if (tie) {
                     const int slot = ntied + __popc(mask & lt);
@@ -1155,7 +1164,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
                         for (int p = lane; p < m; p += 32) L.u.sp.A[p] = (uint16_t)p;
                         __syncwarp();
                     }
-                    warp_qselect(L.u.sp.A, L.run[j % 3], L.buf[spare], L.u.sp.F, L.u.sp.PTR, lj, nj,
+                    warp_qselect(L.u.sp.A, L.run[j % 3], L.buf[spare], L.u.sp.VAL, L.u.sp.PTR, lj, nj,
                                  &counters[C_ERROR]);
                     if (lane == 0) L.u.sp.done[nd] = tag;
                     nd++;
@@ -1184,18 +1193,16 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
                     const bool f = valid && L.u.sp.flag[e];
                     const unsigned mask = __ballot_sync(FULL_MASK, f);
                     const int Fp = carry + __popc(mask & lt);
-                    if (valid) L.u.sp.F[p] = (uint16_t)Fp;
                     carry += __popc(mask);
-                    __syncwarp();
                     if (valid) {
                         const uint32_t sg = L.u.sp.seg[p];
                         const int lo = (int)(sg & 0xFFFFu), n = (int)(sg >> 16);
                         int to = p;
                         if (n >= 2) {
-                            const int k = n >> 1;
-                            const int lb = Fp - L.u.sp.F[lo];
-                            to = f ? lo + lb : lo + k + (p - lo) - lb;
-                            // inside the node by construction (exactly k
+                            // left members before p within its node
+                            const int lb = Fp - (int)L.u.sp.base[p];
+                            to = f ? lo + lb : p + (n >> 1) - lb;
+                            // inside the node by construction (exactly n/2
                             // left members); checked all the same
                             if (to < lo || to >= lo + n) {
                                 bad = true;
