@@ -243,7 +243,7 @@ def main():
             tr = json.load(f)
         # DRAM bytes per launch measured by ncu on a smaller case, scaled to
         # this workload's launch by the expansion bytes it processes
-        if tr.get("bytes_expansion"):
+        if tr.get("bytes_expansion_per_launch"):
             per_launch_exp = exp_bytes / max(1, sum(s["chunks"] for s in stats))
             traffic = tr["dram_bytes_per_launch"] * per_launch_exp / tr["bytes_expansion_per_launch"]
 
