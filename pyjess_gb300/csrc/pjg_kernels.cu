@@ -351,8 +351,11 @@ __device__ __noinline__ void kd_exact(int32_t *perm, int m, const int32_t *ca, c
 }
 
 struct LeafWarp {
-    float v[3][LEAF_FAST_MAX];       // FP32 coordinates by candidate index
-    float cur[LEAF_FAST_MAX];        // current axis values in position order
+    uint32_t ur[3][LEAF_FAST_MAX];   // unique axis ranks by candidate index
+    uint16_t lr[3][LEAF_FAST_MAX];   // strict-lower axis ranks (low 16 bits: equal
+                                     // ranks stay equal, a rare false tie only
+                                     // sends the list to k_leaf_sorted)
+    uint32_t cur[LEAF_FAST_MAX];     // current axis unique rank in position order
     uint16_t ord[2][LEAF_FAST_MAX];  // candidate index at each position
     uint16_t seg_lo[LEAF_FAST_MAX];  // node (segment) of each position
     uint16_t seg_n[LEAF_FAST_MAX];
@@ -395,8 +398,8 @@ __device__ void write_leaves(const uint16_t *order, int m, int64_t o, const int3
     write_boxes(m, o, leaf_xyz, bo, blk_lo, blk_hi);
 }
 
-// Short lists (at most rank_max entries) without a tie: rank method, one
-// warp per list.  Longer or tied lists go to k_leaf_sorted's worklists (up
+// Short lists (at most rank_max entries) without a tie: rank method (each
+// entry's rank in its node by counting smaller keys), one warp per list.  Longer or tied lists go to k_leaf_sorted's worklists (up
 // to LEAF_SORTED_MAX entries), the rest to k_leaf_exact's.
 __global__ void __launch_bounds__(LEAF_WARPS * 32)
     k_leaf_order(ChunkView cv, int32_t n_sigs, const int32_t *count, const int64_t *offset,
@@ -418,23 +421,29 @@ __global__ void __launch_bounds__(LEAF_WARPS * 32)
         bool tie = m > rank_max;
         int src = 0;
         if (!tie) {
+            // keys: the atoms' unique axis ranks (an exact order of the FP64
+            // coordinates, equal ones by atom index); a tie at a median
+            // boundary is read from the strict-lower ranks
+            const int64_t gbase = cv.atom_base[w / n_sigs];
+            const int32_t *ca = cand_atom + o;
             for (int i = lane; i < m; i += 32) {
-                float4 p = cand_xyz[o + i];
-                L.v[0][i] = p.x;
-                L.v[1][i] = p.y;
-                L.v[2][i] = p.z;
-                L.cur[i] = p.x;
+                const int64_t g = gbase + ca[i];
+                for (int a = 0; a < 3; a++) {
+                    L.ur[a][i] = cv.urank[a * cv.n_atoms + g];
+                    L.lr[a][i] = (uint16_t)cv.lrank[a * cv.n_atoms + g];
+                }
                 L.ord[0][i] = (uint16_t)i;
                 L.seg_lo[i] = 0;
                 L.seg_n[i] = (uint16_t)m;
             }
+            __syncwarp();
+            for (int i = lane; i < m; i += 32) L.cur[i] = L.ur[0][i];
             __syncwarp();
             int levels = 0;
             while ((1 << levels) < m) levels++;
             for (int d = 0; d < levels; d++) {
                 const uint16_t *A = L.ord[src];
                 uint16_t *B = L.ord[src ^ 1];
-                bool t = false;
                 for (int p = lane; p < m; p += 32) {
                     const int lo = L.seg_lo[p], n = L.seg_n[p];
                     const int e = A[p];
@@ -442,30 +451,23 @@ __global__ void __launch_bounds__(LEAF_WARPS * 32)
                         B[p] = (uint16_t)e;
                         continue;
                     }
-                    const float x = L.cur[p];
-                    int less = 0, eq = 0, before = 0;
-#pragma unroll 4
-                    for (int q = lo; q < lo + n; q++) {
-                        const float y = L.cur[q];
-                        less += y < x;
-                        eq += y == x;
-                        before += (y < x) | ((y == x) & (q < p));
-                    }
-                    const int k = n / 2;
-                    if (less < k && less + eq > k) t = true;
+                    const uint32_t x = L.cur[p];
+                    int before = 0;
+#pragma unroll 8
+                    for (int q = lo; q < lo + n; q++) before += L.cur[q] < x;
                     B[lo + before] = (uint16_t)e;
                 }
                 __syncwarp();
-                if (__any_sync(FULL_MASK, t)) {
-                    tie = true;
-                    break;
-                }
-                const int nax = (d + 1) % 3;
+                // median-boundary ties, next axis keys, child nodes
+                const int ax = d % 3, nax = (d + 1) % 3;
+                bool t = false;
                 for (int p = lane; p < m; p += 32) {
                     const int lo = L.seg_lo[p], n = L.seg_n[p];
-                    L.cur[p] = L.v[nax][B[p]];
+                    const int e = B[p];
+                    L.cur[p] = L.ur[nax][e];
                     if (n <= 1) continue;
                     const int k = n / 2;
+                    if (p == lo + k && L.lr[ax][B[p - 1]] == L.lr[ax][e]) t = true;
                     if (p < lo + k) {
                         L.seg_n[p] = (uint16_t)k;
                     } else {
@@ -475,6 +477,10 @@ __global__ void __launch_bounds__(LEAF_WARPS * 32)
                 }
                 src ^= 1;
                 __syncwarp();
+                if (__any_sync(FULL_MASK, t)) {
+                    tie = true;
+                    break;
+                }
             }
         }
         if (tie) {
