@@ -136,6 +136,12 @@ typedef struct {
     double ms_total;                 /* device time of the whole query     */
     int32_t launches;                /* kernels launched by the query      */
     int32_t chunks;                  /* structure chunks processed         */
+    int64_t leaf_lists;              /* lists put in kd leaf order         */
+    int64_t leaf_entries;            /* entries of those lists             */
+    int64_t suspensions;             /* pair searches stopped at a list
+                                        with no leaf order yet (rerun)     */
+    int32_t search_rounds;           /* search launches                    */
+    int32_t pad;
 } pjg_stats;
 
 typedef struct pjg_templates pjg_templates;

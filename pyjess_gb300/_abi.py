@@ -72,6 +72,11 @@ class Stats(C.Structure):
         ("ms_total", C.c_double),
         ("launches", C.c_int32),
         ("chunks", C.c_int32),
+        ("leaf_lists", C.c_int64),
+        ("leaf_entries", C.c_int64),
+        ("suspensions", C.c_int64),
+        ("search_rounds", C.c_int32),
+        ("pad", C.c_int32),
     ]
 
     def as_dict(self) -> dict:

@@ -609,10 +609,14 @@ int sm_count() {
 }
 
 // exclusive scan in[0..n) -> out[0..n), recursive over tile sums
+// kernels launched by scan_exclusive on this thread (query statistics)
+thread_local int t_scan_launches = 0;
+
 template <typename T>
 cudaError_t scan_exclusive(const T *in, int64_t n, int64_t *out, std::vector<DBuf<int64_t>> &tmp,
                            cudaStream_t st, int depth = 0) {
     if (n <= 0) return cudaSuccess;
+    t_scan_launches += n > SCAN_TILE_ITEMS ? 2 : 1;
     const int TILE = SCAN_TILE_ITEMS;
     int64_t tiles = (n + TILE - 1) / TILE;
     if ((int)tmp.size() < 2 * (depth + 1)) tmp.resize(2 * (depth + 1));
@@ -660,6 +664,11 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     DBuf<unsigned long long> d_counters, d_ccount, d_rtotals;
     DBuf<int32_t> d_c_pair, d_c_atoms, d_pair_rows, d_cnt_q;
     DBuf<int64_t> d_c_ord, d_off_q;
+    // lists ordered on demand: per-list state, requested lists, suspended pairs
+    DBuf<int32_t> d_lstate;
+    DBuf<int64_t> d_work;
+    DBuf<unsigned long long> d_nwork, d_nsusp;
+    DBuf<Suspended> d_susp_a, d_susp_b;
     DBuf<double> d_c_rmsd;
     // per complete row, in reference order
     DBuf<double> d_r_rmsd, d_r_rot, d_r_cen;
@@ -670,8 +679,21 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     const int stride = std::max(tp->nmax, 1);
     unsigned long long counters[C_NUM] = {};
     float ms = 0.f;
-    double ms_cand = 0, ms_exp = 0, ms_sup = 0, ms_total = 0;
-    int launches = 0, chunks = 0;
+    double ms_cand = 0, ms_exp = 0, ms_sup = 0, ms_total = 0, ms_search = 0;
+    int launches = 0, chunks = 0, search_rounds = 0;
+    t_scan_launches = 0;
+    int64_t suspensions = 0;
+    // levels whose lists are put in kd leaf order before the search (deeper
+    // lists when a pair's frontier first reaches them); PJG_LEAF_LEVELS
+    // overrides it, a negative value orders every list up front.  The plain
+    // per-structure path orders every list up front: with one structure a
+    // chunk, the host round trip of each extra search round costs more
+    // than the ordering it saves.
+    int demand_levels = P->mode == PJG_MODE_PLAIN_FP64 ? -1 : 5;
+    {
+        const char *v = getenv("PJG_LEAF_LEVELS");
+        if (v && *v) demand_levels = atoi(v);
+    }
     std::vector<int64_t> totals(S);
 
     if (T == 0 || S == 0) {
@@ -779,6 +801,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 s1++;
             }
             chunks++;
+            const double ms_search_chunk0 = ms_search;
             const int Sc = s1 - s0;
             const int64_t Wc = (int64_t)Sc * G;
             ChunkView cv{Sc, sp->d_atom_base + s0, sp->d_atom_count + s0, sp->d_xyz64, sp->d_xyz32, sp->d_name,
@@ -815,26 +838,64 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 int blocks = (int)std::min<int64_t>((Wc + 7) / 8, (int64_t)sm_count() * 32);
                 launch_candidates(st, std::max(blocks, 1), true, cv, sv, nullptr, nullptr, d_offset.p, d_cand_atom.p,
                                   d_cand_xyz.p);
-                int lb = (int)std::min<int64_t>((Wc + LEAF_WARPS - 1) / LEAF_WARPS, (int64_t)sm_count() * 32);
                 CUDA_TRY(dalloc(d_exact_list, (size_t)Wc, st));
                 CUDA_TRY(dalloc(d_exact_count, 1, st));
                 CUDA_TRY(dalloc(d_sorted_list, 3 * (size_t)Wc, st));
                 CUDA_TRY(dalloc(d_sorted_count, 3, st));
-                launch_leaf_order(st, std::max(lb, 1), cv, G, cnt_c, d_offset.p, d_boff.p, d_cand_atom.p,
-                                  d_cand_xyz.p, d_leaf_atom.p, d_leaf_xyz.p, d_blk_lo.p, d_blk_hi.p,
-                                  d_sorted_list.p, d_sorted_count.p, Wc, d_exact_list.p, d_exact_count.p,
-                                  d_counters.p);
-                launches += 9;
+                launches += 2;  // block counts, candidate fill
                 CUDA_TRY(cudaGetLastError());
             }
-            CUDA_TRY(cudaEventRecord(ev[2], st));
             TemplateView tv{T, tp->nmax, tp->d_atom_begin, tp->d_sig, tp->d_pos, tp->d_key, tp->d_param_begin,
                             d_params.p};
             CandView cd{G, cnt_c, d_offset.p, d_cand_atom.p, d_cand_xyz.p, d_leaf_atom.p, d_leaf_xyz.p,
                         d_boff.p, d_blk_lo.p, d_blk_hi.p};
+            const int64_t n_pairs = (int64_t)Sc * T;
+            // kd leaf order: up front for the lists of the first
+            // `demand_levels` levels of every pair that can run, later (between
+            // search rounds) for each deeper list a pair's frontier reaches;
+            // a negative value orders every list of the chunk up front
+            LeafDemand dm{};
+            const int leaf_blocks =
+                std::max(1, (int)std::min<int64_t>((Wc + LEAF_WARPS - 1) / LEAF_WARPS, (int64_t)sm_count() * 32));
+            auto order_requested = [&]() -> cudaError_t {
+                launch_leaf_order(st, leaf_blocks, cv, G, cnt_c, d_offset.p, d_boff.p, d_cand_atom.p, d_cand_xyz.p,
+                                  d_leaf_atom.p, d_leaf_xyz.p, d_blk_lo.p, d_blk_hi.p, d_sorted_list.p,
+                                  d_sorted_count.p, Wc, d_exact_list.p, d_exact_count.p, d_counters.p, dm.work,
+                                  dm.n_work);
+                launches += 6;
+                if (dm.state) {
+                    launch_mark_ordered(st, sm_count() * 4, dm);
+                    launches++;
+                }
+                return cudaGetLastError();
+            };
+            if (demand_levels < 0) {
+                CUDA_TRY(order_requested());
+            } else {
+                CUDA_TRY(dalloc(d_lstate, (size_t)Wc, st));
+                CUDA_TRY(dalloc(d_work, (size_t)Wc, st));
+                CUDA_TRY(dalloc(d_nwork, 1, st));
+                CUDA_TRY(dalloc(d_nsusp, 1, st));
+                CUDA_TRY(dalloc(d_susp_a, (size_t)n_pairs, st));
+                CUDA_TRY(dalloc(d_susp_b, (size_t)n_pairs, st));
+                CUDA_TRY(cudaMemsetAsync(d_lstate.p, 0, (size_t)Wc * sizeof(int32_t), st));
+                CUDA_TRY(cudaMemsetAsync(d_nwork.p, 0, sizeof(unsigned long long), st));
+                dm.state = d_lstate.p;
+                dm.work = d_work.p;
+                dm.n_work = d_nwork.p;
+                dm.n_suspended = d_nsusp.p;
+                if (n_pairs > INT32_MAX) {
+                    status = fail(PJG_ERR_CAPACITY, "too many pairs in one chunk");
+                    goto done;
+                }
+                launch_demand_levels(st, sm_count() * 16, tv, cd, (int32_t)n_pairs, demand_levels, P->reorder, dm);
+                launches++;
+                CUDA_TRY(order_requested());
+            }
+            CUDA_TRY(cudaEventRecord(ev[2], st));
             SearchArgs sa;
             sa.n_pairs = Sc * T;
-            if ((int64_t)Sc * T > INT32_MAX) {
+            if (n_pairs > INT32_MAX) {
                 status = fail(PJG_ERR_CAPACITY, "too many pairs in one chunk");
                 goto done;
             }
@@ -863,7 +924,6 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             unsigned long long snap[C_NUM];
             CUDA_TRY(cudaMemcpyAsync(snap, d_counters.p, sizeof snap, cudaMemcpyDeviceToHost, st));
             CUDA_TRY(cudaStreamSynchronize(st));
-            const int64_t n_pairs = (int64_t)Sc * T;
             CUDA_TRY(dalloc(d_pair_rows, (size_t)n_pairs, st));
             if (c_cap < 2 * n_pairs) {
                 // room for two complete rows a pair before the first attempt
@@ -875,26 +935,69 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 if (cut_inline) CUDA_TRY(dalloc(d_c_rmsd, c_cap, st));
             }
             for (int attempt = 0; attempt < 8; attempt++) {
-                CUDA_TRY(cudaMemsetAsync(d_pair_counter.p, 0, sizeof(int32_t), st));
                 CUDA_TRY(cudaMemsetAsync(d_ccount.p, 0, sizeof(unsigned long long), st));
                 CUDA_TRY(cudaMemsetAsync(d_pair_rows.p, 0, (size_t)n_pairs * sizeof(int32_t), st));
                 CompleteRows cr{d_ccount.p, c_cap, stride, d_c_pair.p, d_c_ord.p, d_c_atoms.p,
                                 cut_inline ? d_c_rmsd.p : nullptr, d_pair_rows.p};
                 int grid = sm_count() * 8;
-                CUDA_TRY(launch_search(st, grid, wide, fp32, cv, tv, cd, sa, d_pair_counter.p, scn_c, cr, d_counters.p));
-                launches++;
-                CUDA_TRY(cudaGetLastError());
                 unsigned long long nc = 0;
-                CUDA_TRY(cudaMemcpyAsync(&nc, d_ccount.p, sizeof nc, cudaMemcpyDeviceToHost, st));
-                CUDA_TRY(cudaStreamSynchronize(st));
+                // search rounds: every pair, then the pairs suspended at a
+                // list that had no leaf order (ordered in between), until
+                // no pair is suspended
+                dm.resume = nullptr;
+                dm.n_resume = 0;
+                Suspended *next_out = d_susp_a.p, *spare = d_susp_b.p;
+                for (int round = 0;; round++) {
+                    CUDA_TRY(cudaMemsetAsync(d_pair_counter.p, 0, sizeof(int32_t), st));
+                    if (dm.state) {
+                        dm.suspended = next_out;
+                        CUDA_TRY(cudaMemsetAsync(d_nwork.p, 0, sizeof(unsigned long long), st));
+                        CUDA_TRY(cudaMemsetAsync(d_nsusp.p, 0, sizeof(unsigned long long), st));
+                    }
+                    CUDA_TRY(cudaEventRecord(ev[6], st));
+                    CUDA_TRY(launch_search(st, grid, wide, fp32, cv, tv, cd, sa, d_pair_counter.p, scn_c, cr,
+                                           d_counters.p, dm));
+                    CUDA_TRY(cudaEventRecord(ev[7], st));
+                    launches++;
+                    CUDA_TRY(cudaGetLastError());
+                    unsigned long long ns = 0;
+                    CUDA_TRY(cudaMemcpyAsync(&nc, d_ccount.p, sizeof nc, cudaMemcpyDeviceToHost, st));
+                    if (dm.state) CUDA_TRY(cudaMemcpyAsync(&ns, d_nsusp.p, sizeof ns, cudaMemcpyDeviceToHost, st));
+                    CUDA_TRY(cudaStreamSynchronize(st));
+                    {
+                        float m = 0.f;
+                        cudaEventElapsedTime(&m, ev[6], ev[7]);
+                        ms_search += m;
+                    }
+                    search_rounds++;
+                    if (ns == 0) break;
+                    if (round > 64) {
+                        status = fail(PJG_ERR_CAPACITY, "leaf order on demand did not converge");
+                        goto done;
+                    }
+                    suspensions += (int64_t)ns;
+                    // the lists the suspended pairs reached, then those pairs
+                    CUDA_TRY(order_requested());
+                    dm.resume = next_out;
+                    dm.n_resume = (int32_t)ns;
+                    std::swap(next_out, spare);
+                }
                 if ((int64_t)nc <= c_cap) break;
                 // the row buffer was too small: grow and run the chunk again
-                // (the counters of the failed attempt are rolled back)
+                // (the search counters of the failed attempt are rolled back;
+                // lists ordered meanwhile stay ordered)
                 c_cap = (int64_t)nc + nc / 4 + 1024;
                 CUDA_TRY(dalloc(d_c_pair, c_cap, st));
                 CUDA_TRY(dalloc(d_c_ord, c_cap, st));
                 CUDA_TRY(dalloc(d_c_atoms, (size_t)c_cap * stride, st));
                 if (cut_inline) CUDA_TRY(dalloc(d_c_rmsd, c_cap, st));
+                {
+                    unsigned long long cur[C_NUM];
+                    CUDA_TRY(cudaMemcpyAsync(cur, d_counters.p, sizeof cur, cudaMemcpyDeviceToHost, st));
+                    CUDA_TRY(cudaStreamSynchronize(st));
+                    for (int c : {C_LEAF_EXACT, C_LEAF_SORTED, C_LEAF_REPLAY, C_LEAF_LISTS, C_LEAF_ENTRIES, C_ERROR})
+                        snap[c] = cur[c];
+                }
                 CUDA_TRY(cudaMemcpyAsync(d_counters.p, snap, sizeof snap, cudaMemcpyHostToDevice, st));
             }
             CUDA_TRY(cudaEventRecord(ev[3], st));
@@ -956,8 +1059,10 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 cudaEventElapsedTime(&m1, ev[1], ev[2]);
                 cudaEventElapsedTime(&m2, ev[2], ev[3]);
                 cudaEventElapsedTime(&m3, ev[3], ev[4]);
-                ms_cand += m1;
-                ms_exp += m2;
+                // search launches count as expansion; the leaf order run
+                // between search rounds counts with the candidate lists
+                ms_cand += m1 + (m2 - (float)(ms_search - ms_search_chunk0));
+                ms_exp += ms_search - ms_search_chunk0;
                 ms_sup += m3;
             }
             s0 = s1;
@@ -999,8 +1104,12 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     res->stats.ms_expansion = ms_exp;
     res->stats.ms_superposition = ms_sup;
     res->stats.ms_total = ms_total;
-    res->stats.launches = launches;
+    res->stats.launches = launches + t_scan_launches;
     res->stats.chunks = chunks;
+    res->stats.leaf_lists = (int64_t)counters[C_LEAF_LISTS];
+    res->stats.leaf_entries = (int64_t)counters[C_LEAF_ENTRIES];
+    res->stats.suspensions = suspensions;
+    res->stats.search_rounds = search_rounds;
 
 done:
     if (st) {
@@ -1013,7 +1122,8 @@ done:
         dfree(d_exact_count, st); dfree(d_sorted_list, st); dfree(d_sorted_count, st);
         dfree(d_r_rmsd, st); dfree(d_r_rot, st); dfree(d_r_cen, st); dfree(d_r_nan, st); dfree(d_r_hit, st);
         dfree(d_r_warn, st); dfree(d_r_hatoms, st); dfree(d_r_src, st); dfree(d_r_hidx, st); dfree(d_r_widx, st);
-        dfree(d_r_aidx, st);
+        dfree(d_r_aidx, st); dfree(d_lstate, st); dfree(d_work, st); dfree(d_nwork, st); dfree(d_nsusp, st);
+        dfree(d_susp_a, st); dfree(d_susp_b, st);
         for (auto &b : scan_tmp) dfree(b, st);
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);

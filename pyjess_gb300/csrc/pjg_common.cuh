@@ -127,6 +127,8 @@ enum Counter : int {
     C_LEAF_EXACT,     // lists ordered by the exact sequential replay
     C_LEAF_SORTED,    // lists ordered by sorted axes
     C_LEAF_REPLAY,    // kd nodes replayed by qselect in the sorted-axis path
+    C_LEAF_LISTS,     // lists put in kd leaf order
+    C_LEAF_ENTRIES,   // entries of those lists
     C_ERROR,          // error code: 1 template > 32 atoms, 2 frontier tile too
                       // small, 3 time budget exhausted, 4 leaf order: too many
                       // small subtrees, 5 a partition did not converge, 6 an

@@ -406,17 +406,22 @@ __global__ void __launch_bounds__(LEAF_WARPS * 32)
                  const int64_t *blk_offset, const int32_t *cand_atom, const float4 *cand_xyz,
                  int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi, int64_t *sorted_list,
                  unsigned long long *sorted_count, int64_t list_cap, int64_t *exact_list,
-                 unsigned long long *exact_count, unsigned long long *counters, int rank_max) {
+                 unsigned long long *exact_count, unsigned long long *counters, int rank_max,
+                 const int64_t *work, const unsigned long long *n_work) {
     __shared__ LeafWarp sh[LEAF_WARPS];
     const int lane = lane_id();
     LeafWarp &L = sh[threadIdx.x >> 5];
     int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    int64_t total = (int64_t)cv.n_structures * n_sigs;
-    unsigned long long n_exact = 0, n_sorted = 0;
-    for (int64_t w = warp; w < total; w += nwarps) {
+    // the requested lists, or every list of the chunk
+    int64_t total = work ? (int64_t)*n_work : (int64_t)cv.n_structures * n_sigs;
+    unsigned long long n_exact = 0, n_sorted = 0, n_lists = 0, n_entries = 0;
+    for (int64_t item = warp; item < total; item += nwarps) {
+        const int64_t w = work ? work[item] : item;
         const int m = count[w];
         if (m <= 0) continue;
+        n_lists++;
+        n_entries += (unsigned long long)m;
         const int64_t o = offset[w];
         bool tie = m > rank_max;
         int src = 0;
@@ -500,6 +505,8 @@ __global__ void __launch_bounds__(LEAF_WARPS * 32)
     }
     if (lane == 0 && n_exact) atomicAdd(&counters[C_LEAF_EXACT], n_exact);
     if (lane == 0 && n_sorted) atomicAdd(&counters[C_LEAF_SORTED], n_sorted);
+    if (lane == 0 && n_lists) atomicAdd(&counters[C_LEAF_LISTS], n_lists);
+    if (lane == 0 && n_entries) atomicAdd(&counters[C_LEAF_ENTRIES], n_entries);
 }
 
 // Exact replay for the lists k_leaf_order could not order by ranks (a tie
@@ -1243,6 +1250,48 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     if (lane == 0 && n_replay) atomicAdd(&counters[C_LEAF_REPLAY], n_replay);
 }
 
+// Lists needed before the search starts: a pair with no empty candidate
+// list reads the lists of levels 1, 2, ... in kd leaf order as its frontier
+// reaches them; the lists of the first `max_level` levels are requested
+// here (warp per pair, the level order of k_search), deeper ones by the
+// search itself when a pair first reaches them.
+__global__ void k_demand_levels(TemplateView tv, CandView cd, int32_t n_pairs, int32_t max_level, int32_t reorder,
+                                LeafDemand dm) {
+    const int lane = lane_id();
+    const int T = tv.n_templates, G = cd.n_sigs;
+    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t pair = warp; pair < n_pairs; pair += nwarps) {
+        const int s = (int)(pair / T), t = (int)(pair % T);
+        const int ab = tv.atom_begin[t];
+        const int n = tv.atom_begin[t + 1] - ab;
+        if (n < 2 || n > 32) continue;
+        int c = INT_MAX;
+        int64_t w = 0;
+        if (lane < n) {
+            w = (int64_t)s * G + tv.sig[ab + lane];
+            c = cd.count[w];
+        }
+        if (__ballot_sync(FULL_MASK, lane < n && c == 0)) continue;
+        int rank = lane;
+        if (reorder) {
+            rank = 0;
+            for (int j = 0; j < n; j++) {
+                int cj = __shfl_sync(FULL_MASK, c, j);
+                if (cj < c || (cj == c && j < lane)) rank++;
+            }
+        }
+        if (lane < n && rank >= 1 && rank <= max_level && dm.state[w] == 0 && atomicCAS(&dm.state[w], 0, 1) == 0)
+            dm.work[atomicAdd(dm.n_work, 1ull)] = w;
+    }
+}
+
+__global__ void k_mark_ordered(LeafDemand dm) {
+    const int64_t n = (int64_t)*dm.n_work;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dm.state[dm.work[i]] = 2;
+}
+
 __global__ void k_block_counts(int64_t n, const int32_t *count, int32_t *nblk) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) nblk[i] = (count[i] + 31) / 32;
@@ -1620,7 +1669,7 @@ __device__ __noinline__ bool decide_fp64(unsigned exact_mask, int lev, const int
 template <typename PosT, bool FP32>
 __global__ void __launch_bounds__(SEARCH_WARPS * 32)
     k_search(ChunkView cv, TemplateView tv, CandView cd, SearchArgs sa, int32_t *pair_counter,
-             const int32_t *scanned, CompleteRows out, unsigned long long *counters) {
+             const int32_t *scanned, CompleteRows out, unsigned long long *counters, LeafDemand dm) {
     extern __shared__ __align__(16) unsigned char smem[];
     using E = Entry<PosT>;
     const int lane = lane_id();
@@ -1650,11 +1699,17 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
         return timed_out;
     };
 
+    // pairs of this round: every pair of the chunk, or the pairs that an
+    // earlier round suspended (each with the rows it has already emitted)
+    const bool fresh = dm.resume == nullptr;
+    const int n_items = fresh ? sa.n_pairs : dm.n_resume;
     for (;;) {
-        int pair = 0;
-        if (lane == 0) pair = atomicAdd(pair_counter, 1);
-        pair = __shfl_sync(FULL_MASK, pair, 0);
-        if (pair >= sa.n_pairs || timed_out) break;
+        int item = 0;
+        if (lane == 0) item = atomicAdd(pair_counter, 1);
+        item = __shfl_sync(FULL_MASK, item, 0);
+        if (item >= n_items || timed_out) break;
+        const int pair = fresh ? item : dm.resume[item].pair;
+        const int64_t skip = fresh ? 0 : dm.resume[item].skip;
         const int s = pair / T;
         const int t = pair % T;
         const int ab = tv.atom_begin[t];
@@ -1680,7 +1735,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
                 bc += __shfl_xor_sync(FULL_MASK, bc, o);
                 cc += __shfl_xor_sync(FULL_MASK, cc, o);
             }
-            if (lane == 0) {
+            if (lane == 0 && fresh) {
                 atomicAdd(&counters[C_PAIRS], 1ull);
                 atomicAdd(&counters[C_BYTES_CAND], (unsigned long long)bc);
                 atomicAdd(&counters[C_CAND], (unsigned long long)cc);
@@ -1706,9 +1761,13 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
         __syncwarp();
         // tile capacity: equal entry count for levels 0..n-2
         int cap = n >= 2 ? (int)min((int64_t)4096, tile_units / (n - 1)) : 0;
+        // levels whose list is in kd leaf order (level 0 reads the
+        // candidate order)
+        bool lvl_ready = true;
         if (lane < n) {
             int tk = st.order[lane];
             int64_t w2 = (int64_t)s * G + tv.sig[ab + tk];
+            if (dm.state && lane > 0) lvl_ready = dm.state[w2] == 2;
             st.lvl_off[lane] = cd.offset[w2];
             st.blk_off[lane] = cd.blk_offset[w2];
             st.lvl_cnt[lane] = cd.count[w2];
@@ -1719,6 +1778,8 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
             st.cnd[lane] = 0;
             st.tile[lane] = cap * lane;
         }
+        const unsigned ready_mask = __ballot_sync(FULL_MASK, lvl_ready);
+        bool suspended = false;
         __syncwarp();
         if (n >= 2 && cap < 32) {
             if (lane == 0) atomicMax(&counters[C_ERROR], 2ull);
@@ -1785,12 +1846,15 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
                 m = __ballot_sync(FULL_MASK, pass);
             }
             int np = __popc(m);
+            // rows before `skip` were emitted before the pair was suspended
+            const int64_t seen = skip - emitted;
+            const int nold = seen <= 0 ? 0 : seen >= np ? np : (int)seen;
             int64_t base = 0;
-            if (lane == 0) base = (int64_t)atomicAdd(out.count, (unsigned long long)np);
+            if (lane == 0 && np > nold) base = (int64_t)atomicAdd(out.count, (unsigned long long)(np - nold));
             base = __shfl_sync(FULL_MASK, base, 0);
-            if (pass) {
+            if (pass && __popc(m & ((1u << lane) - 1u)) >= nold) {
                 int rk = __popc(m & ((1u << lane) - 1u));
-                int64_t ri = base + rk;
+                int64_t ri = base + rk - nold;
                 if (ri < out.capacity) {
                     int32_t *dst = out.atoms + ri * out.stride;
                     for (int j = 0; j < n; j++) dst[j] = at[j];
@@ -1862,6 +1926,21 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
                     __syncwarp();
                     lev--;
                     continue;
+                }
+                if (!((ready_mask >> child) & 1u)) {
+                    // the child level's list has no kd leaf order yet:
+                    // request it and suspend the pair until the next round
+                    if (lane == 0) {
+                        const int64_t w = (int64_t)s * G + tv.sig[ab + st.order[child]];
+                        if (atomicCAS(&dm.state[w], 0, 1) == 0) dm.work[atomicAdd(dm.n_work, 1ull)] = w;
+                        Suspended sp;
+                        sp.pair = pair;
+                        sp.pad = 0;
+                        sp.skip = emitted > skip ? emitted : skip;
+                        dm.suspended[atomicAdd(dm.n_suspended, 1ull)] = sp;
+                    }
+                    suspended = true;
+                    break;
                 }
                 const int mc = st.lvl_cnt[child];
                 const int qn = st.order[child];
@@ -2141,6 +2220,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
             }
         }
         __syncwarp();
+        if (suspended) continue;
         if (lane == 0 && emitted > 0) out.pair_rows[pair] = (int32_t)emitted;
         // ---- statistics of the pair
         for (int o = 16; o; o >>= 1) rechecks += __shfl_xor_sync(FULL_MASK, rechecks, o);
@@ -2355,7 +2435,8 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
                        const int64_t *offset, const int64_t *blk_offset, const int32_t *cand_atom,
                        const float4 *cand_xyz, int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
                        int64_t *sorted_list, unsigned long long *sorted_count, int64_t list_cap,
-                       int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters) {
+                       int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters,
+                       const int64_t *work, const unsigned long long *n_work) {
     cudaMemsetAsync(sorted_count, 0, 3 * sizeof(unsigned long long), st);
     cudaMemsetAsync(exact_count, 0, sizeof(unsigned long long), st);
     // lists longer than rank_max take the sorted-axis split (the rank
@@ -2367,7 +2448,8 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
     }();
     k_leaf_order<<<blocks, LEAF_WARPS * 32, 0, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, cand_xyz,
                                                     leaf_atom, leaf_xyz, blk_lo, blk_hi, sorted_list, sorted_count,
-                                                    list_cap, exact_list, exact_count, counters, rank_max);
+                                                    list_cap, exact_list, exact_count, counters, rank_max,
+                                                    work, n_work);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -2413,6 +2495,15 @@ void launch_axis_ranks(cudaStream_t st, int32_t n_structures, const int64_t *ato
                                                                           tile_key, tile_idx, lrank, urank);
 }
 
+void launch_demand_levels(cudaStream_t st, int blocks, const TemplateView &tv, const CandView &cd, int32_t n_pairs,
+                          int32_t max_level, int32_t reorder, const LeafDemand &dm) {
+    if (n_pairs > 0 && max_level > 0) k_demand_levels<<<blocks, 256, 0, st>>>(tv, cd, n_pairs, max_level, reorder, dm);
+}
+
+void launch_mark_ordered(cudaStream_t st, int blocks, const LeafDemand &dm) {
+    k_mark_ordered<<<blocks, 256, 0, st>>>(dm);
+}
+
 void launch_block_counts(cudaStream_t st, int64_t n, const int32_t *count, int32_t *nblk) {
     if (n > 0) k_block_counts<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, count, nblk);
 }
@@ -2420,7 +2511,8 @@ void launch_block_counts(cudaStream_t st, int64_t n, const int32_t *count, int32
 template <typename RowT, bool FP32>
 static cudaError_t search_variant(cudaStream_t st, int grid, const ChunkView &cv, const TemplateView &tv,
                                   const CandView &cd, const SearchArgs &sa, int32_t *pair_counter,
-                                  const int32_t *scanned, const CompleteRows &out, unsigned long long *counters) {
+                                  const int32_t *scanned, const CompleteRows &out, unsigned long long *counters,
+                                  const LeafDemand &dm) {
     size_t smem = (size_t)sa.warp_smem * SEARCH_WARPS;
     cudaError_t e = cudaFuncSetAttribute(k_search<RowT, FP32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -2431,18 +2523,21 @@ static cudaError_t search_variant(cudaStream_t st, int grid, const ChunkView &cv
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (per_sm > 0 && sms > 0) grid = per_sm * sms;
-    k_search<RowT, FP32><<<grid, SEARCH_WARPS * 32, smem, st>>>(cv, tv, cd, sa, pair_counter, scanned, out, counters);
+    k_search<RowT, FP32><<<grid, SEARCH_WARPS * 32, smem, st>>>(cv, tv, cd, sa, pair_counter, scanned, out, counters,
+                                                                 dm);
     return cudaGetLastError();
 }
 
 cudaError_t launch_search(cudaStream_t st, int grid, bool wide, bool fp32, const ChunkView &cv,
                           const TemplateView &tv, const CandView &cd, const SearchArgs &sa, int32_t *pair_counter,
-                          const int32_t *scanned, const CompleteRows &out, unsigned long long *counters) {
+                          const int32_t *scanned, const CompleteRows &out, unsigned long long *counters,
+                          const LeafDemand &dm) {
     if (wide)
-        return fp32 ? search_variant<uint32_t, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters)
-                    : search_variant<uint32_t, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters);
-    return fp32 ? search_variant<uint16_t, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters)
-                : search_variant<uint16_t, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters);
+        return fp32 ? search_variant<uint32_t, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm)
+                    : search_variant<uint32_t, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters,
+                                                      dm);
+    return fp32 ? search_variant<uint16_t, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm)
+                : search_variant<uint16_t, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm);
 }
 
 void launch_superpose(cudaStream_t st, int blocks, const ChunkView &cv, const TemplateView &tv,

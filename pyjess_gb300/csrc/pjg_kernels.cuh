@@ -35,6 +35,30 @@ struct SearchArgs {
     uint64_t budget_ns;                // per-warp wall-time budget (globaltimer)
 };
 
+// A pair whose search stopped at a level whose candidate list had no kd
+// leaf order yet: it runs again from its beginning once the list is
+// ordered, skipping the `skip` complete rows it has already emitted (the
+// search is deterministic, so the replay emits the same rows in the same
+// order).
+struct Suspended {
+    int32_t pair;
+    int32_t pad;
+    int64_t skip;
+};
+
+// Lists put in kd leaf order on demand.  state[w] per list of the chunk:
+// 0 no leaf order, 1 requested (in `work`), 2 ordered.  state == nullptr:
+// every list is ordered.
+struct LeafDemand {
+    int32_t *state;
+    int64_t *work;                     // requested lists, appended
+    unsigned long long *n_work;
+    const Suspended *resume;           // pairs of this search round;
+    int32_t n_resume;                  //   nullptr: pairs 0 .. n_pairs-1
+    Suspended *suspended;              // pairs that stopped at an unordered
+    unsigned long long *n_suspended;   //   list in this round
+};
+
 // Complete assignments written by k_search.
 struct CompleteRows {
     unsigned long long *count;
@@ -91,11 +115,22 @@ void launch_scan_tiles_i32(cudaStream_t st, const int32_t *in, int64_t n, int64_
 void launch_scan_tiles_i64(cudaStream_t st, const int64_t *in, int64_t n, int64_t *out, int64_t *tile_sums);
 void launch_scan_add(cudaStream_t st, int64_t *out, int64_t n, const int64_t *tile_offsets);
 
+// kd leaf order of the lists in `work` (n_work entries, read on the device),
+// or of every list of the chunk when work == nullptr
 void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t n_sigs, const int32_t *count,
                        const int64_t *offset, const int64_t *blk_offset, const int32_t *cand_atom,
                        const float4 *cand_xyz, int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
                        int64_t *sorted_list, unsigned long long *sorted_count, int64_t list_cap,
-                       int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters);
+                       int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters,
+                       const int64_t *work, const unsigned long long *n_work);
+
+// requests (LeafDemand) the lists of levels 1 .. max_level of every pair
+// of the chunk that has no empty candidate list
+void launch_demand_levels(cudaStream_t st, int blocks, const TemplateView &tv, const CandView &cd, int32_t n_pairs,
+                          int32_t max_level, int32_t reorder, const LeafDemand &dm);
+
+// state[work[i]] = 2 for the n_work requested lists
+void launch_mark_ordered(cudaStream_t st, int blocks, const LeafDemand &dm);
 
 // per-structure axis ranks (lrank, urank: [3][n_atoms], structure-local
 // values); tile_key / tile_idx: scratch of 3 * n_atoms entries
@@ -110,7 +145,8 @@ void launch_block_counts(cudaStream_t st, int64_t n, const int32_t *count, int32
 // atoms), fp32 = guarded FP32 distance tests (else exact FP64 throughout)
 cudaError_t launch_search(cudaStream_t st, int grid, bool wide, bool fp32, const ChunkView &cv,
                           const TemplateView &tv, const CandView &cd, const SearchArgs &sa, int32_t *pair_counter,
-                          const int32_t *scanned, const CompleteRows &out, unsigned long long *counters);
+                          const int32_t *scanned, const CompleteRows &out, unsigned long long *counters,
+                          const LeafDemand &dm);
 
 void launch_superpose(cudaStream_t st, int blocks, const ChunkView &cv, const TemplateView &tv,
                       const CompleteRows &in, const RowResults &out);

@@ -296,3 +296,66 @@ def test_query_many_matches_query(t133, t412, amy, ayx):
         assert [tuple(a.serial for a in h.atoms(False)) for h in hits] == \
                [tuple(a.serial for a in h.atoms(False)) for h in single]
         assert [h.rmsd for h in hits] == [h.rmsd for h in single]
+
+
+# --- kd leaf order on demand ----------------------------------------------------
+#
+# PJG_LEAF_LEVELS sets how many levels' lists are put in leaf order before
+# the search; deeper lists are ordered when a pair first reaches them, the
+# pair being suspended and replayed (skipping the rows it already emitted).
+# Small values force many suspensions; -1 orders every list up front.
+
+
+@pytest.mark.parametrize("levels", [-1, 0, 1, 2])
+def test_leaf_order_on_demand_config3(monkeypatch, levels):
+    from pyjess_gb300 import workloads as W
+
+    monkeypatch.setenv("PJG_LEAF_LEVELS", str(levels))
+    wl = W.config(3, n_structures=30, n_templates=300)
+    res, ref = compare(wl.templates, wl.structures, mode="fp32", **wl.params)
+    st = res.stats()
+    if levels in (0, 1):
+        assert st["suspensions"] > 0 and st["search_rounds"] > 1
+    if levels == -1:
+        assert st["suspensions"] == 0 and st["search_rounds"] == st["chunks"]
+
+
+@pytest.mark.parametrize("levels", [0, 1])
+@pytest.mark.parametrize("best", [False, True])
+def test_leaf_order_on_demand_cut(monkeypatch, levels, best):
+    """max_candidates cut (applied inside the search in non-best mode) and
+    best_match across suspended and replayed pairs."""
+    from pyjess_gb300 import workloads as W
+
+    monkeypatch.setenv("PJG_LEAF_LEVELS", str(levels))
+    wl = W.config(4, n_structures=3, n_templates=6, residues=(300, 500))
+    p = dict(wl.params)
+    p["max_candidates"] = 50
+    compare(wl.templates, wl.structures, best_match=best, **p)
+
+
+@pytest.mark.parametrize("levels", [0, 1])
+@pytest.mark.parametrize("mode", MODES)
+def test_leaf_order_on_demand_golden(monkeypatch, t133, t412, amy, levels, mode):
+    from pyjess_gb300 import Jess
+    from pyjess_gb300._pack import pack_molecules
+
+    monkeypatch.setenv("PJG_LEAF_LEVELS", str(levels))
+    jess = Jess([t133, t412, t133])
+    compare(jess._packed_templates(), pack_molecules([amy]), mode=mode, rmsd_threshold=2,
+            distance_cutoff=4, max_dynamic_distance=4, reorder=False)
+
+
+def test_leaf_order_on_demand_orders_fewer_entries(monkeypatch):
+    from pyjess_gb300 import workloads as W
+
+    wl = W.config(3, n_structures=20, n_templates=1000)
+    monkeypatch.setenv("PJG_LEAF_LEVELS", "-1")
+    full = gpu_query(wl.templates, wl.structures, **wl.params)
+    monkeypatch.setenv("PJG_LEAF_LEVELS", "4")
+    lazy = gpu_query(wl.templates, wl.structures, **wl.params)
+    assert hit_keys(full.arrays()) == hit_keys(lazy.arrays())
+    fs, ls = full.stats(), lazy.stats()
+    assert ls["leaf_entries"] < fs["leaf_entries"]
+    for key in ("partials", "complete", "bytes_expansion", "fp64_rechecks"):
+        assert fs[key] == ls[key], key
