@@ -669,6 +669,9 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     DBuf<int64_t> d_work;
     DBuf<unsigned long long> d_nwork, d_nsusp;
     DBuf<Suspended> d_susp_a, d_susp_b;
+    DBuf<unsigned char> d_pool_a, d_pool_b;
+    DBuf<unsigned long long> d_pool_used;
+    int64_t pool_cap = 0;
     DBuf<double> d_c_rmsd;
     // per complete row, in reference order
     DBuf<double> d_r_rmsd, d_r_rot, d_r_cen;
@@ -878,6 +881,24 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 CUDA_TRY(dalloc(d_nsusp, 1, st));
                 CUDA_TRY(dalloc(d_susp_a, (size_t)n_pairs, st));
                 CUDA_TRY(dalloc(d_susp_b, (size_t)n_pairs, st));
+                if (pool_cap == 0) {
+                    // saved search states of suspended pairs, one pool per
+                    // round in turn: a sixteenth of the free memory each,
+                    // 64 MiB to 4 GiB (a pair that finds its pool full is
+                    // rerun from its start instead)
+                    size_t free_b = 0, total_b = 0;
+                    int64_t cap = 64ll << 20;
+                    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+                        cap = std::max<int64_t>(cap, std::min<int64_t>(4ll << 30, (int64_t)(free_b / 16)));
+                    const char *v = getenv("PJG_STATE_POOL");
+                    if (v && atoll(v) >= 0) cap = atoll(v);
+                    pool_cap = std::max<int64_t>(cap, 16);
+                    CUDA_TRY(dalloc(d_pool_a, (size_t)pool_cap, st));
+                    CUDA_TRY(dalloc(d_pool_b, (size_t)pool_cap, st));
+                    CUDA_TRY(dalloc(d_pool_used, 1, st));
+                }
+                dm.pool_used = d_pool_used.p;
+                dm.pool_cap = pool_cap;
                 CUDA_TRY(cudaMemsetAsync(d_lstate.p, 0, (size_t)Wc * sizeof(int32_t), st));
                 CUDA_TRY(cudaMemsetAsync(d_nwork.p, 0, sizeof(unsigned long long), st));
                 dm.state = d_lstate.p;
@@ -946,13 +967,17 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 // no pair is suspended
                 dm.resume = nullptr;
                 dm.n_resume = 0;
+                dm.pool_in = nullptr;
                 Suspended *next_out = d_susp_a.p, *spare = d_susp_b.p;
+                unsigned char *pool_next = d_pool_a.p, *pool_spare = d_pool_b.p;
                 for (int round = 0;; round++) {
                     CUDA_TRY(cudaMemsetAsync(d_pair_counter.p, 0, sizeof(int32_t), st));
                     if (dm.state) {
                         dm.suspended = next_out;
+                        dm.pool_out = pool_next;
                         CUDA_TRY(cudaMemsetAsync(d_nwork.p, 0, sizeof(unsigned long long), st));
                         CUDA_TRY(cudaMemsetAsync(d_nsusp.p, 0, sizeof(unsigned long long), st));
+                        CUDA_TRY(cudaMemsetAsync(d_pool_used.p, 0, sizeof(unsigned long long), st));
                     }
                     CUDA_TRY(cudaEventRecord(ev[6], st));
                     CUDA_TRY(launch_search(st, grid, wide, fp32, cv, tv, cd, sa, d_pair_counter.p, scn_c, cr,
@@ -980,7 +1005,9 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                     CUDA_TRY(order_requested());
                     dm.resume = next_out;
                     dm.n_resume = (int32_t)ns;
+                    dm.pool_in = pool_next;
                     std::swap(next_out, spare);
+                    std::swap(pool_next, pool_spare);
                 }
                 if ((int64_t)nc <= c_cap) break;
                 // the row buffer was too small: grow and run the chunk again
@@ -1123,7 +1150,7 @@ done:
         dfree(d_r_rmsd, st); dfree(d_r_rot, st); dfree(d_r_cen, st); dfree(d_r_nan, st); dfree(d_r_hit, st);
         dfree(d_r_warn, st); dfree(d_r_hatoms, st); dfree(d_r_src, st); dfree(d_r_hidx, st); dfree(d_r_widx, st);
         dfree(d_r_aidx, st); dfree(d_lstate, st); dfree(d_work, st); dfree(d_nwork, st); dfree(d_nsusp, st);
-        dfree(d_susp_a, st); dfree(d_susp_b, st);
+        dfree(d_susp_a, st); dfree(d_susp_b, st); dfree(d_pool_a, st); dfree(d_pool_b, st); dfree(d_pool_used, st);
         for (auto &b : scan_tmp) dfree(b, st);
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);

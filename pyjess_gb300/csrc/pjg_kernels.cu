@@ -1710,6 +1710,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
         if (item >= n_items || timed_out) break;
         const int pair = fresh ? item : dm.resume[item].pair;
         const int64_t skip = fresh ? 0 : dm.resume[item].skip;
+        const int64_t saved = fresh ? -1 : dm.resume[item].state;
         const int s = pair / T;
         const int t = pair % T;
         const int ab = tv.atom_begin[t];
@@ -1881,6 +1882,38 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
             int lev = -1;
             int chain_lev = -1, chain_par = -1;
             float box_lo[3], box_hi[3];
+            if (saved >= 0) {
+                // resume a suspended pair from its saved state
+                const unsigned char *b = dm.pool_in + saved;
+                const SavedPair h = *reinterpret_cast<const SavedPair *>(b);
+                root = h.root;
+                lev = h.lev;
+                emitted = h.emitted;
+                cut_base = h.cut_base;
+                if (lane == 0) rechecks = h.rechecks;
+                const int64_t hdr = (int64_t)sizeof(SavedPair) + 16LL * (lev + 1);
+                int4 c4 = make_int4(0, 0, 0, 0);
+                if (lane <= lev) {
+                    c4 = reinterpret_cast<const int4 *>(b + sizeof(SavedPair))[lane];
+                    st.F[lane] = c4.x;
+                    st.cnt[lane] = c4.y;
+                    st.par[lane] = c4.z;
+                    st.cnd[lane] = c4.w;
+                }
+                int tile_pre = c4.y;
+                for (int o = 1; o < 32; o <<= 1) {
+                    int v = __shfl_up_sync(FULL_MASK, tile_pre, o);
+                    if (lane >= o) tile_pre += v;
+                }
+                const E *srcb = reinterpret_cast<const E *>(b + hdr);
+                for (int j = 0; j <= lev; j++) {
+                    const int cj = __shfl_sync(FULL_MASK, c4.y, j);
+                    const int pj = __shfl_sync(FULL_MASK, tile_pre, j) - cj;
+                    E *dst = tiles + st.tile[j];
+                    for (int i = lane; i < cj; i += 32) dst[i] = srcb[pj + i];
+                }
+                __syncwarp();
+            }
             while (!stop) {
                 if (over_budget()) break;
                 if (lev < 0) {
@@ -1929,14 +1962,57 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32)
                 }
                 if (!((ready_mask >> child) & 1u)) {
                     // the child level's list has no kd leaf order yet:
-                    // request it and suspend the pair until the next round
+                    // request it and suspend the pair until the next round.
+                    // Its child tile and every deeper one are empty here, so
+                    // the state is the header, the cursors of levels 0..lev
+                    // and the used entries of their tiles.
+                    unsigned long long rs = rechecks;
+                    for (int o = 16; o; o >>= 1) rs += __shfl_xor_sync(FULL_MASK, rs, o);
+                    int used = lane <= lev ? st.cnt[lane] : 0;
+                    int tile_pre = used;  // inclusive prefix over levels
+                    for (int o = 1; o < 32; o <<= 1) {
+                        int v = __shfl_up_sync(FULL_MASK, tile_pre, o);
+                        if (lane >= o) tile_pre += v;
+                    }
+                    const int total = __shfl_sync(FULL_MASK, tile_pre, 31);
+                    const int64_t hdr = (int64_t)sizeof(SavedPair) + 16LL * (lev + 1);
+                    const int64_t bytes = (hdr + (int64_t)total * (int64_t)sizeof(E) + 15) & ~15LL;
+                    int64_t off = -1;
+                    if (lane == 0 && dm.pool_out) {
+                        unsigned long long o = atomicAdd(dm.pool_used, (unsigned long long)bytes);
+                        if ((int64_t)o + bytes <= dm.pool_cap) off = (int64_t)o;
+                    }
+                    off = __shfl_sync(FULL_MASK, off, 0);
+                    if (off >= 0) {
+                        unsigned char *b = dm.pool_out + off;
+                        if (lane == 0) {
+                            SavedPair h;
+                            h.root = root;
+                            h.lev = lev;
+                            h.emitted = emitted;
+                            h.cut_base = cut_base;
+                            h.rechecks = rs;
+                            *reinterpret_cast<SavedPair *>(b) = h;
+                        }
+                        if (lane <= lev)
+                            reinterpret_cast<int4 *>(b + sizeof(SavedPair))[lane] =
+                                make_int4(st.F[lane], st.cnt[lane], st.par[lane], st.cnd[lane]);
+                        E *dst = reinterpret_cast<E *>(b + hdr);
+                        for (int j = 0; j <= lev; j++) {
+                            const int cj = __shfl_sync(FULL_MASK, used, j);
+                            const int pj = __shfl_sync(FULL_MASK, tile_pre, j) - cj;
+                            const E *src = tiles + st.tile[j];
+                            for (int i = lane; i < cj; i += 32) dst[pj + i] = src[i];
+                        }
+                    }
                     if (lane == 0) {
                         const int64_t w = (int64_t)s * G + tv.sig[ab + st.order[child]];
                         if (atomicCAS(&dm.state[w], 0, 1) == 0) dm.work[atomicAdd(dm.n_work, 1ull)] = w;
                         Suspended sp;
                         sp.pair = pair;
                         sp.pad = 0;
-                        sp.skip = emitted > skip ? emitted : skip;
+                        sp.skip = off >= 0 ? 0 : (emitted > skip ? emitted : skip);
+                        sp.state = off;
                         dm.suspended[atomicAdd(dm.n_suspended, 1ull)] = sp;
                     }
                     suspended = true;

@@ -36,14 +36,28 @@ struct SearchArgs {
 };
 
 // A pair whose search stopped at a level whose candidate list had no kd
-// leaf order yet: it runs again from its beginning once the list is
-// ordered, skipping the `skip` complete rows it has already emitted (the
+// leaf order yet.  Once the list is ordered the pair resumes from its saved
+// search state (`state` >= 0: byte offset into the state pool of the round
+// that suspended it) or, when the pool was full, runs again from its
+// beginning, skipping the `skip` complete rows it has already emitted (the
 // search is deterministic, so the replay emits the same rows in the same
 // order).
 struct Suspended {
     int32_t pair;
     int32_t pad;
     int64_t skip;
+    int64_t state;
+};
+
+// Saved search state of a suspended pair (16-byte aligned in the pool):
+// this header, then per level 0..lev an int4 (F, cnt, par, cnd), then the
+// used entries of those levels' tiles.
+struct SavedPair {
+    int32_t root;
+    int32_t lev;
+    int64_t emitted;
+    int64_t cut_base;
+    unsigned long long rechecks;
 };
 
 // Lists put in kd leaf order on demand.  state[w] per list of the chunk:
@@ -57,6 +71,10 @@ struct LeafDemand {
     int32_t n_resume;                  //   nullptr: pairs 0 .. n_pairs-1
     Suspended *suspended;              // pairs that stopped at an unordered
     unsigned long long *n_suspended;   //   list in this round
+    unsigned char *pool_out;           // states saved in this round
+    unsigned long long *pool_used;     //   (bytes taken; may pass pool_cap)
+    int64_t pool_cap;
+    const unsigned char *pool_in;      // states of the pairs of this round
 };
 
 // Complete assignments written by k_search.

@@ -302,15 +302,28 @@ def test_query_many_matches_query(t133, t412, amy, ayx):
 #
 # PJG_LEAF_LEVELS sets how many levels' lists are put in leaf order before
 # the search; deeper lists are ordered when a pair first reaches them, the
-# pair being suspended and replayed (skipping the rows it already emitted).
-# Small values force many suspensions; -1 orders every list up front.
+# pair being suspended and resumed from its saved search state, or, when the
+# state pool is full (PJG_STATE_POOL=0 forces it), replayed from its start
+# skipping the rows it already emitted.  Small values force many
+# suspensions; -1 orders every list up front.
+
+POOLS = [None, "0"]
 
 
+def set_pool(monkeypatch, pool):
+    if pool is None:
+        monkeypatch.delenv("PJG_STATE_POOL", raising=False)
+    else:
+        monkeypatch.setenv("PJG_STATE_POOL", pool)
+
+
+@pytest.mark.parametrize("pool", POOLS)
 @pytest.mark.parametrize("levels", [-1, 0, 1, 2])
-def test_leaf_order_on_demand_config3(monkeypatch, levels):
+def test_leaf_order_on_demand_config3(monkeypatch, levels, pool):
     from pyjess_gb300 import workloads as W
 
     monkeypatch.setenv("PJG_LEAF_LEVELS", str(levels))
+    set_pool(monkeypatch, pool)
     wl = W.config(3, n_structures=30, n_templates=300)
     res, ref = compare(wl.templates, wl.structures, mode="fp32", **wl.params)
     st = res.stats()
@@ -320,27 +333,31 @@ def test_leaf_order_on_demand_config3(monkeypatch, levels):
         assert st["suspensions"] == 0 and st["search_rounds"] == st["chunks"]
 
 
+@pytest.mark.parametrize("pool", POOLS)
 @pytest.mark.parametrize("levels", [0, 1])
 @pytest.mark.parametrize("best", [False, True])
-def test_leaf_order_on_demand_cut(monkeypatch, levels, best):
+def test_leaf_order_on_demand_cut(monkeypatch, levels, best, pool):
     """max_candidates cut (applied inside the search in non-best mode) and
-    best_match across suspended and replayed pairs."""
+    best_match across suspended and resumed (or replayed) pairs."""
     from pyjess_gb300 import workloads as W
 
     monkeypatch.setenv("PJG_LEAF_LEVELS", str(levels))
+    set_pool(monkeypatch, pool)
     wl = W.config(4, n_structures=3, n_templates=6, residues=(300, 500))
     p = dict(wl.params)
     p["max_candidates"] = 50
     compare(wl.templates, wl.structures, best_match=best, **p)
 
 
+@pytest.mark.parametrize("pool", POOLS)
 @pytest.mark.parametrize("levels", [0, 1])
 @pytest.mark.parametrize("mode", MODES)
-def test_leaf_order_on_demand_golden(monkeypatch, t133, t412, amy, levels, mode):
+def test_leaf_order_on_demand_golden(monkeypatch, t133, t412, amy, levels, mode, pool):
     from pyjess_gb300 import Jess
     from pyjess_gb300._pack import pack_molecules
 
     monkeypatch.setenv("PJG_LEAF_LEVELS", str(levels))
+    set_pool(monkeypatch, pool)
     jess = Jess([t133, t412, t133])
     compare(jess._packed_templates(), pack_molecules([amy]), mode=mode, rmsd_threshold=2,
             distance_cutoff=4, max_dynamic_distance=4, reorder=False)
