@@ -126,6 +126,55 @@ __device__ __forceinline__ bool sig_match(const SigView &sv, int g, int rule, ui
     return false;
 }
 
+// A signature's rule with up to four of its names held in registers (read
+// once per list instead of once per scanned atom).
+struct SigRegs {
+    int g, rule, n0, n1, mainchain;
+    uint32_t nm[4];
+};
+
+__device__ __forceinline__ SigRegs load_sig(const SigView &sv, int g) {
+    SigRegs r;
+    r.g = g;
+    r.rule = sv.rule[g];
+    r.n0 = sv.name_begin[g];
+    r.n1 = sv.name_begin[g + 1];
+    r.mainchain = sv.mainchain[g];
+    for (int i = 0; i < 4; i++) r.nm[i] = r.n0 + i < r.n1 ? sv.names[r.n0 + i] : 0u;
+    return r;
+}
+
+__device__ __forceinline__ bool sig_match_regs(const SigView &sv, const SigRegs &r, uint32_t name,
+                                               uint32_t resname) {
+    const int nn = r.n1 - r.n0;
+    if (nn > 4) return sig_match(sv, r.g, r.rule, name, resname);
+    switch (r.rule) {
+    case RULE_ANY:
+        return true;
+    case RULE_NAME:
+    case RULE_NAME_OR_PARTNER:
+    case RULE_NAME_OR_MAINCHAIN: {
+        bool hit = false;
+#pragma unroll
+        for (int i = 0; i < 4; i++) hit |= i < nn && r.nm[i] == name;
+        if (hit) return true;
+        if (r.rule == RULE_NAME_OR_MAINCHAIN) return r.mainchain && is_mainchain(name);
+        if (r.rule == RULE_NAME_OR_PARTNER) {
+            for (int i = sv.partner_begin[r.g]; i < sv.partner_begin[r.g + 1]; i++)
+                if (sv.partner_res[i] == resname && sv.partner_name[i] == name) return true;
+        }
+        return false;
+    }
+    case RULE_ELEMENT: {
+        bool hit = false;
+#pragma unroll
+        for (int i = 0; i < 4; i++) hit |= i < nn && (r.nm[i] & 0xFFFFu) == (name & 0xFFFFu);
+        return hit;
+    }
+    }
+    return false;
+}
+
 // One warp per (structure, signature).  FILL=false: lengths and scanned
 // counts; FILL=true: write the list in candidate order.
 template <bool FILL>
@@ -139,12 +188,14 @@ __global__ void k_candidates(ChunkView cv, SigView sv, int32_t *count, int32_t *
         int s = (int)(w / sv.n_sigs);
         int g = (int)(w % sv.n_sigs);
         int code = sv.code[g];
-        int rule = sv.rule[g];
+        const SigRegs sr = load_sig(sv, g);
         int64_t abase = cv.atom_base[s];
         int nat = cv.atom_count[s];
         int cnt = 0, sc = 0;
         int64_t out0 = FILL ? offset[w] : 0;
-        auto visit = [&](int p_lo, int p_hi, bool via_sorted) {
+        // atoms p_lo..p_hi of the residue bucket `rn` (via_sorted) or of
+        // the molecule in order
+        auto visit = [&](int p_lo, int p_hi, bool via_sorted, uint32_t rn) {
             for (int p0 = p_lo; p0 < p_hi; p0 += 32) {
                 int p = p0 + lane;
                 bool valid = p < p_hi;
@@ -152,7 +203,8 @@ __global__ void k_candidates(ChunkView cv, SigView sv, int32_t *count, int32_t *
                 int atom = 0;
                 if (valid) {
                     atom = via_sorted ? cv.sorted[abase + p] : p;
-                    ok = sig_match(sv, g, rule, cv.name[abase + atom], cv.resname[abase + atom]);
+                    const uint32_t res = via_sorted ? rn : cv.resname[abase + atom];
+                    ok = sig_match_regs(sv, sr, cv.name[abase + atom], res);
                 }
                 unsigned m = __ballot_sync(FULL_MASK, ok);
                 if (FILL && ok) {
@@ -161,8 +213,8 @@ __global__ void k_candidates(ChunkView cv, SigView sv, int32_t *count, int32_t *
                     cand_xyz[out0 + pos] = cv.xyz32[abase + atom];
                 }
                 cnt += __popc(m);
-                sc += min(32, p_hi - p0);
             }
+            sc += p_hi - p_lo;
         };
         if (code >= -1 && code <= 8) {
             int b0 = cv.bucket_begin[s], b1 = cv.bucket_begin[s + 1];
@@ -178,10 +230,10 @@ __global__ void k_candidates(ChunkView cv, SigView sv, int32_t *count, int32_t *
                     }
                 }
                 if (found < 0) continue;
-                visit(cv.bucket_lo[found], cv.bucket_hi[found], true);
+                visit(cv.bucket_lo[found], cv.bucket_hi[found], true, rn);
             }
         } else {
-            visit(0, nat, false);
+            visit(0, nat, false, 0u);
         }
         if (!FILL && lane == 0) {
             count[w] = cnt;
@@ -1667,7 +1719,7 @@ __device__ __noinline__ bool decide_fp64(unsigned exact_mask, int lev, const int
 }
 
 template <typename PosT, bool FP32>
-__global__ void __launch_bounds__(SEARCH_WARPS * 32)
+__global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
     k_search(ChunkView cv, TemplateView tv, CandView cd, SearchArgs sa, int32_t *pair_counter,
              const int32_t *scanned, CompleteRows out, unsigned long long *counters, LeafDemand dm) {
     extern __shared__ __align__(16) unsigned char smem[];

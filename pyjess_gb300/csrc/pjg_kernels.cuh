@@ -15,6 +15,10 @@ namespace pjg {
 #endif
 
 constexpr int SEARCH_WARPS = 8;        // warps per block of k_search
+// resident k_search blocks per SM the register allocation is sized for
+#ifndef PJG_SEARCH_MIN_BLOCKS
+#define PJG_SEARCH_MIN_BLOCKS 2
+#endif
 constexpr int LEAF_WARPS = 4;          // warps per block of k_leaf_order
 constexpr int LEAF_FAST_MAX = 192;     // capacity of the rank method's buffers
 constexpr int LEAF_RANK_MAX = 192;     // default: longest list ordered by the rank method
