@@ -660,7 +660,10 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     DBuf<int64_t> d_exact_list, d_sorted_list;
     DBuf<unsigned long long> d_exact_count, d_sorted_count;
     DBuf<float4> d_blk_lo, d_blk_hi;
-    DBuf<float4> d_cand_xyz, d_leaf_xyz;
+    DBuf<float4> d_leaf_xyz, d_leaf_xyz2;
+    DBuf<int32_t> d_leaf_atom2;
+    DBuf<int64_t> d_leaf_off;
+    DBuf<unsigned long long> d_leaf_used;
     DBuf<unsigned long long> d_counters, d_ccount, d_rtotals;
     DBuf<int32_t> d_c_pair, d_c_atoms, d_pair_rows, d_cnt_q;
     DBuf<int64_t> d_c_ord, d_off_q;
@@ -692,7 +695,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     // per-structure path orders every list up front: with one structure a
     // chunk, the host round trip of each extra search round costs more
     // than the ordering it saves.
-    int demand_levels = P->mode == PJG_MODE_PLAIN_FP64 ? -1 : 5;
+    int demand_levels = P->mode == PJG_MODE_PLAIN_FP64 ? -1 : 4;
     {
         const char *v = getenv("PJG_LEAF_LEVELS");
         if (v && *v) demand_levels = atoi(v);
@@ -765,7 +768,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
         SigView sv{G, tp->d_code, tp->d_rule, tp->d_mainchain, tp->d_name_begin, tp->d_names, tp->d_res_begin,
                    tp->d_resnames, tp->d_partner_begin, tp->d_partner_res, tp->d_partner_name};
         int blocks = (int)std::min<int64_t>((W + 7) / 8, (int64_t)sm_count() * 32);
-        launch_candidates(st, std::max(blocks, 1), false, cv, sv, d_count.p, d_scanned.p, nullptr, nullptr, nullptr);
+        launch_candidates(st, std::max(blocks, 1), false, cv, sv, d_count.p, d_scanned.p, nullptr, nullptr);
         k_struct_totals<<<std::max(1, std::min(S, sm_count() * 8)), 256, 0, st>>>(S, G, d_count.p, d_totals.p);
         launches += 2;
         CUDA_TRY(cudaGetLastError());
@@ -774,17 +777,30 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     }
 
     {
-        // chunks of structures under an entry budget
-        // entries per chunk: candidate lists cost ~42 B an entry (atom and
-        // FP32 point, candidate and leaf order, block boxes); a third of the
-        // free device memory, at least 48M and at most 2G entries.  Fewer,
-        // larger chunks leave fewer kernel tails (a launch waits for its
-        // heaviest list or pair).  PJG_ENTRY_BUDGET overrides it.
+        // chunks of structures under an entry budget.  A candidate entry
+        // costs at most ~26 B: its atom in candidate order (4), block boxes
+        // (~1), per-list arrays (~1) and, once its list is put in leaf order,
+        // its atom and FP32 point in leaf order (20; allocated as lists are
+        // requested).  The budget takes 60% of the free device memory
+        // (counting memory the stream-ordered pool holds unused) at that
+        // worst case, at least 48M entries, which leaves room for growing
+        // the leaf arrays (old and new copies live at once while they grow).  Fewer, larger chunks leave fewer
+        // kernel tails and search rounds.  PJG_ENTRY_BUDGET overrides it.
         int64_t ENTRY_BUDGET = 48ll << 20;
         {
             size_t free_b = 0, total_b = 0;
-            if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
-                ENTRY_BUDGET = std::max<int64_t>(ENTRY_BUDGET, std::min<int64_t>(2ll << 30, (int64_t)(free_b / 3 / 42)));
+            if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+                cudaMemPool_t pool;
+                if (cudaDeviceGetDefaultMemPool(&pool, res->device) == cudaSuccess) {
+                    uint64_t reserved = 0, used = 0;
+                    if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess &&
+                        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess &&
+                        reserved > used)
+                        free_b += (size_t)(reserved - used);
+                }
+                cudaGetLastError();
+                ENTRY_BUDGET = std::max<int64_t>(ENTRY_BUDGET, (int64_t)((double)free_b * 0.6 / 26.0));
+            }
             const char *v = getenv("PJG_ENTRY_BUDGET");
             if (v && atoll(v) > 0) ENTRY_BUDGET = atoll(v);
         }
@@ -834,13 +850,24 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             CUDA_TRY(dalloc(d_blk_lo, (size_t)std::max<int64_t>(nblocks, 1), st));
             CUDA_TRY(dalloc(d_blk_hi, (size_t)std::max<int64_t>(nblocks, 1), st));
             CUDA_TRY(dalloc(d_cand_atom, (size_t)entries, st));
-            CUDA_TRY(dalloc(d_leaf_atom, (size_t)entries, st));
-            CUDA_TRY(dalloc(d_cand_xyz, (size_t)entries, st));
-            CUDA_TRY(dalloc(d_leaf_xyz, (size_t)entries, st));
+            // leaf-order arrays: every entry when every list is ordered up
+            // front, else half of them to start with (grown on demand;
+            // PJG_LEAF_CAPACITY sets the starting size)
+            {
+                int64_t cap0 = demand_levels < 0 ? entries : std::max<int64_t>(entries / 2, 1 << 20);
+                const char *v = getenv("PJG_LEAF_CAPACITY");
+                if (demand_levels >= 0 && v && atoll(v) > 0) {
+                    cap0 = atoll(v);
+                    dfree(d_leaf_atom, st);
+                    dfree(d_leaf_xyz, st);
+                }
+                CUDA_TRY(dalloc(d_leaf_atom, (size_t)cap0, st));
+            }
+            CUDA_TRY(dalloc(d_leaf_xyz, d_leaf_atom.n, st));
+            int64_t leaf_filled = 0;  // leaf entries of the lists ordered so far
             {
                 int blocks = (int)std::min<int64_t>((Wc + 7) / 8, (int64_t)sm_count() * 32);
-                launch_candidates(st, std::max(blocks, 1), true, cv, sv, nullptr, nullptr, d_offset.p, d_cand_atom.p,
-                                  d_cand_xyz.p);
+                launch_candidates(st, std::max(blocks, 1), true, cv, sv, nullptr, nullptr, d_offset.p, d_cand_atom.p);
                 CUDA_TRY(dalloc(d_exact_list, (size_t)Wc, st));
                 CUDA_TRY(dalloc(d_exact_count, 1, st));
                 CUDA_TRY(dalloc(d_sorted_list, 3 * (size_t)Wc, st));
@@ -850,7 +877,9 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             }
             TemplateView tv{T, tp->nmax, tp->d_atom_begin, tp->d_sig, tp->d_pos, tp->d_key, tp->d_param_begin,
                             d_params.p};
-            CandView cd{G, cnt_c, d_offset.p, d_cand_atom.p, d_cand_xyz.p, d_leaf_atom.p, d_leaf_xyz.p,
+            if (demand_levels >= 0) CUDA_TRY(dalloc(d_leaf_off, (size_t)Wc, st));
+            const int64_t *leaf_off = demand_levels < 0 ? d_offset.p : d_leaf_off.p;
+            CandView cd{G, cnt_c, d_offset.p, d_cand_atom.p, leaf_off, d_leaf_atom.p, d_leaf_xyz.p,
                         d_boff.p, d_blk_lo.p, d_blk_hi.p};
             const int64_t n_pairs = (int64_t)Sc * T;
             // kd leaf order: up front for the lists of the first
@@ -860,8 +889,32 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             LeafDemand dm{};
             const int leaf_blocks =
                 std::max(1, (int)std::min<int64_t>((Wc + LEAF_WARPS - 1) / LEAF_WARPS, (int64_t)sm_count() * 32));
+            // room in the leaf arrays for `need` entries (the lists ordered so
+            // far keep their places)
+            auto ensure_leaf = [&](int64_t need) -> cudaError_t {
+                if (need <= (int64_t)d_leaf_atom.n) return cudaSuccess;
+                const size_t cap2 = (size_t)std::max<int64_t>(need + need / 4, (int64_t)d_leaf_atom.n * 3 / 2);
+                cudaError_t e = dalloc(d_leaf_atom2, cap2, st);
+                if (e == cudaSuccess) e = dalloc(d_leaf_xyz2, cap2, st);
+                if (e != cudaSuccess) return e;
+                if (leaf_filled > 0) {
+                    e = cudaMemcpyAsync(d_leaf_atom2.p, d_leaf_atom.p, (size_t)leaf_filled * sizeof(int32_t),
+                                        cudaMemcpyDeviceToDevice, st);
+                    if (e == cudaSuccess)
+                        e = cudaMemcpyAsync(d_leaf_xyz2.p, d_leaf_xyz.p, (size_t)leaf_filled * sizeof(float4),
+                                            cudaMemcpyDeviceToDevice, st);
+                    if (e != cudaSuccess) return e;
+                }
+                std::swap(d_leaf_atom, d_leaf_atom2);
+                std::swap(d_leaf_xyz, d_leaf_xyz2);
+                dfree(d_leaf_atom2, st);
+                dfree(d_leaf_xyz2, st);
+                cd.leaf_atom = d_leaf_atom.p;
+                cd.leaf_xyz = d_leaf_xyz.p;
+                return cudaSuccess;
+            };
             auto order_requested = [&]() -> cudaError_t {
-                launch_leaf_order(st, leaf_blocks, cv, G, cnt_c, d_offset.p, d_boff.p, d_cand_atom.p, d_cand_xyz.p,
+                launch_leaf_order(st, leaf_blocks, cv, G, cnt_c, d_offset.p, d_boff.p, d_cand_atom.p, leaf_off,
                                   d_leaf_atom.p, d_leaf_xyz.p, d_blk_lo.p, d_blk_hi.p, d_sorted_list.p,
                                   d_sorted_count.p, Wc, d_exact_list.p, d_exact_count.p, d_counters.p, dm.work,
                                   dm.n_work);
@@ -905,13 +958,22 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 dm.work = d_work.p;
                 dm.n_work = d_nwork.p;
                 dm.n_suspended = d_nsusp.p;
+                CUDA_TRY(dalloc(d_leaf_used, 1, st));
+                CUDA_TRY(cudaMemsetAsync(d_leaf_used.p, 0, sizeof(unsigned long long), st));
+                dm.leaf_offset = d_leaf_off.p;
+                dm.leaf_used = d_leaf_used.p;
                 if (n_pairs > INT32_MAX) {
                     status = fail(PJG_ERR_CAPACITY, "too many pairs in one chunk");
                     goto done;
                 }
                 launch_demand_levels(st, sm_count() * 16, tv, cd, (int32_t)n_pairs, demand_levels, P->reorder, dm);
                 launches++;
+                unsigned long long used = 0;
+                CUDA_TRY(cudaMemcpyAsync(&used, d_leaf_used.p, sizeof used, cudaMemcpyDeviceToHost, st));
+                CUDA_TRY(cudaStreamSynchronize(st));
+                CUDA_TRY(ensure_leaf((int64_t)used));
                 CUDA_TRY(order_requested());
+                leaf_filled = (int64_t)used;
             }
             CUDA_TRY(cudaEventRecord(ev[2], st));
             SearchArgs sa;
@@ -985,9 +1047,12 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                     CUDA_TRY(cudaEventRecord(ev[7], st));
                     launches++;
                     CUDA_TRY(cudaGetLastError());
-                    unsigned long long ns = 0;
+                    unsigned long long ns = 0, used = 0;
                     CUDA_TRY(cudaMemcpyAsync(&nc, d_ccount.p, sizeof nc, cudaMemcpyDeviceToHost, st));
-                    if (dm.state) CUDA_TRY(cudaMemcpyAsync(&ns, d_nsusp.p, sizeof ns, cudaMemcpyDeviceToHost, st));
+                    if (dm.state) {
+                        CUDA_TRY(cudaMemcpyAsync(&ns, d_nsusp.p, sizeof ns, cudaMemcpyDeviceToHost, st));
+                        CUDA_TRY(cudaMemcpyAsync(&used, d_leaf_used.p, sizeof used, cudaMemcpyDeviceToHost, st));
+                    }
                     CUDA_TRY(cudaStreamSynchronize(st));
                     {
                         float m = 0.f;
@@ -1002,7 +1067,9 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                     }
                     suspensions += (int64_t)ns;
                     // the lists the suspended pairs reached, then those pairs
+                    CUDA_TRY(ensure_leaf((int64_t)used));
                     CUDA_TRY(order_requested());
+                    leaf_filled = (int64_t)used;
                     dm.resume = next_out;
                     dm.n_resume = (int32_t)ns;
                     dm.pool_in = pool_next;
@@ -1142,7 +1209,8 @@ done:
     if (st) {
         dfree(d_params, st); dfree(d_count, st); dfree(d_scanned, st); dfree(d_cand_atom, st);
         dfree(d_leaf_atom, st); dfree(d_pair_counter, st); dfree(d_offset, st); dfree(d_totals, st);
-        dfree(d_cand_xyz, st); dfree(d_leaf_xyz, st); dfree(d_counters, st); dfree(d_ccount, st);
+        dfree(d_leaf_xyz, st); dfree(d_leaf_atom2, st); dfree(d_leaf_xyz2, st); dfree(d_leaf_off, st);
+        dfree(d_leaf_used, st); dfree(d_counters, st); dfree(d_ccount, st);
         dfree(d_rtotals, st); dfree(d_c_pair, st); dfree(d_c_atoms, st); dfree(d_pair_rows, st);
         dfree(d_cnt_q, st); dfree(d_c_ord, st); dfree(d_off_q, st); dfree(d_c_rmsd, st); dfree(d_boff, st);
         dfree(d_nblk, st); dfree(d_blk_lo, st); dfree(d_blk_hi, st); dfree(d_exact_list, st);

@@ -13,10 +13,11 @@
 //                 per template: n x n distance matrix (FP64)
 //                 per query: n x n annulus parameters (FP64 + FP32 bounds)
 //   candidate lists, per (structure, signature) of a structure chunk:
-//                 cand order : i32 atom + float4 (level-0 seeds)
+//                 cand order : i32 atom (level-0 seeds; points from xyz32)
 //                 leaf order : i32 atom + float4 (levels >= 1), the order
 //                              in which the reference's kd-tree DFS reports
-//                              accepted leaves
+//                              accepted leaves; only for the lists put in
+//                              leaf order, packed in request order
 #pragma once
 
 #include <cstdint>
@@ -100,11 +101,11 @@ struct TemplateView {
 struct CandView {
     int32_t n_sigs;                 // lists are indexed [s * n_sigs + g]
     const int32_t *count;           // |C|
-    const int64_t *offset;          // start in the entry arrays
+    const int64_t *offset;          // start in cand_atom
     const int32_t *cand_atom;       // structure-local atom, candidate order
-    const float4 *cand_xyz;
+    const int64_t *leaf_offset;     // start in the leaf arrays (ordered lists)
     const int32_t *leaf_atom;       // structure-local atom, kd leaf order
-    const float4 *leaf_xyz;
+    const float4 *leaf_xyz;         // its FP32 point (xyz32)
     const int64_t *blk_offset;      // first block of the list
     const float4 *blk_lo;           // bounding box of each block of 32
     const float4 *blk_hi;           //   consecutive leaves (FP32)

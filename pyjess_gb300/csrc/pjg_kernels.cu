@@ -179,7 +179,7 @@ __device__ __forceinline__ bool sig_match_regs(const SigView &sv, const SigRegs 
 // counts; FILL=true: write the list in candidate order.
 template <bool FILL>
 __global__ void k_candidates(ChunkView cv, SigView sv, int32_t *count, int32_t *scanned,
-                             const int64_t *offset, int32_t *cand_atom, float4 *cand_xyz) {
+                             const int64_t *offset, int32_t *cand_atom) {
     int lane = lane_id();
     int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -210,7 +210,6 @@ __global__ void k_candidates(ChunkView cv, SigView sv, int32_t *count, int32_t *
                 if (FILL && ok) {
                     int pos = cnt + __popc(m & ((1u << lane) - 1u));
                     cand_atom[out0 + pos] = atom;
-                    cand_xyz[out0 + pos] = cv.xyz32[abase + atom];
                 }
                 cnt += __popc(m);
             }
@@ -438,16 +437,16 @@ __device__ void write_boxes(int m, int64_t o, const float4 *leaf_xyz, int64_t bo
 
 // Leaf order of a list from its partitioned candidate array `order`
 // (read backwards: the right subtree is visited first), plus its block boxes.
-__device__ void write_leaves(const uint16_t *order, int m, int64_t o, const int32_t *ca, const float4 *cand_xyz,
+__device__ void write_leaves(const uint16_t *order, int m, int64_t lo, const int32_t *ca, const float4 *pts,
                              int32_t *leaf_atom, float4 *leaf_xyz, int64_t bo, float4 *blk_lo, float4 *blk_hi) {
     const int lane = lane_id();
     for (int r = lane; r < m; r += 32) {
         int e = order[m - 1 - r];
-        leaf_atom[o + r] = ca[e];
-        leaf_xyz[o + r] = cand_xyz[o + e];
+        leaf_atom[lo + r] = ca[e];
+        leaf_xyz[lo + r] = pts[ca[e]];
     }
     __syncwarp();
-    write_boxes(m, o, leaf_xyz, bo, blk_lo, blk_hi);
+    write_boxes(m, lo, leaf_xyz, bo, blk_lo, blk_hi);
 }
 
 // Short lists (at most rank_max entries) without a tie: rank method (each
@@ -455,7 +454,7 @@ __device__ void write_leaves(const uint16_t *order, int m, int64_t o, const int3
 // to LEAF_SORTED_MAX entries), the rest to k_leaf_exact's.
 __global__ void __launch_bounds__(LEAF_WARPS * 32)
     k_leaf_order(ChunkView cv, int32_t n_sigs, const int32_t *count, const int64_t *offset,
-                 const int64_t *blk_offset, const int32_t *cand_atom, const float4 *cand_xyz,
+                 const int64_t *blk_offset, const int32_t *cand_atom, const int64_t *leaf_offset,
                  int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi, int64_t *sorted_list,
                  unsigned long long *sorted_count, int64_t list_cap, int64_t *exact_list,
                  unsigned long long *exact_count, unsigned long long *counters, int rank_max,
@@ -553,7 +552,8 @@ __global__ void __launch_bounds__(LEAF_WARPS * 32)
             __syncwarp();
             continue;
         }
-        write_leaves(L.ord[src], m, o, cand_atom + o, cand_xyz, leaf_atom, leaf_xyz, blk_offset[w], blk_lo, blk_hi);
+        write_leaves(L.ord[src], m, leaf_offset[w], cand_atom + o, cv.xyz32 + cv.atom_base[w / n_sigs], leaf_atom,
+                     leaf_xyz, blk_offset[w], blk_lo, blk_hi);
     }
     if (lane == 0 && n_exact) atomicAdd(&counters[C_LEAF_EXACT], n_exact);
     if (lane == 0 && n_sorted) atomicAdd(&counters[C_LEAF_SORTED], n_sorted);
@@ -721,7 +721,7 @@ __device__ void lane_qselect(uint16_t *A, double *Kb, int n, int k) {
 // at or below it are left to the smaller instantiation
 template <int MAXN, int MINN>
 __global__ void k_leaf_exact(ChunkView cv, int32_t n_sigs, const int32_t *count, const int64_t *offset,
-                             const int64_t *blk_offset, const int32_t *cand_atom, const float4 *cand_xyz,
+                             const int64_t *blk_offset, const int32_t *cand_atom, const int64_t *leaf_offset,
                              int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
                              const int64_t *exact_list, const unsigned long long *exact_count,
                              unsigned long long *counters) {
@@ -745,14 +745,16 @@ __global__ void k_leaf_exact(ChunkView cv, int32_t n_sigs, const int32_t *count,
         if (m <= MINN || (m > MAXN && MAXN != EXACT_MAX)) continue;
         const int s = (int)(w / n_sigs);
         const int64_t o = offset[w];
+        const int64_t lo = leaf_offset[w];
         const int32_t *ca = cand_atom + o;
         const double *xyz = cv.xyz64 + 3 * cv.atom_base[s];
+        const float4 *pts = cv.xyz32 + cv.atom_base[s];
         if (m > MAXN) {
             // sequential replay on one lane, global scratch
-            int32_t *perm = leaf_atom + o;
+            int32_t *perm = leaf_atom + lo;
             if (lane == 0) kd_exact(perm, m, ca, xyz);
             __syncwarp();
-            for (int r = lane; r < m; r += 32) leaf_xyz[o + r] = cand_xyz[o + perm[m - 1 - r]];
+            for (int r = lane; r < m; r += 32) leaf_xyz[lo + r] = pts[ca[perm[m - 1 - r]]];
             __syncwarp();
             for (int r = lane; r < m / 2; r += 32) {
                 int32_t x = perm[r], y = perm[m - 1 - r];
@@ -847,12 +849,12 @@ __global__ void k_leaf_exact(ChunkView cv, int32_t n_sigs, const int32_t *count,
             if (n_small > 256 && lane == 0) atomicMax(&counters[C_ERROR], 4ull);
             for (int r = lane; r < m; r += 32) {
                 int e = S.A[m - 1 - r];
-                leaf_atom[o + r] = ca[e];
-                leaf_xyz[o + r] = cand_xyz[o + e];
+                leaf_atom[lo + r] = ca[e];
+                leaf_xyz[lo + r] = pts[ca[e]];
             }
         }
         __syncwarp();
-        write_boxes(m, o, leaf_xyz, blk_offset[w], blk_lo, blk_hi);
+        write_boxes(m, lo, leaf_xyz, blk_offset[w], blk_lo, blk_hi);
     }
 }
 
@@ -1042,7 +1044,7 @@ __device__ void warp_qselect(uint16_t *A, const uint16_t *K, uint16_t *X, uint16
 template <int M, int MINN, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32, 1)
     k_leaf_sorted(ChunkView cv, int32_t n_sigs, const int32_t *count, const int64_t *offset,
-                  const int64_t *blk_offset, const int32_t *cand_atom, const float4 *cand_xyz, int32_t *leaf_atom,
+                  const int64_t *blk_offset, const int32_t *cand_atom, const int64_t *leaf_offset, int32_t *leaf_atom,
                   float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi, const int64_t *sorted_list,
                   const unsigned long long *sorted_count, int64_t *exact_list, unsigned long long *exact_count,
                   unsigned long long *counters) {
@@ -1296,10 +1298,20 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
             __syncwarp();
             continue;
         }
-        write_leaves(L.buf[cur0], m, o, ca, cand_xyz, leaf_atom, leaf_xyz, blk_offset[w], blk_lo, blk_hi);
+        write_leaves(L.buf[cur0], m, leaf_offset[w], ca, cv.xyz32 + gbase, leaf_atom, leaf_xyz, blk_offset[w], blk_lo,
+                     blk_hi);
     }
     if (lane == 0 && n_exact) atomicAdd(&counters[C_LEAF_EXACT], n_exact);
     if (lane == 0 && n_replay) atomicAdd(&counters[C_LEAF_REPLAY], n_replay);
+}
+
+// Request list w (m entries) for kd leaf order: the first request moves it
+// from state 0 to 1, reserves its place in the leaf arrays and queues it.
+__device__ __forceinline__ void request_list(const LeafDemand &dm, int64_t w, int m) {
+    if (dm.state[w] == 0 && atomicCAS(&dm.state[w], 0, 1) == 0) {
+        dm.leaf_offset[w] = (int64_t)atomicAdd(dm.leaf_used, (unsigned long long)m);
+        dm.work[atomicAdd(dm.n_work, 1ull)] = w;
+    }
 }
 
 // Lists needed before the search starts: a pair with no empty candidate
@@ -1333,8 +1345,7 @@ __global__ void k_demand_levels(TemplateView tv, CandView cd, int32_t n_pairs, i
                 if (cj < c || (cj == c && j < lane)) rank++;
             }
         }
-        if (lane < n && rank >= 1 && rank <= max_level && dm.state[w] == 0 && atomicCAS(&dm.state[w], 0, 1) == 0)
-            dm.work[atomicAdd(dm.n_work, 1ull)] = w;
+        if (lane < n && rank >= 1 && rank <= max_level) request_list(dm, w, c);
     }
 }
 
@@ -1821,7 +1832,9 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
             int tk = st.order[lane];
             int64_t w2 = (int64_t)s * G + tv.sig[ab + tk];
             if (dm.state && lane > 0) lvl_ready = dm.state[w2] == 2;
-            st.lvl_off[lane] = cd.offset[w2];
+            // level 0 reads the list in candidate order, the others in kd
+            // leaf order (their leaf offset is set once the list is ordered)
+            st.lvl_off[lane] = lane == 0 ? cd.offset[w2] : cd.leaf_offset[w2];
             st.blk_off[lane] = cd.blk_offset[w2];
             st.lvl_cnt[lane] = cd.count[w2];
             st.tkey[lane] = tv.key[ab + tk];
@@ -1851,7 +1864,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
             return j == 0 ? cd.cand_atom[off0 + pos] : cd.leaf_atom[st.lvl_off[j] + pos];
         };
         auto level_xyz = [&](int j, int pos) -> float4 {
-            return j == 0 ? cd.cand_xyz[off0 + pos] : cd.leaf_xyz[st.lvl_off[j] + pos];
+            return j == 0 ? cv.xyz32[abase + cd.cand_atom[off0 + pos]] : cd.leaf_xyz[st.lvl_off[j] + pos];
         };
 
         bool stop = false;
@@ -2057,9 +2070,12 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                             for (int i = lane; i < cj; i += 32) dst[pj + i] = src[i];
                         }
                     }
+                    // request the lists of this level and of every deeper
+                    // one (a resumed pair then never stops again: a chunk
+                    // takes at most two search rounds)
+                    if (lane >= child && lane < n && !((ready_mask >> lane) & 1u))
+                        request_list(dm, (int64_t)s * G + tv.sig[ab + st.order[lane]], st.lvl_cnt[lane]);
                     if (lane == 0) {
-                        const int64_t w = (int64_t)s * G + tv.sig[ab + st.order[child]];
-                        if (atomicCAS(&dm.state[w], 0, 1) == 0) dm.work[atomicAdd(dm.n_work, 1ull)] = w;
                         Suspended sp;
                         sp.pair = pair;
                         sp.pad = 0;
@@ -2091,6 +2107,17 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         __syncwarp();
                         lev = child;
                         continue;
+                    }
+                    // the boxes of the first 32 blocks from the cursor do not
+                    // depend on the parent's chain: their loads are issued
+                    // before the chain is gathered
+                    const int nblk = (mc + 31) >> 5;
+                    const int gfirst = st.cnd[lev];
+                    const int64_t boff = st.blk_off[child];
+                    float4 bl = make_float4(0.f, 0.f, 0.f, 0.f), bh = bl;
+                    if (gfirst + lane < nblk) {
+                        bl = cd.blk_lo[boff + gfirst + lane];
+                        bh = cd.blk_hi[boff + gfirst + lane];
                     }
                     if (chain_lev != lev || chain_par != ppar) {
                         // positions of the parent's chain, by walking the tiles
@@ -2135,26 +2162,43 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                     // the 32 lanes and the passing ones become children (or
                     // complete rows); the parent is left early only when the
                     // child tile cannot take another block
-                    const int nblk = (mc + 31) >> 5;
                     int ncnt = ccnt;
                     int resume = -1;
-                    for (int g0 = st.cnd[lev]; g0 < nblk && resume < 0 && !stop; g0 += 32) {
+                    for (int g0 = gfirst; g0 < nblk && resume < 0 && !stop; g0 += 32) {
                         const int b = g0 + lane;
                         bool hit = false;
                         if (b < nblk) {
-                            const float4 bl = cd.blk_lo[st.blk_off[child] + b];
-                            const float4 bh = cd.blk_hi[st.blk_off[child] + b];
                             hit = !(bl.x > box_hi[0] || bh.x < box_lo[0] || bl.y > box_hi[1] || bh.y < box_lo[1] ||
                                     bl.z > box_hi[2] || bh.z < box_lo[2]);
                         }
+                        // boxes of the next 32 blocks, loaded while these are
+                        // processed
+                        if (b + 32 < nblk) {
+                            bl = cd.blk_lo[boff + b + 32];
+                            bh = cd.blk_hi[boff + b + 32];
+                        }
                         unsigned hm = __ballot_sync(FULL_MASK, hit);
-                        while (hm) {
-                            const int blk = g0 + __ffs(hm) - 1;
+                        // hit blocks in order; the leaves of the next hit
+                        // block are loaded while the current one is tested
+                        int nxt = -1;
+                        float4 xn = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (hm) {
+                            nxt = g0 + __ffs(hm) - 1;
                             hm &= hm - 1;
+                            if (nxt * 32 + lane < mc) xn = cd.leaf_xyz[coff + nxt * 32 + lane];
+                        }
+                        while (nxt >= 0) {
+                            const int blk = nxt;
+                            const float4 xc = xn;
+                            nxt = -1;
+                            if (hm) {
+                                nxt = g0 + __ffs(hm) - 1;
+                                hm &= hm - 1;
+                                if (nxt * 32 + lane < mc) xn = cd.leaf_xyz[coff + nxt * 32 + lane];
+                            }
                             cr = blk * 32 + lane;
                             pass = false;
                             if (cr < mc) {
-                                const float4 xc = cd.leaf_xyz[coff + cr];
                                 const int32_t kn = __float_as_int(xc.w);
                                 pass = true;
                                 unsigned exact = 0;
@@ -2539,10 +2583,9 @@ void launch_params(cudaStream_t st, int n_templates, const int32_t *atom_begin, 
 }
 
 void launch_candidates(cudaStream_t st, int blocks, bool fill, const ChunkView &cv, const SigView &sv,
-                       int32_t *count, int32_t *scanned, const int64_t *offset, int32_t *cand_atom,
-                       float4 *cand_xyz) {
-    if (fill) k_candidates<true><<<blocks, 256, 0, st>>>(cv, sv, count, scanned, offset, cand_atom, cand_xyz);
-    else k_candidates<false><<<blocks, 256, 0, st>>>(cv, sv, count, scanned, offset, cand_atom, cand_xyz);
+                       int32_t *count, int32_t *scanned, const int64_t *offset, int32_t *cand_atom) {
+    if (fill) k_candidates<true><<<blocks, 256, 0, st>>>(cv, sv, count, scanned, offset, cand_atom);
+    else k_candidates<false><<<blocks, 256, 0, st>>>(cv, sv, count, scanned, offset, cand_atom);
 }
 
 void launch_scan_tiles_i32(cudaStream_t st, const int32_t *in, int64_t n, int64_t *out, int64_t *tile_sums) {
@@ -2561,7 +2604,7 @@ void launch_scan_add(cudaStream_t st, int64_t *out, int64_t n, const int64_t *ti
 
 void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t n_sigs, const int32_t *count,
                        const int64_t *offset, const int64_t *blk_offset, const int32_t *cand_atom,
-                       const float4 *cand_xyz, int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
+                       const int64_t *leaf_offset, int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
                        int64_t *sorted_list, unsigned long long *sorted_count, int64_t list_cap,
                        int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters,
                        const int64_t *work, const unsigned long long *n_work) {
@@ -2574,7 +2617,7 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
         int r = v ? atoi(v) : LEAF_RANK_MAX;
         return r < 1 ? 1 : r > LEAF_FAST_MAX ? LEAF_FAST_MAX : r;
     }();
-    k_leaf_order<<<blocks, LEAF_WARPS * 32, 0, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, cand_xyz,
+    k_leaf_order<<<blocks, LEAF_WARPS * 32, 0, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset,
                                                     leaf_atom, leaf_xyz, blk_lo, blk_hi, sorted_list, sorted_count,
                                                     list_cap, exact_list, exact_count, counters, rank_max,
                                                     work, n_work);
@@ -2586,24 +2629,24 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
     // LEAF_SORTED_MAX 50 KB (1 a block)
     constexpr int SS0 = (int)sizeof(SortedWarp<512>) * 4;
     cudaFuncSetAttribute(k_leaf_sorted<512, 0, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, SS0);
-    k_leaf_sorted<512, 0, 4><<<sms * 4, 128, SS0, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, cand_xyz,
+    k_leaf_sorted<512, 0, 4><<<sms * 4, 128, SS0, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset,
                                                        leaf_atom, leaf_xyz, blk_lo, blk_hi, sorted_list,
                                                        sorted_count, exact_list, exact_count, counters);
     constexpr int SS1 = (int)sizeof(SortedWarp<1024>) * 2;
     cudaFuncSetAttribute(k_leaf_sorted<1024, 512, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, SS1);
     k_leaf_sorted<1024, 512, 2><<<sms * 4, 64, SS1, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom,
-                                                         cand_xyz, leaf_atom, leaf_xyz, blk_lo, blk_hi,
+                                                         leaf_offset, leaf_atom, leaf_xyz, blk_lo, blk_hi,
                                                          sorted_list + list_cap, sorted_count + 1, exact_list,
                                                          exact_count, counters);
     constexpr int SS2 = (int)sizeof(SortedWarp<LEAF_SORTED_MAX>);
     cudaFuncSetAttribute(k_leaf_sorted<LEAF_SORTED_MAX, 1024, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SS2);
     k_leaf_sorted<LEAF_SORTED_MAX, 1024, 1><<<sms * 4, 32, SS2, st>>>(
-        cv, n_sigs, count, offset, blk_offset, cand_atom, cand_xyz, leaf_atom, leaf_xyz, blk_lo, blk_hi,
+        cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset, leaf_atom, leaf_xyz, blk_lo, blk_hi,
         sorted_list + 2 * list_cap, sorted_count + 2, exact_list, exact_count, counters);
     // exact replay: lists up to 1024 entries 16 KB a warp, 4 warps a block
     constexpr int SM1 = 1024 * 16 * 4;
     cudaFuncSetAttribute(k_leaf_exact<1024, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM1);
-    k_leaf_exact<1024, 0><<<sms * 3, 128, SM1, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, cand_xyz,
+    k_leaf_exact<1024, 0><<<sms * 3, 128, SM1, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset,
                                                     leaf_atom, leaf_xyz, blk_lo, blk_hi, exact_list, exact_count,
                                                     counters);
     // longer lists: 64 KB a warp, one warp a block (beyond EXACT_MAX: one
@@ -2611,7 +2654,7 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
     constexpr int SM2 = EXACT_MAX * 16;
     cudaFuncSetAttribute(k_leaf_exact<EXACT_MAX, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM2);
     k_leaf_exact<EXACT_MAX, 1024><<<sms * 3, 32, SM2, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom,
-                                                           cand_xyz, leaf_atom, leaf_xyz, blk_lo, blk_hi,
+                                                           leaf_offset, leaf_atom, leaf_xyz, blk_lo, blk_hi,
                                                            exact_list, exact_count, counters);
 }
 

@@ -14,7 +14,10 @@ namespace pjg {
 #define PJG_NOALLOC_MAX_ROWS (1 << 20)
 #endif
 
-constexpr int SEARCH_WARPS = 8;        // warps per block of k_search
+#ifndef PJG_SEARCH_WARPS
+#define PJG_SEARCH_WARPS 8
+#endif
+constexpr int SEARCH_WARPS = PJG_SEARCH_WARPS;  // warps per block of k_search
 // resident k_search blocks per SM the register allocation is sized for
 #ifndef PJG_SEARCH_MIN_BLOCKS
 #define PJG_SEARCH_MIN_BLOCKS 2
@@ -75,6 +78,10 @@ struct LeafDemand {
     int32_t n_resume;                  //   nullptr: pairs 0 .. n_pairs-1
     Suspended *suspended;              // pairs that stopped at an unordered
     unsigned long long *n_suspended;   //   list in this round
+    int64_t *leaf_offset;              // [lists] set at the list's request
+    unsigned long long *leaf_used;     // leaf entries reserved (may pass the
+                                       //   arrays' capacity: the host grows
+                                       //   them before the lists are ordered)
     unsigned char *pool_out;           // states saved in this round
     unsigned long long *pool_used;     //   (bytes taken; may pass pool_cap)
     int64_t pool_cap;
@@ -127,8 +134,7 @@ void launch_params(cudaStream_t st, int n_templates, const int32_t *atom_begin, 
                    const double *dist, const double *weight, double r, double s, double g, AnnulusParam *out);
 
 void launch_candidates(cudaStream_t st, int blocks, bool fill, const ChunkView &cv, const SigView &sv,
-                       int32_t *count, int32_t *scanned, const int64_t *offset, int32_t *cand_atom,
-                       float4 *cand_xyz);
+                       int32_t *count, int32_t *scanned, const int64_t *offset, int32_t *cand_atom);
 
 // exclusive scan of one tile (SCAN_TILE entries) per block
 constexpr int SCAN_TILE_THREADS = 512;
@@ -141,7 +147,7 @@ void launch_scan_add(cudaStream_t st, int64_t *out, int64_t n, const int64_t *ti
 // or of every list of the chunk when work == nullptr
 void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t n_sigs, const int32_t *count,
                        const int64_t *offset, const int64_t *blk_offset, const int32_t *cand_atom,
-                       const float4 *cand_xyz, int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
+                       const int64_t *leaf_offset, int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
                        int64_t *sorted_list, unsigned long long *sorted_count, int64_t list_cap,
                        int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters,
                        const int64_t *work, const unsigned long long *n_work);

@@ -376,3 +376,18 @@ def test_leaf_order_on_demand_orders_fewer_entries(monkeypatch):
     assert ls["leaf_entries"] < fs["leaf_entries"]
     for key in ("partials", "complete", "bytes_expansion", "fp64_rechecks"):
         assert fs[key] == ls[key], key
+
+
+@pytest.mark.parametrize("levels", [1, 4])
+def test_leaf_arrays_grow(monkeypatch, levels):
+    """Leaf-order arrays that start at one entry grow as lists are requested
+    (before the search and between rounds); one structure per chunk."""
+    from pyjess_gb300 import workloads as W
+
+    monkeypatch.setenv("PJG_LEAF_LEVELS", str(levels))
+    monkeypatch.setenv("PJG_LEAF_CAPACITY", "1")
+    wl = W.config(3, n_structures=12, n_templates=300)
+    compare(wl.templates, wl.structures, mode="fp32", **wl.params)
+    monkeypatch.setenv("PJG_ENTRY_BUDGET", "1")
+    res, _ = compare(wl.templates, wl.structures, mode="fp32", **wl.params)
+    assert res.stats()["chunks"] == 12
