@@ -991,8 +991,8 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 // entries for every level but the last
                 int levels = std::max(1, tp->nmax - 1);
                 size_t entry = sp->max_atoms > 65535 ? 8 : 4;
-                size_t need = 2816 + entry * 64 * (size_t)levels;
-                sa.warp_smem = (int)((std::max<size_t>(need, 8192) + 15) & ~size_t(15));
+                size_t need = 4096 + entry * 64 * (size_t)levels;
+                sa.warp_smem = (int)((std::max<size_t>(need, 9472) + 15) & ~size_t(15));
             }
             sa.cut_inline = cut_inline ? 1 : 0;
             sa.rmsd_threshold = P->rmsd_threshold;

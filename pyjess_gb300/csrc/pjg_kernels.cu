@@ -1628,6 +1628,9 @@ struct PairState {
     float4 cxyz[32];
     float4 cthr[32];
     int32_t cpos[32];
+    // block mode: leaves inside the parent's join box awaiting the full test
+    float4 qxyz[64];
+    int32_t qpos[64];
 };
 
 template <typename PosT>
@@ -2108,11 +2111,21 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         lev = child;
                         continue;
                     }
-                    // the boxes of the first 32 blocks from the cursor do not
-                    // depend on the parent's chain: their loads are issued
-                    // before the chain is gathered
+                    // The parent's chain, then every block from the cursor on
+                    // whose bounding box meets the join box, in leaf order.
+                    // Each lane tests its leaf against the join box; the
+                    // leaves inside it go to a queue in shared memory, and the
+                    // full test (chain/residue rules, FP32 annuli, FP64
+                    // recheck) runs on batches of 32 queued leaves, so the
+                    // children (or complete rows) come out in leaf order.  The
+                    // cursor st.cnd[lev] is the first leaf position not yet
+                    // tested; the parent is left early only when the child
+                    // tile cannot take another batch.  The boxes of the first
+                    // 32 blocks do not depend on the chain: their loads are
+                    // issued before the chain is gathered.
                     const int nblk = (mc + 31) >> 5;
-                    const int gfirst = st.cnd[lev];
+                    const int pstart = st.cnd[lev];
+                    const int gfirst = pstart >> 5;
                     const int64_t boff = st.blk_off[child];
                     float4 bl = make_float4(0.f, 0.f, 0.f, 0.f), bh = bl;
                     if (gfirst + lane < nblk) {
@@ -2157,13 +2170,75 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         chain_par = ppar;
                         __syncwarp();
                     }
-                    // every block from the cursor on whose bounding box meets
-                    // the join box, in order: its 32 candidates are tested by
-                    // the 32 lanes and the passing ones become children (or
-                    // complete rows); the parent is left early only when the
-                    // child tile cannot take another block
                     int ncnt = ccnt;
                     int resume = -1;
+                    int queued = 0;
+                    // full test of queue entries 0..k-1 (lane i takes entry i),
+                    // then the entries after them move to the queue's front
+                    auto run_batch = [&](int k) {
+                        cr = lane < k ? st.qpos[lane] : 0;
+                        const float4 xc = lane < k ? st.qxyz[lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+                        pass = false;
+                        if (lane < k) {
+                            const int32_t kn = __float_as_int(xc.w);
+                            pass = true;
+                            unsigned exact = 0;
+                            for (int j = 0; j <= lev; j++) {
+                                const float4 xj = st.cxyz[j];
+                                if (!check_pair(__float_as_int(xj.w), kn, st.tkey[j], tn, sa.ignore_chain)) {
+                                    pass = false;
+                                    break;
+                                }
+                                if (FP32) {
+                                    const float dx = xj.x - xc.x, dy = xj.y - xc.y, dz = xj.z - xc.z;
+                                    const float d2 = dx * dx + dy * dy + dz * dz;
+                                    const float4 th = st.cthr[j];
+                                    if (d2 < th.x || d2 > th.w) {
+                                        pass = false;
+                                        break;
+                                    }
+                                    if (!(d2 >= th.y && d2 <= th.z)) exact |= 1u << j;
+                                } else {
+                                    exact |= 1u << j;
+                                }
+                            }
+                            if (pass && exact) {
+                                if (FP32) rechecks += __popc(exact);
+                                int32_t atoms[32];
+                                for (int j = 0; j <= lev; j++) atoms[j] = level_atom(j, st.cpos[j]);
+                                pass = decide_fp64(exact, lev, atoms, cd.leaf_atom[coff + cr], xyz64, prm, st.order,
+                                                   n, qn, cd.leaf_atom + coff, mc, cr);
+                            }
+                        }
+                        const unsigned m = __ballot_sync(FULL_MASK, pass);
+                        if (last) {
+                            int32_t pos[32];
+                            for (int j = 0; j <= lev; j++) pos[j] = st.cpos[j];
+                            emit(pass, pos, cr);
+                        } else if (pass) {
+                            E e;
+                            e.pos = (PosT)cr;
+                            e.parent = (uint16_t)ppar;
+                            ctile[ncnt + __popc(m & ((1u << lane) - 1u))] = e;
+                        }
+                        if (!last) ncnt += __popc(m);
+                        if (lane == 0) st.F[child] += __popc(m);
+                        const int rest = queued - k;
+                        int qp = 0;
+                        float4 qx = make_float4(0.f, 0.f, 0.f, 0.f);
+                        __syncwarp();
+                        if (lane < rest) {
+                            qp = st.qpos[k + lane];
+                            qx = st.qxyz[k + lane];
+                        }
+                        __syncwarp();
+                        if (lane < rest) {
+                            st.qpos[lane] = qp;
+                            st.qxyz[lane] = qx;
+                        }
+                        __syncwarp();
+                        queued = rest;
+                    };
                     for (int g0 = gfirst; g0 < nblk && resume < 0 && !stop; g0 += 32) {
                         const int b = g0 + lane;
                         bool hit = false;
@@ -2179,7 +2254,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         }
                         unsigned hm = __ballot_sync(FULL_MASK, hit);
                         // hit blocks in order; the leaves of the next hit
-                        // block are loaded while the current one is tested
+                        // block are loaded while the current one is queued
                         int nxt = -1;
                         float4 xn = make_float4(0.f, 0.f, 0.f, 0.f);
                         if (hm) {
@@ -2196,61 +2271,35 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                                 hm &= hm - 1;
                                 if (nxt * 32 + lane < mc) xn = cd.leaf_xyz[coff + nxt * 32 + lane];
                             }
-                            cr = blk * 32 + lane;
-                            pass = false;
-                            if (cr < mc) {
-                                const int32_t kn = __float_as_int(xc.w);
-                                pass = true;
-                                unsigned exact = 0;
-                                for (int j = 0; j <= lev; j++) {
-                                    const float4 xj = st.cxyz[j];
-                                    if (!check_pair(__float_as_int(xj.w), kn, st.tkey[j], tn, sa.ignore_chain)) {
-                                        pass = false;
-                                        break;
-                                    }
-                                    if (FP32) {
-                                        const float dx = xj.x - xc.x, dy = xj.y - xc.y, dz = xj.z - xc.z;
-                                        const float d2 = dx * dx + dy * dy + dz * dz;
-                                        const float4 th = st.cthr[j];
-                                        if (d2 < th.x || d2 > th.w) {
-                                            pass = false;
-                                            break;
-                                        }
-                                        if (!(d2 >= th.y && d2 <= th.z)) exact |= 1u << j;
-                                    } else {
-                                        exact |= 1u << j;
-                                    }
-                                }
-                                if (pass && exact) {
-                                    if (FP32) rechecks += __popc(exact);
-                                    int32_t atoms[32];
-                                    for (int j = 0; j <= lev; j++) atoms[j] = level_atom(j, st.cpos[j]);
-                                    pass = decide_fp64(exact, lev, atoms, cd.leaf_atom[coff + cr], xyz64, prm, st.order,
-                                                       n, qn, cd.leaf_atom + coff, mc, cr);
-                                }
+                            const int q = blk * 32 + lane;
+                            const bool inb = q < mc && q >= pstart &&
+                                             !(xc.x < box_lo[0] || xc.x > box_hi[0] || xc.y < box_lo[1] ||
+                                               xc.y > box_hi[1] || xc.z < box_lo[2] || xc.z > box_hi[2]);
+                            const unsigned im = __ballot_sync(FULL_MASK, inb);
+                            if (inb) {
+                                const int qi = queued + __popc(im & ((1u << lane) - 1u));
+                                st.qpos[qi] = q;
+                                st.qxyz[qi] = xc;
                             }
-                            const unsigned m = __ballot_sync(FULL_MASK, pass);
-                            if (last) {
-                                int32_t pos[32];
-                                for (int j = 0; j <= lev; j++) pos[j] = st.cpos[j];
-                                emit(pass, pos, cr);
-                            } else if (pass) {
-                                E e;
-                                e.pos = (PosT)cr;
-                                e.parent = (uint16_t)ppar;
-                                ctile[ncnt + __popc(m & ((1u << lane) - 1u))] = e;
-                            }
-                            if (!last) ncnt += __popc(m);
-                            if (lane == 0) st.F[child] += __popc(m);
-                            if (stop) break;
-                            if (!last && cap - ncnt < 32) {
-                                // child tile full: finish it first, then
-                                // come back to this parent at the next block
-                                resume = blk + 1;
-                                break;
+                            queued += __popc(im);
+                            __syncwarp();
+                            if (queued >= 32) {
+                                if (!last && cap - ncnt < 32) {
+                                    // child tile full: finish it first, then
+                                    // come back to this parent at the queue's
+                                    // first leaf
+                                    resume = st.qpos[0];
+                                    break;
+                                }
+                                run_batch(32);
+                                if (stop) break;
                             }
                         }
                         if (over_budget()) stop = true;
+                    }
+                    if (resume < 0 && !stop && queued > 0) {
+                        if (!last && cap - ncnt < 32) resume = st.qpos[0];
+                        else run_batch(queued);
                     }
                     __syncwarp();
                     if (lane == 0) {
