@@ -241,11 +241,12 @@ def main():
     if os.path.exists(tpath):
         with open(tpath) as f:
             tr = json.load(f)
-        # DRAM bytes per launch measured by ncu on a smaller case, scaled to
-        # this workload's launch by the expansion bytes it processes
-        if tr.get("bytes_expansion_per_launch"):
-            per_launch_exp = exp_bytes / max(1, sum(s["chunks"] for s in stats))
-            traffic = tr["dram_bytes_per_launch"] * per_launch_exp / tr["bytes_expansion_per_launch"]
+        # DRAM bytes per algorithmic expansion byte, measured by ncu over the
+        # k_search launches of one query of a smaller case, times the
+        # expansion bytes of an average launch of this workload
+        if tr.get("dram_per_expansion_byte"):
+            launches_k = max(1, sum(s["search_rounds"] for s in stats))
+            traffic = tr["dram_per_expansion_byte"] * exp_bytes / launches_k
 
     # ---- plain FP64 per-structure path on a subset (the method the batched
     # path is measured against)
@@ -339,7 +340,8 @@ def main():
         "stage_ms": {"candidates": s0["ms_candidates"], "expansion": s0["ms_expansion"],
                      "superposition": s0["ms_superposition"], "total": s0["ms_total"]},
         "counters": {k: s0[k] for k in ("pairs", "candidate_entries", "partials", "complete", "passing", "hits",
-                                        "fp64_rechecks", "leaf_exact", "chunks")},
+                                        "fp64_rechecks", "leaf_lists", "leaf_entries", "leaf_exact", "suspensions",
+                                        "search_rounds", "chunks")},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": launches,
