@@ -227,19 +227,152 @@ struct pjg_results {
 
 namespace {
 
-// Device-to-host copy into caller memory: pinned for the duration of the
-// copy when it is large (one DMA at full link speed), plain otherwise.
-cudaError_t copy_out(void *dst, const void *src, size_t bytes) {
-    if (!dst || bytes == 0) return cudaSuccess;
-    bool reg = false;
-    if (bytes >= (16u << 20)) {
-        reg = cudaHostRegister(dst, bytes, cudaHostRegisterDefault) == cudaSuccess;
-        if (!reg) cudaGetLastError();  // not pinnable here: plain copy
+// Device-to-host copy of result arrays into caller memory.  Small copies
+// are plain cudaMemcpy.  Large ones are split into equal byte ranges, one
+// per host thread; each thread copies its range in 8 MiB pieces through two
+// pinned staging buffers of its own (DMA of piece k+1 overlaps the memcpy of
+// piece k into the caller's pages), so the link, the memcpy bandwidth and
+// the first-touch page faults of fresh caller arrays are spread over the
+// host's cores.  The pinned buffers are kept for later calls.
+
+struct CopySeg {
+    void *dst;
+    const void *src;
+    size_t bytes;
+};
+
+struct StageSlot {
+    void *buf[2] = {nullptr, nullptr};
+};
+
+constexpr size_t STAGE_PIECE = 8u << 20;
+
+std::mutex g_stage_mu;
+std::vector<StageSlot *> g_stage_free;
+
+StageSlot *stage_get() {
+    {
+        std::lock_guard<std::mutex> g(g_stage_mu);
+        if (!g_stage_free.empty()) {
+            StageSlot *s = g_stage_free.back();
+            g_stage_free.pop_back();
+            return s;
+        }
     }
-    cudaError_t e = cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost);
-    if (reg) cudaHostUnregister(dst);
+    StageSlot *s = new StageSlot;
+    for (auto &b : s->buf)
+        if (cudaHostAlloc(&b, STAGE_PIECE, cudaHostAllocPortable) != cudaSuccess) {
+            cudaGetLastError();
+            for (auto &c : s->buf)
+                if (c) cudaFreeHost(c);
+            delete s;
+            return nullptr;
+        }
+    return s;
+}
+
+void stage_put(StageSlot *s) {
+    std::lock_guard<std::mutex> g(g_stage_mu);
+    g_stage_free.push_back(s);
+}
+
+// bytes [lo, hi) of the concatenation of `segs`, by one thread
+cudaError_t copy_range(const std::vector<CopySeg> &segs, size_t lo, size_t hi, int device) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return e;
+    StageSlot *slot = stage_get();
+    cudaStream_t st = nullptr;
+    if (!slot || cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+        // no staging: plain copies of this range
+        cudaGetLastError();
+        size_t base = 0;
+        for (const CopySeg &sg : segs) {
+            const size_t a = std::max(lo, base), b = std::min(hi, base + sg.bytes);
+            if (a < b) {
+                e = cudaMemcpy((char *)sg.dst + (a - base), (const char *)sg.src + (a - base), b - a,
+                               cudaMemcpyDeviceToHost);
+                if (e != cudaSuccess) break;
+            }
+            base += sg.bytes;
+        }
+        if (slot) stage_put(slot);
+        return e;
+    }
+    // pieces of at most STAGE_PIECE bytes, none crossing a segment
+    struct Piece {
+        char *dst;
+        const char *src;
+        size_t n;
+    };
+    std::vector<Piece> pieces;
+    size_t base = 0;
+    for (const CopySeg &sg : segs) {
+        const size_t a = std::max(lo, base), b = std::min(hi, base + sg.bytes);
+        for (size_t x = a; x < b; x += STAGE_PIECE)
+            pieces.push_back({(char *)sg.dst + (x - base), (const char *)sg.src + (x - base),
+                              std::min(STAGE_PIECE, b - x)});
+        base += sg.bytes;
+    }
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    for (auto &d : done)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&d, cudaEventDisableTiming);
+    for (size_t k = 0; k < pieces.size() && e == cudaSuccess; k++) {
+        if (k == 0) {
+            e = cudaMemcpyAsync(slot->buf[0], pieces[0].src, pieces[0].n, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaEventRecord(done[0], st);
+        }
+        if (e == cudaSuccess && k + 1 < pieces.size()) {
+            const int nb = (int)((k + 1) & 1);
+            e = cudaMemcpyAsync(slot->buf[nb], pieces[k + 1].src, pieces[k + 1].n, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaEventRecord(done[nb], st);
+        }
+        if (e == cudaSuccess) e = cudaEventSynchronize(done[k & 1]);
+        if (e == cudaSuccess) std::memcpy(pieces[k].dst, slot->buf[k & 1], pieces[k].n);
+    }
+    cudaStreamSynchronize(st);
+    for (auto &d : done)
+        if (d) cudaEventDestroy(d);
+    cudaStreamDestroy(st);
+    stage_put(slot);
     return e;
 }
+
+cudaError_t copy_out_all(const std::vector<CopySeg> &segs_in) {
+    std::vector<CopySeg> segs;
+    size_t total = 0;
+    for (const CopySeg &sg : segs_in)
+        if (sg.dst && sg.bytes) {
+            segs.push_back(sg);
+            total += sg.bytes;
+        }
+    if (total == 0) return cudaSuccess;
+    int device = 0;
+    cudaGetDevice(&device);
+    unsigned hw = std::thread::hardware_concurrency();
+    // one thread per MiB up to 16 (or the host's cores); a thread keeps 16
+    // MiB of pinned staging
+    int threads = (int)std::min<size_t>(std::min<unsigned>(hw ? hw : 1, 16u), total >> 20);
+    if (threads <= 1) {
+        for (const CopySeg &sg : segs) {
+            cudaError_t e = cudaMemcpy(sg.dst, sg.src, sg.bytes, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+    const size_t slice = ((total + threads - 1) / threads + 4095) & ~size_t(4095);
+    std::vector<cudaError_t> errs(threads, cudaSuccess);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; t++) {
+        const size_t lo = std::min(total, (size_t)t * slice), hi = std::min(total, lo + slice);
+        pool.emplace_back([&, t, lo, hi] { errs[t] = copy_range(segs, lo, hi, device); });
+    }
+    for (auto &th : pool) th.join();
+    for (cudaError_t e : errs)
+        if (e != cudaSuccess) return e;
+    return cudaSuccess;
+}
+
+cudaError_t copy_out(void *dst, const void *src, size_t bytes) { return copy_out_all({{dst, src, bytes}}); }
 
 }  // namespace
 
@@ -1249,14 +1382,14 @@ pjg_status pjg_results_copy(const pjg_results *r, int32_t *structure, int32_t *t
     int prev = 0;
     cudaGetDevice(&prev);
     if (prev != r->device) cudaSetDevice(r->device);
-    cudaError_t e = copy_out(structure, hs.structure, 4 * n);
-    if (e == cudaSuccess) e = copy_out(template_index, hs.tpl, 4 * n);
-    if (e == cudaSuccess) e = copy_out(ordinal, hs.ordinal, 8 * n);
-    if (e == cudaSuccess) e = copy_out(rmsd, hs.rmsd, 8 * n);
-    if (e == cudaSuccess) e = copy_out(rotation, hs.rot, 72 * n);
-    if (e == cudaSuccess) e = copy_out(centres, hs.centres, 48 * n);
-    if (e == cudaSuccess) e = copy_out(atom_offset, hs.atom_offset, 8 * n);
-    if (e == cudaSuccess) e = copy_out(atoms, hs.atoms_, 4 * (size_t)hs.atoms);
+    cudaError_t e = copy_out_all({{structure, hs.structure, 4 * n},
+                                  {template_index, hs.tpl, 4 * n},
+                                  {ordinal, hs.ordinal, 8 * n},
+                                  {rmsd, hs.rmsd, 8 * n},
+                                  {rotation, hs.rot, 72 * n},
+                                  {centres, hs.centres, 48 * n},
+                                  {atom_offset, hs.atom_offset, 8 * n},
+                                  {atoms, hs.atoms_, 4 * (size_t)hs.atoms}});
     if (prev != r->device) cudaSetDevice(prev);
     if (e != cudaSuccess) return fail(PJG_ERR_CUDA, "results copy: %s", cudaGetErrorString(e));
     return PJG_OK;

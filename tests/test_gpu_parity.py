@@ -391,3 +391,21 @@ def test_leaf_arrays_grow(monkeypatch, levels):
     monkeypatch.setenv("PJG_ENTRY_BUDGET", "1")
     res, _ = compare(wl.templates, wl.structures, mode="fp32", **wl.params)
     assert res.stats()["chunks"] == 12
+
+
+def test_large_result_copy_out():
+    """Results of several MiB come back through the threaded, staged copy
+    (one host thread per MiB, pinned double buffers): every field matches the
+    oracle, and a second copy of the same results is identical."""
+    from pyjess_gb300 import workloads as W
+
+    wl = W.config(3, n_structures=60, n_templates=600)
+    res, ref = compare(wl.templates, wl.structures, mode="fp32", **wl.params)
+    a = res.arrays()
+    nbytes = sum(v.nbytes for k, v in a.items() if hasattr(v, "nbytes"))
+    assert nbytes > (4 << 20), nbytes
+    res._arrays = None
+    b = res.arrays()
+    for k in a:
+        if hasattr(a[k], "nbytes"):
+            assert np.array_equal(a[k], b[k]), k
