@@ -18,9 +18,10 @@ FP32-guarded distance tests with FP64 recheck.
               host cores, on a bounded sample of the same workload
 
 `--impl reference` times that CPU implementation alone on this workload
-(bounded sample per step).  Under torchrun (N>1) structures are sharded
-across ranks (weak scaling: every rank runs all templates against its own
-2,000 structures); rank 0 prints one JSON line.
+(bounded sample per step).  Under torchrun (N>1) every rank runs its own
+config-3 instance (independent pairs: weak scaling, no data-path
+collective); the step time is the maximum over ranks (gloo all-reduce) and
+rank 0 prints one JSON line.
 """
 
 from __future__ import annotations
@@ -127,15 +128,24 @@ def measured_peaks():
 
 
 def workload(args, rank=0, world=1):
+    """This rank's share of a multi-GPU run: rank 0 takes config 3 itself,
+    rank r an independent instance drawn with the same distributions (weak
+    scaling: the pairs of every rank are independent, no data-path
+    collective)."""
     from pyjess_gb300 import workloads as W
 
-    wl = W.config(3, n_structures=args.structures, n_templates=args.templates)
-    if world > 1:
-        # weak scaling: every rank runs its own full structure set (a
-        # different seed per rank would change the hit statistics; the same
-        # shape is kept, structures are re-drawn per rank index)
-        pass
-    return wl
+    return W.config(3, n_structures=args.structures, n_templates=args.templates, shard=rank if world > 1 else 0)
+
+
+def max_over_ranks(value, dist):
+    """The largest `value` over all ranks (gloo all-reduce), or `value`."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def cpu_sample(wl, n_structures, threads):
@@ -218,13 +228,7 @@ def main():
             step_ms.append(st["ms_total"])
             launches += st["launches"]
             arr = res.arrays()
-    total_ms = sum(step_ms)
-    if dist:
-        import torch
-
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(step_ms), dist)
     pairs_step = wl.pairs
     value = pairs_step * world * args.steps / (total_ms / 1e3)
     s0 = stats[-1]
@@ -291,13 +295,7 @@ def main():
                 for k, v in zip(phases, (t2 - t1, t3 - t2, t4 - t3, t5 - t4)):
                     phases[k] += 1e3 * v / args.steps
             d2h = sum(v.nbytes for k, v in a2.items() if hasattr(v, "nbytes"))
-        tot = sum(times)
-        if dist:
-            import torch
-
-            t = torch.tensor([tot], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            tot = float(t.item())
+        tot = max_over_ranks(sum(times), dist)
         e2e = {"value": pairs_step * world * args.steps / tot, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "phases_ms": {k: round(v, 1) for k, v in phases.items()}}
 

@@ -318,11 +318,13 @@ class Workload:
 
 
 def config(index: int, *, scale: float = 1.0, n_structures=None, n_templates=None,
-           residues=None) -> Workload:
+           residues=None, shard: int = 0) -> Workload:
     """Benchmark configuration `index` (0-4).  `scale` shrinks structure and
     template counts proportionally (parity tests run reduced instances);
-    `residues` = (lo, hi) overrides the structure length range of config 4."""
-    ss = _seed(index)
+    `residues` = (lo, hi) overrides the structure length range of config 4;
+    `shard` > 0 draws an independent instance with the same distributions
+    (one per rank of a multi-GPU run)."""
+    ss = _seed(index) if shard == 0 else _seed(index, shard)
     if index == 0:
         rng = np.random.Generator(np.random.PCG64(ss))
         s = make_structure(rng, 300)
