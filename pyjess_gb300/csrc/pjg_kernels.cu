@@ -1628,6 +1628,10 @@ struct PairState {
     float4 cxyz[32];
     float4 cthr[32];
     int32_t cpos[32];
+    // join box of the chain below the parent's level, and the parent index
+    // (one level up) that chain belongs to
+    float pbox[6];
+    int32_t chain_gp;
     // block mode: leaves inside the parent's join box awaiting the full test
     float4 qxyz[64];
     int32_t qpos[64];
@@ -1862,12 +1866,14 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
         const int m0 = st.lvl_cnt[0];
         const int64_t off0 = st.lvl_off[0];
 
-        // atom of level j at list position pos
+        // atom of level j at tile entry value pos: level-0 entries hold the
+        // atom itself (the seeds' candidate-order positions are only a
+        // cursor), deeper ones the position in the level's leaf order
         auto level_atom = [&](int j, int pos) -> int32_t {
-            return j == 0 ? cd.cand_atom[off0 + pos] : cd.leaf_atom[st.lvl_off[j] + pos];
+            return j == 0 ? pos : cd.leaf_atom[st.lvl_off[j] + pos];
         };
         auto level_xyz = [&](int j, int pos) -> float4 {
-            return j == 0 ? cv.xyz32[abase + cd.cand_atom[off0 + pos]] : cd.leaf_xyz[st.lvl_off[j] + pos];
+            return j == 0 ? cv.xyz32[abase + pos] : cd.leaf_xyz[st.lvl_off[j] + pos];
         };
 
         bool stop = false;
@@ -1941,7 +1947,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
             // reporting (patches/Scanner.c.patch:244-263): seeds 1..m0-1
             for (int b = 1; b < m0 && !stop; b += 32) {
                 int p = b + lane;
-                emit(p < m0, nullptr, p);
+                emit(p < m0, nullptr, p < m0 ? cd.cand_atom[off0 + p] : 0);
                 if (over_budget()) stop = true;
             }
             if (lane == 0) st.F[0] = m0;
@@ -1990,7 +1996,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                     E *t0 = tiles + st.tile[0];
                     for (int i = lane; i < kk; i += 32) {
                         E e;
-                        e.pos = (PosT)(root + i);
+                        e.pos = (PosT)cd.cand_atom[off0 + root + i];
                         e.parent = 0;
                         t0[i] = e;
                     }
@@ -2133,39 +2139,77 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         bh = cd.blk_hi[boff + gfirst + lane];
                     }
                     if (chain_lev != lev || chain_par != ppar) {
-                        // positions of the parent's chain, by walking the tiles
-                        __syncwarp();
-                        if (lane == 0) {
-                            int idx = ppar;
-                            for (int j = lev; j >= 0; j--) {
-                                E e = tiles[st.tile[j] + idx];
-                                st.cpos[j] = (int)e.pos;
-                                idx = e.parent;
+                        const E pe = tiles[st.tile[lev] + ppar];
+                        float olo[3] = {-INFINITY, -INFINITY, -INFINITY}, ohi[3] = {INFINITY, INFINITY, INFINITY};
+                        if (chain_lev == lev && lev > 0 && (int)pe.parent == st.chain_gp) {
+                            // a sibling of the previous parent: levels below
+                            // lev are unchanged, only this parent's point
+                            // and box are new
+                            if (lane == lev) {
+                                const float4 cj = level_xyz(lev, (int)pe.pos);
+                                st.cxyz[lev] = cj;
+                                st.cpos[lev] = (int)pe.pos;
+                                const float rb = sqrtf(fmaxf(st.cthr[lev].w, 0.f)) * 1.000001f + 1e-3f;
+                                olo[0] = cj.x - rb;
+                                olo[1] = cj.y - rb;
+                                olo[2] = cj.z - rb;
+                                ohi[0] = cj.x + rb;
+                                ohi[1] = cj.y + rb;
+                                ohi[2] = cj.z + rb;
                             }
+                        } else {
+                            // positions of the parent's chain, by walking the tiles
+                            __syncwarp();
+                            if (lane == 0) {
+                                int idx = ppar;
+                                for (int j = lev; j >= 0; j--) {
+                                    E e = tiles[st.tile[j] + idx];
+                                    st.cpos[j] = (int)e.pos;
+                                    idx = e.parent;
+                                }
+                                st.chain_gp = (int)pe.parent;
+                            }
+                            __syncwarp();
+                            float lo[3] = {-INFINITY, -INFINITY, -INFINITY}, hi[3] = {INFINITY, INFINITY, INFINITY};
+                            if (lane <= lev) {
+                                float4 cj = level_xyz(lane, st.cpos[lane]);
+                                float4 th = prm[st.order[lane] * n + qn].thr;
+                                st.cxyz[lane] = cj;
+                                st.cthr[lane] = th;
+                                float rb = sqrtf(fmaxf(th.w, 0.f)) * 1.000001f + 1e-3f;
+                                lo[0] = cj.x - rb;
+                                lo[1] = cj.y - rb;
+                                lo[2] = cj.z - rb;
+                                hi[0] = cj.x + rb;
+                                hi[1] = cj.y + rb;
+                                hi[2] = cj.z + rb;
+                            }
+                            if (lane == lev)
+                                for (int i = 0; i < 3; i++) {
+                                    olo[i] = lo[i];
+                                    ohi[i] = hi[i];
+                                }
+                            // join box of levels below lev (kept for siblings)
+                            for (int i = 0; i < 3; i++) {
+                                float a = lane < lev ? lo[i] : -INFINITY, b = lane < lev ? hi[i] : INFINITY;
+                                for (int off = 16; off; off >>= 1) {
+                                    a = fmaxf(a, __shfl_xor_sync(FULL_MASK, a, off));
+                                    b = fminf(b, __shfl_xor_sync(FULL_MASK, b, off));
+                                }
+                                if (lane == 0) {
+                                    st.pbox[i] = a;
+                                    st.pbox[3 + i] = b;
+                                }
+                            }
+                            __syncwarp();
                         }
-                        __syncwarp();
-                        float lo[3] = {-INFINITY, -INFINITY, -INFINITY}, hi[3] = {INFINITY, INFINITY, INFINITY};
-                        if (lane <= lev) {
-                            float4 cj = level_xyz(lane, st.cpos[lane]);
-                            float4 th = prm[st.order[lane] * n + qn].thr;
-                            st.cxyz[lane] = cj;
-                            st.cthr[lane] = th;
-                            float rb = sqrtf(fmaxf(th.w, 0.f)) * 1.000001f + 1e-3f;
-                            lo[0] = cj.x - rb;
-                            lo[1] = cj.y - rb;
-                            lo[2] = cj.z - rb;
-                            hi[0] = cj.x + rb;
-                            hi[1] = cj.y + rb;
-                            hi[2] = cj.z + rb;
-                        }
+                        // the parent's own box, from lane lev, met with the
+                        // prefix box
                         for (int i = 0; i < 3; i++) {
-                            for (int off = 16; off; off >>= 1) {
-                                lo[i] = fmaxf(lo[i], __shfl_xor_sync(FULL_MASK, lo[i], off));
-                                hi[i] = fminf(hi[i], __shfl_xor_sync(FULL_MASK, hi[i], off));
-                            }
-                            box_lo[i] = lo[i];
-                            box_hi[i] = hi[i];
+                            box_lo[i] = fmaxf(st.pbox[i], __shfl_sync(FULL_MASK, olo[i], lev));
+                            box_hi[i] = fminf(st.pbox[3 + i], __shfl_sync(FULL_MASK, ohi[i], lev));
                         }
+                        __syncwarp();
                         chain_lev = lev;
                         chain_par = ppar;
                         __syncwarp();
