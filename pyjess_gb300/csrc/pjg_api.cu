@@ -23,6 +23,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
+#include <unordered_map>
 #include <mutex>
 #include <numeric>
 #include <atomic>
@@ -97,13 +99,27 @@ void dfree(DBuf<T> &b, cudaStream_t st) {
 }
 
 template <typename T>
-cudaError_t upload(T **dst, const std::vector<T> &v) {
-    size_t bytes = std::max<size_t>(v.size(), 1) * sizeof(T);
-    cudaError_t e = cudaMalloc((void **)dst, bytes);
+cudaError_t upload(T **dst, const T *src, size_t n) {
+    cudaError_t e = cudaMalloc((void **)dst, std::max<size_t>(n, 1) * sizeof(T));
     if (e != cudaSuccess) return e;
-    if (!v.empty()) e = cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (n) e = cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice);
     return e;
 }
+
+template <typename T>
+cudaError_t upload(T **dst, const std::vector<T> &v) {
+    return upload(dst, v.data(), v.size());
+}
+
+// Host staging array of n elements left uninitialised (every element is
+// written before use; a std::vector would zero it first).
+template <typename T>
+struct HostArray {
+    std::unique_ptr<T[]> p;
+    explicit HostArray(size_t n) : p(new T[std::max<size_t>(n, 1)]) {}
+    T &operator[](size_t i) { return p[i]; }
+    const T &operator[](size_t i) const { return p[i]; }
+};
 
 // Chemically equivalent atom pairs used by match mode 1 (see the oracle's
 // same_position rule; pinned by the reference fixture for ASN OD1/ND2).
@@ -413,7 +429,11 @@ pjg_status pjg_templates_create(const pjg_template_set *set, pjg_templates **out
     std::vector<int32_t> sig(A), key(A);
     std::vector<double> pos(3 * (size_t)A), weight(A);
     // signatures
-    std::map<std::vector<uint32_t>, int> sig_ids;
+    // signature ids by the bytes of (code, name count, names, residue names)
+    std::unordered_map<std::string, int> sig_ids;
+    sig_ids.reserve((size_t)A);
+    std::vector<uint32_t> names, res, keyv;
+    std::string keys;
     std::vector<int32_t> s_code, s_rule, s_main, s_nb{0}, s_rb{0}, s_pb{0};
     std::vector<uint32_t> s_names, s_res, s_pres, s_pname;
     for (int t = 0; t < T; t++) {
@@ -435,22 +455,24 @@ pjg_status pjg_templates_create(const pjg_template_set *set, pjg_templates **out
             delete h;
             return fail(PJG_ERR_INVALID, "template atom %d: invalid match mode %d", a, code);
         }
-        std::vector<uint32_t> names, res;
+        names.clear();
+        res.clear();
         for (int q = set->name_offset[a]; q < set->name_offset[a + 1]; q++) names.push_back(pack_upper(set->names + 4 * q));
         for (int q = set->resname_offset[a]; q < set->resname_offset[a + 1]; q++) {
             uint32_t r = pack_upper(set->resnames + 4 * q);
             if (std::find(res.begin(), res.end(), r) == res.end()) res.push_back(r);
         }
-        std::vector<uint32_t> keyv;
+        keyv.clear();
         keyv.push_back((uint32_t)code);
         keyv.push_back((uint32_t)names.size());
         keyv.insert(keyv.end(), names.begin(), names.end());
         keyv.insert(keyv.end(), res.begin(), res.end());
-        auto it = sig_ids.find(keyv);
+        keys.assign(reinterpret_cast<const char *>(keyv.data()), keyv.size() * sizeof(uint32_t));
+        auto it = sig_ids.find(keys);
         int id;
         if (it == sig_ids.end()) {
             id = (int)s_code.size();
-            sig_ids.emplace(keyv, id);
+            sig_ids.emplace(keys, id);
             int mode = code >= 100 ? code - 100 : code;
             int rule = mode == -1 ? RULE_ANY : mode == 1 ? RULE_NAME_OR_PARTNER : mode == 2 ? RULE_NAME_OR_MAINCHAIN
                      : mode == 3 ? RULE_ELEMENT : RULE_NAME;
@@ -567,9 +589,10 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
     h->N = N;
     std::vector<int64_t> base(std::max(S, 0));
     std::vector<int32_t> count(std::max(S, 0));
-    std::vector<float4> xyz32(N);
-    std::vector<uint32_t> name(N), resname(N);
-    std::vector<int32_t> sorted(N), bucket_begin{0}, bucket_lo, bucket_hi;
+    HostArray<float4> xyz32((size_t)N);
+    HostArray<uint32_t> name((size_t)N), resname((size_t)N);
+    HostArray<int32_t> sorted((size_t)N);
+    std::vector<int32_t> bucket_begin{0}, bucket_lo, bucket_hi;
     std::vector<uint32_t> bucket_name;
     for (int s = 0; s < S; s++) {
         int64_t b0 = set->atom_offset[s], b1 = set->atom_offset[s + 1];
@@ -581,12 +604,6 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
             delete h;
             return fail(PJG_ERR_INVALID, "structure %d too large", s);
         }
-        for (int64_t i = 3 * b0; i < 3 * b1; i++)
-            if (!std::isfinite(set->xyz[i])) {
-                delete h;
-                return fail(PJG_ERR_INVALID, "structure %d atom %lld: non-finite coordinate", s,
-                            (long long)(i / 3 - b0));
-            }
         base[s] = b0;
         count[s] = (int)(b1 - b0);
         h->max_atoms = std::max(h->max_atoms, count[s]);
@@ -598,12 +615,17 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
         std::vector<uint32_t> name;
         std::vector<int32_t> lo, hi;
         double radius = 0.0;
+        int64_t bad = -1;  // first atom with a non-finite coordinate
     };
     std::vector<Buckets> bk(std::max(S, 0));
     auto prepare = [&](int s) {
         const int64_t b0 = base[s];
         const int n = count[s];
         Buckets &B = bk[s];
+        for (int i = 0; i < n && B.bad < 0; i++)
+            for (int d = 0; d < 3; d++)
+                if (!std::isfinite(set->xyz[3 * (b0 + i) + d])) B.bad = i;
+        if (B.bad >= 0) return;
         double c[3] = {0, 0, 0};
         for (int i = 0; i < n; i++)
             for (int d = 0; d < 3; d++) c[d] += set->xyz[3 * (b0 + i) + d];
@@ -621,18 +643,42 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
             name[a] = pack_upper(set->name + 4 * a);
             resname[a] = pack_upper(set->resname + 4 * a);
         }
-        // ResIndex: stable order by (residue name, serial)
+        // ResIndex: stable order by (residue name, serial) -- a counting
+        // sort by residue name (in byte order of the upper-cased name), then
+        // a stable sort by serial of each bucket not already in serial order
         std::vector<int32_t> idx(n);
-        std::iota(idx.begin(), idx.end(), 0);
-        auto bigkey = [&](int i) {
-            const uint8_t *r = set->resname + 4 * (b0 + i);
-            return ((uint32_t)up(r[0]) << 24) | ((uint32_t)up(r[1]) << 16) | ((uint32_t)up(r[2]) << 8) | up(r[3]);
-        };
-        std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) {
-            uint32_t kx = bigkey(x), ky = bigkey(y);
-            if (kx != ky) return kx < ky;
-            return set->serial[b0 + x] < set->serial[b0 + y];
-        });
+        {
+            std::vector<std::pair<uint32_t, int32_t>> kinds;  // big-endian name, count
+            std::vector<int32_t> kind(n);
+            for (int i = 0; i < n; i++) {
+                const uint8_t *r = set->resname + 4 * (b0 + i);
+                const uint32_t k = ((uint32_t)up(r[0]) << 24) | ((uint32_t)up(r[1]) << 16) |
+                                   ((uint32_t)up(r[2]) << 8) | up(r[3]);
+                int q = 0;
+                while (q < (int)kinds.size() && kinds[q].first != k) q++;
+                if (q == (int)kinds.size()) kinds.push_back({k, 0});
+                kinds[q].second++;
+                kind[i] = q;
+            }
+            std::vector<int> by(kinds.size());
+            std::iota(by.begin(), by.end(), 0);
+            std::sort(by.begin(), by.end(), [&](int x, int y) { return kinds[x].first < kinds[y].first; });
+            std::vector<int32_t> start(kinds.size());
+            int acc = 0;
+            for (int q : by) {
+                start[q] = acc;
+                acc += kinds[q].second;
+            }
+            std::vector<int32_t> fill = start;
+            for (int i = 0; i < n; i++) idx[fill[kind[i]]++] = i;
+            const int32_t *ser = set->serial + b0;
+            for (size_t q = 0; q < kinds.size(); q++) {
+                int32_t *lo = idx.data() + start[q], *hi = lo + kinds[q].second;
+                bool ordered = true;
+                for (int32_t *x = lo; x + 1 < hi && ordered; x++) ordered = ser[x[0]] <= ser[x[1]];
+                if (!ordered) std::stable_sort(lo, hi, [&](int x, int y) { return ser[x] < ser[y]; });
+            }
+        }
         for (int i = 0; i < n; i++) {
             sorted[b0 + i] = idx[i];
             uint32_t rn = resname[b0 + idx[i]];
@@ -655,6 +701,11 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
         worker();
         for (auto &th : pool) th.join();
     }
+    for (int s = 0; s < S; s++)
+        if (bk[s].bad >= 0) {
+            delete h;
+            return fail(PJG_ERR_INVALID, "structure %d atom %lld: non-finite coordinate", s, (long long)bk[s].bad);
+        }
     for (int s = 0; s < S; s++) {
         const Buckets &B = bk[s];
         h->max_radius = std::max(h->max_radius, B.radius);
@@ -669,10 +720,10 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
         e = cudaMemcpy(h->d_xyz64, set->xyz, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = upload(&h->d_atom_base, base);
     if (e == cudaSuccess) e = upload(&h->d_atom_count, count);
-    if (e == cudaSuccess) e = upload(&h->d_xyz32, xyz32);
-    if (e == cudaSuccess) e = upload(&h->d_name, name);
-    if (e == cudaSuccess) e = upload(&h->d_resname, resname);
-    if (e == cudaSuccess) e = upload(&h->d_sorted, sorted);
+    if (e == cudaSuccess) e = upload(&h->d_xyz32, xyz32.p.get(), (size_t)N);
+    if (e == cudaSuccess) e = upload(&h->d_name, name.p.get(), (size_t)N);
+    if (e == cudaSuccess) e = upload(&h->d_resname, resname.p.get(), (size_t)N);
+    if (e == cudaSuccess) e = upload(&h->d_sorted, sorted.p.get(), (size_t)N);
     if (e == cudaSuccess) e = upload(&h->d_bucket_begin, bucket_begin);
     if (e == cudaSuccess) e = upload(&h->d_bucket_name, bucket_name);
     if (e == cudaSuccess) e = upload(&h->d_bucket_lo, bucket_lo);
