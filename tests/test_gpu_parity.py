@@ -394,9 +394,10 @@ def test_leaf_arrays_grow(monkeypatch, levels):
 
 
 def test_large_result_copy_out():
-    """Results of several MiB come back through the threaded, staged copy
-    (one host thread per MiB, pinned double buffers): every field matches the
-    oracle, and a second copy of the same results is identical."""
+    """Results of several MiB come back through the threaded copy (one host
+    thread per MiB, each touching then copying its range of the caller's
+    arrays): every field matches the oracle, and a second copy of the same
+    results is identical."""
     from pyjess_gb300 import workloads as W
 
     wl = W.config(3, n_structures=60, n_templates=600)
