@@ -170,6 +170,8 @@ struct pjg_structures {
     int32_t *d_bucket_begin = nullptr, *d_bucket_lo = nullptr, *d_bucket_hi = nullptr;
     uint32_t *d_bucket_name = nullptr;
     uint32_t *d_lrank = nullptr, *d_urank = nullptr;  // [3][N] axis ranks
+    int32_t *d_nh_begin = nullptr, *d_nh_count = nullptr;  // name histogram per bucket
+    uint32_t *d_nh_name = nullptr;
     int device = 0;
 };
 
@@ -544,6 +546,8 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
     struct Buckets {
         std::vector<uint32_t> name;
         std::vector<int32_t> lo, hi;
+        std::vector<uint32_t> hname;  // distinct atom names of each bucket, sorted
+        std::vector<int32_t> hcount, hbegin{0};
         double radius = 0.0;
         int64_t bad = -1;  // first atom with a non-finite coordinate
     };
@@ -619,6 +623,21 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
             }
         }
         if (n > 0) B.hi.push_back(n);
+        // per bucket: its distinct atom names and their counts
+        std::vector<uint32_t> nm;
+        for (size_t k = 0; k < B.name.size(); k++) {
+            nm.clear();
+            for (int i = B.lo[k]; i < B.hi[k]; i++) nm.push_back(name[b0 + idx[i]]);
+            std::sort(nm.begin(), nm.end());
+            for (size_t i = 0; i < nm.size(); i++) {
+                if (i == 0 || nm[i] != nm[i - 1]) {
+                    B.hname.push_back(nm[i]);
+                    B.hcount.push_back(0);
+                }
+                B.hcount.back()++;
+            }
+            B.hbegin.push_back((int32_t)B.hname.size());
+        }
     };
     {
         const int nthreads = (int)std::max<unsigned>(1, std::min<unsigned>(32, std::thread::hardware_concurrency()));
@@ -636,6 +655,14 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
             delete h;
             return fail(PJG_ERR_INVALID, "structure %d atom %lld: non-finite coordinate", s, (long long)bk[s].bad);
         }
+    std::vector<int32_t> nh_begin{0}, nh_count;
+    std::vector<uint32_t> nh_name;
+    for (int s = 0; s < S; s++) {
+        const Buckets &B = bk[s];
+        for (size_t k = 0; k + 1 < B.hbegin.size(); k++) nh_begin.push_back((int32_t)nh_name.size() + B.hbegin[k + 1]);
+        nh_name.insert(nh_name.end(), B.hname.begin(), B.hname.end());
+        nh_count.insert(nh_count.end(), B.hcount.begin(), B.hcount.end());
+    }
     for (int s = 0; s < S; s++) {
         const Buckets &B = bk[s];
         h->max_radius = std::max(h->max_radius, B.radius);
@@ -658,6 +685,9 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
     if (e == cudaSuccess) e = upload(&h->d_bucket_name, bucket_name);
     if (e == cudaSuccess) e = upload(&h->d_bucket_lo, bucket_lo);
     if (e == cudaSuccess) e = upload(&h->d_bucket_hi, bucket_hi);
+    if (e == cudaSuccess) e = upload(&h->d_nh_begin, nh_begin);
+    if (e == cudaSuccess) e = upload(&h->d_nh_name, nh_name);
+    if (e == cudaSuccess) e = upload(&h->d_nh_count, nh_count);
     if (e == cudaSuccess) {
         // axis ranks of every atom (the leaf-order sorted-axis path)
         const size_t n3 = 3 * (size_t)std::max<int64_t>(N, 1);
@@ -690,7 +720,7 @@ void pjg_structures_destroy(pjg_structures *h) {
     if (!h) return;
     void *ptrs[] = {h->d_atom_base, h->d_atom_count, h->d_xyz64, h->d_xyz32, h->d_name, h->d_resname,
                     h->d_sorted, h->d_bucket_begin, h->d_bucket_name, h->d_bucket_lo, h->d_bucket_hi,
-                    h->d_lrank, h->d_urank};
+                    h->d_lrank, h->d_urank, h->d_nh_begin, h->d_nh_name, h->d_nh_count};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete h;
@@ -878,7 +908,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
         CUDA_TRY(dalloc(d_totals, (size_t)S, st));
         ChunkView cv{S, sp->d_atom_base, sp->d_atom_count, sp->d_xyz64, sp->d_xyz32, sp->d_name, sp->d_resname,
                      sp->d_sorted, sp->d_bucket_begin, sp->d_bucket_name, sp->d_bucket_lo, sp->d_bucket_hi,
-                     sp->N, sp->d_lrank, sp->d_urank};
+                     sp->N, sp->d_lrank, sp->d_urank, sp->d_nh_begin, sp->d_nh_name, sp->d_nh_count};
         SigView sv{G, tp->d_code, tp->d_rule, tp->d_mainchain, tp->d_name_begin, tp->d_names, tp->d_res_begin,
                    tp->d_resnames, tp->d_partner_begin, tp->d_partner_res, tp->d_partner_name};
         int blocks = (int)std::min<int64_t>((W + 7) / 8, (int64_t)sm_count() * 32);
@@ -939,7 +969,8 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             const int64_t Wc = (int64_t)Sc * G;
             ChunkView cv{Sc, sp->d_atom_base + s0, sp->d_atom_count + s0, sp->d_xyz64, sp->d_xyz32, sp->d_name,
                          sp->d_resname, sp->d_sorted, sp->d_bucket_begin + s0, sp->d_bucket_name, sp->d_bucket_lo,
-                         sp->d_bucket_hi, sp->N, sp->d_lrank, sp->d_urank};
+                         sp->d_bucket_hi, sp->N, sp->d_lrank, sp->d_urank, sp->d_nh_begin, sp->d_nh_name,
+                         sp->d_nh_count};
             SigView sv{G, tp->d_code, tp->d_rule, tp->d_mainchain, tp->d_name_begin, tp->d_names, tp->d_res_begin,
                        tp->d_resnames, tp->d_partner_begin, tp->d_partner_res, tp->d_partner_name};
             int32_t *cnt_c = d_count.p + (int64_t)s0 * G;

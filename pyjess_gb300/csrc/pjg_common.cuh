@@ -71,6 +71,11 @@ struct ChunkView {
     int64_t n_atoms;              // atoms of the whole structure set
     const uint32_t *lrank;        // [3][n_atoms] strict-lower axis rank
     const uint32_t *urank;        // [3][n_atoms] unique axis rank
+    // distinct atom names of each residue bucket (global bucket index) with
+    // their atom counts: [nh_begin[b], nh_begin[b + 1]) into nh_name/nh_count
+    const int32_t *nh_begin;
+    const uint32_t *nh_name;
+    const int32_t *nh_count;
 };
 
 struct SigView {

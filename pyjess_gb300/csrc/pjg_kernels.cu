@@ -242,6 +242,56 @@ __global__ void k_candidates(ChunkView cv, SigView sv, int32_t *count, int32_t *
 }
 
 
+// List lengths without scanning atoms.  Whether an atom joins a list
+// depends only on its (residue name, atom name) and the signature, so a
+// list's length is the sum, over the distinct atom names of each residue
+// bucket it walks, of the counts of the names that pass the rule (the
+// molecule-order codes walk every bucket of the structure).  Warp per
+// (structure, signature), lanes over a bucket's distinct names.
+__global__ void k_candidate_counts(ChunkView cv, SigView sv, int32_t *count, int32_t *scanned) {
+    const int lane = lane_id();
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t total = (int64_t)cv.n_structures * sv.n_sigs;
+    for (int64_t w = warp; w < total; w += nwarps) {
+        const int s = (int)(w / sv.n_sigs);
+        const int g = (int)(w % sv.n_sigs);
+        const int code = sv.code[g];
+        const SigRegs sr = load_sig(sv, g);
+        const int b0 = cv.bucket_begin[s], b1 = cv.bucket_begin[s + 1];
+        int cnt = 0, sc = 0;
+        auto bucket_sum = [&](int b, uint32_t rn) {
+            for (int q = cv.nh_begin[b] + lane; q < cv.nh_begin[b + 1]; q += 32)
+                if (sig_match_regs(sv, sr, cv.nh_name[q], rn)) cnt += cv.nh_count[q];
+        };
+        if (code >= -1 && code <= 8) {
+            for (int ri = sv.res_begin[g]; ri < sv.res_begin[g + 1]; ri++) {
+                const uint32_t rn = sv.resnames[ri];
+                int found = -1;
+                for (int bb = b0; bb < b1; bb += 32) {
+                    const int b = bb + lane;
+                    const unsigned m = __ballot_sync(FULL_MASK, b < b1 && cv.bucket_name[b] == rn);
+                    if (m) {
+                        found = bb + __ffs(m) - 1;
+                        break;
+                    }
+                }
+                if (found < 0) continue;
+                bucket_sum(found, rn);
+                sc += cv.bucket_hi[found] - cv.bucket_lo[found];
+            }
+        } else {
+            for (int b = b0; b < b1; b++) bucket_sum(b, cv.bucket_name[b]);
+            sc = cv.atom_count[s];
+        }
+        for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(FULL_MASK, cnt, o);
+        if (lane == 0) {
+            count[w] = cnt;
+            scanned[w] = sc;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Exclusive scan (int32 -> int64), three phases.
 
@@ -2678,7 +2728,7 @@ void launch_params(cudaStream_t st, int n_templates, const int32_t *atom_begin, 
 void launch_candidates(cudaStream_t st, int blocks, bool fill, const ChunkView &cv, const SigView &sv,
                        int32_t *count, int32_t *scanned, const int64_t *offset, int32_t *cand_atom) {
     if (fill) k_candidates<true><<<blocks, 256, 0, st>>>(cv, sv, count, scanned, offset, cand_atom);
-    else k_candidates<false><<<blocks, 256, 0, st>>>(cv, sv, count, scanned, offset, cand_atom);
+    else k_candidate_counts<<<blocks, 256, 0, st>>>(cv, sv, count, scanned);
 }
 
 void launch_scan_tiles_i32(cudaStream_t st, const int32_t *in, int64_t n, int64_t *out, int64_t *tile_sums) {
