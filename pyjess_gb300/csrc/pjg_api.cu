@@ -172,6 +172,7 @@ struct pjg_structures {
     uint32_t *d_lrank = nullptr, *d_urank = nullptr;  // [3][N] axis ranks
     int32_t *d_nh_begin = nullptr, *d_nh_count = nullptr;  // name histogram per bucket
     uint32_t *d_nh_name = nullptr;
+    uint8_t *d_name_id = nullptr;                      // name index within the bucket
     int device = 0;
 };
 
@@ -524,6 +525,7 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
     HostArray<float4> xyz32((size_t)N);
     HostArray<uint32_t> name((size_t)N), resname((size_t)N);
     HostArray<int32_t> sorted((size_t)N);
+    HostArray<uint8_t> name_id((size_t)N);
     std::vector<int32_t> bucket_begin{0}, bucket_lo, bucket_hi;
     std::vector<uint32_t> bucket_name;
     for (int s = 0; s < S; s++) {
@@ -629,6 +631,7 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
             nm.clear();
             for (int i = B.lo[k]; i < B.hi[k]; i++) nm.push_back(name[b0 + idx[i]]);
             std::sort(nm.begin(), nm.end());
+            const size_t h0 = B.hname.size();
             for (size_t i = 0; i < nm.size(); i++) {
                 if (i == 0 || nm[i] != nm[i - 1]) {
                     B.hname.push_back(nm[i]);
@@ -637,6 +640,12 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
                 B.hcount.back()++;
             }
             B.hbegin.push_back((int32_t)B.hname.size());
+            for (int i = B.lo[k]; i < B.hi[k]; i++) {
+                const int a = idx[i];
+                const size_t id = std::lower_bound(B.hname.begin() + h0, B.hname.end(), name[b0 + a]) -
+                                  (B.hname.begin() + h0);
+                name_id[b0 + a] = (uint8_t)std::min<size_t>(id, 255);
+            }
         }
     };
     {
@@ -688,6 +697,7 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
     if (e == cudaSuccess) e = upload(&h->d_nh_begin, nh_begin);
     if (e == cudaSuccess) e = upload(&h->d_nh_name, nh_name);
     if (e == cudaSuccess) e = upload(&h->d_nh_count, nh_count);
+    if (e == cudaSuccess) e = upload(&h->d_name_id, name_id.p.get(), (size_t)N);
     if (e == cudaSuccess) {
         // axis ranks of every atom (the leaf-order sorted-axis path)
         const size_t n3 = 3 * (size_t)std::max<int64_t>(N, 1);
@@ -720,7 +730,7 @@ void pjg_structures_destroy(pjg_structures *h) {
     if (!h) return;
     void *ptrs[] = {h->d_atom_base, h->d_atom_count, h->d_xyz64, h->d_xyz32, h->d_name, h->d_resname,
                     h->d_sorted, h->d_bucket_begin, h->d_bucket_name, h->d_bucket_lo, h->d_bucket_hi,
-                    h->d_lrank, h->d_urank, h->d_nh_begin, h->d_nh_name, h->d_nh_count};
+                    h->d_lrank, h->d_urank, h->d_nh_begin, h->d_nh_name, h->d_nh_count, h->d_name_id};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete h;
@@ -908,7 +918,8 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
         CUDA_TRY(dalloc(d_totals, (size_t)S, st));
         ChunkView cv{S, sp->d_atom_base, sp->d_atom_count, sp->d_xyz64, sp->d_xyz32, sp->d_name, sp->d_resname,
                      sp->d_sorted, sp->d_bucket_begin, sp->d_bucket_name, sp->d_bucket_lo, sp->d_bucket_hi,
-                     sp->N, sp->d_lrank, sp->d_urank, sp->d_nh_begin, sp->d_nh_name, sp->d_nh_count};
+                     sp->N, sp->d_lrank, sp->d_urank, sp->d_nh_begin, sp->d_nh_name, sp->d_nh_count,
+                     sp->d_name_id};
         SigView sv{G, tp->d_code, tp->d_rule, tp->d_mainchain, tp->d_name_begin, tp->d_names, tp->d_res_begin,
                    tp->d_resnames, tp->d_partner_begin, tp->d_partner_res, tp->d_partner_name};
         int blocks = (int)std::min<int64_t>((W + 7) / 8, (int64_t)sm_count() * 32);
@@ -970,7 +981,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             ChunkView cv{Sc, sp->d_atom_base + s0, sp->d_atom_count + s0, sp->d_xyz64, sp->d_xyz32, sp->d_name,
                          sp->d_resname, sp->d_sorted, sp->d_bucket_begin + s0, sp->d_bucket_name, sp->d_bucket_lo,
                          sp->d_bucket_hi, sp->N, sp->d_lrank, sp->d_urank, sp->d_nh_begin, sp->d_nh_name,
-                         sp->d_nh_count};
+                         sp->d_nh_count, sp->d_name_id};
             SigView sv{G, tp->d_code, tp->d_rule, tp->d_mainchain, tp->d_name_begin, tp->d_names, tp->d_res_begin,
                        tp->d_resnames, tp->d_partner_begin, tp->d_partner_res, tp->d_partner_name};
             int32_t *cnt_c = d_count.p + (int64_t)s0 * G;

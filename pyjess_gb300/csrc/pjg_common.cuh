@@ -76,6 +76,8 @@ struct ChunkView {
     const int32_t *nh_begin;
     const uint32_t *nh_name;
     const int32_t *nh_count;
+    const uint8_t *name_id;       // per atom: index of its name among its
+                                  // bucket's distinct names (255 past 254)
 };
 
 struct SigView {

@@ -229,7 +229,33 @@ __global__ void k_candidates(ChunkView cv, SigView sv, int32_t *count, int32_t *
                     }
                 }
                 if (found < 0) continue;
-                visit(cv.bucket_lo[found], cv.bucket_hi[found], true, rn);
+                // the rule over the bucket's distinct atom names, as a bit
+                // mask indexed by each atom's name index: a bit test per
+                // atom, and no scan at all of a bucket with no passing name
+                const int nb = cv.nh_begin[found], nd = cv.nh_begin[found + 1] - nb;
+                if (nd > 64) {
+                    visit(cv.bucket_lo[found], cv.bucket_hi[found], true, rn);
+                    continue;
+                }
+                const bool m0 = lane < nd && sig_match_regs(sv, sr, cv.nh_name[nb + lane], rn);
+                const bool m1 = lane + 32 < nd && sig_match_regs(sv, sr, cv.nh_name[nb + 32 + lane], rn);
+                const uint64_t mask =
+                    (uint64_t)__ballot_sync(FULL_MASK, m0) | ((uint64_t)__ballot_sync(FULL_MASK, m1) << 32);
+                const int p_lo = cv.bucket_lo[found], p_hi = cv.bucket_hi[found];
+                sc += p_hi - p_lo;
+                if (!mask) continue;
+                for (int p0 = p_lo; p0 < p_hi; p0 += 32) {
+                    const int p = p0 + lane;
+                    int atom = 0;
+                    bool ok = false;
+                    if (p < p_hi) {
+                        atom = cv.sorted[abase + p];
+                        ok = (mask >> cv.name_id[abase + atom]) & 1ull;
+                    }
+                    const unsigned m = __ballot_sync(FULL_MASK, ok);
+                    if (FILL && ok) cand_atom[out0 + cnt + __popc(m & ((1u << lane) - 1u))] = atom;
+                    cnt += __popc(m);
+                }
             }
         } else {
             visit(0, nat, false, 0u);
