@@ -1680,14 +1680,15 @@ __device__ double lane_rmsd(int n, const int32_t *atoms, const double *xyz, cons
 // first over tiles, breadth first inside a tile), which reproduces that
 // order.
 //
-// Two expansion modes per level.  Block mode (lists of 32 or more): one
-// parent at a time; its chain of atoms, key bits and FP32 annulus bounds
-// sit in shared memory and are read by all lanes as broadcasts; the
-// parent's join box (intersection of its annulus boxes) culls whole blocks
-// of 32 consecutive leaves by their bounding boxes, and the 32 candidates
-// of each surviving block are tested by the 32 lanes.  Product mode (short
+// Two expansion modes per level.  Block mode (lists of PJG_BLOCK_MIN = 64
+// or more): one parent at a time; its chain of atoms, key bits and FP32
+// annulus bounds sit in shared memory and are read by all lanes as
+// broadcasts; the parent's join box (intersection of its annulus boxes)
+// culls whole blocks of 32 consecutive leaves by their bounding boxes, the
+// leaves of the surviving blocks inside the join box are queued, and the
+// full tests run on batches of 32 queued leaves.  Product mode (shorter
 // lists): lanes take consecutive (parent, candidate) positions of the
-// flattened product so small lists still fill the warp.
+// flattened product, so a warp step covers several parents.
 
 struct PairState {
     int64_t lvl_off[32];
@@ -2181,7 +2182,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                 int cr = 0;
                 int my_parent = 0;      // product mode: this lane's parent entry
                 int32_t chainpos[32];   // product mode: this lane's parent chain
-                if (mc >= 32) {
+                if (mc >= PJG_BLOCK_MIN) {
                     // ---------------- block mode ----------------
                     if (!last && cap - ccnt < 32) {
                         __syncwarp();
@@ -2509,7 +2510,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                     my_parent = p;
                 }
                 // ---- children / complete rows
-                const bool block_mode = mc >= 32;
+                const bool block_mode = mc >= PJG_BLOCK_MIN;
                 unsigned m = __ballot_sync(FULL_MASK, pass);
                 if (last) {
                     if (block_mode) {

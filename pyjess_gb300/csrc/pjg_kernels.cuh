@@ -22,6 +22,11 @@ constexpr int SEARCH_WARPS = PJG_SEARCH_WARPS;  // warps per block of k_search
 #ifndef PJG_SEARCH_MIN_BLOCKS
 #define PJG_SEARCH_MIN_BLOCKS 2
 #endif
+// shortest child list k_search expands one parent at a time in block mode
+// (shorter lists: product mode, lanes over (parent, candidate) pairs)
+#ifndef PJG_BLOCK_MIN
+#define PJG_BLOCK_MIN 64
+#endif
 constexpr int LEAF_WARPS = 4;          // warps per block of k_leaf_order
 constexpr int LEAF_FAST_MAX = 192;     // capacity of the rank method's buffers
 constexpr int LEAF_RANK_MAX = 192;     // default: longest list ordered by the rank method
