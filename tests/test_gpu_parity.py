@@ -410,3 +410,31 @@ def test_large_result_copy_out():
     for k in a:
         if hasattr(a[k], "nbytes"):
             assert np.array_equal(a[k], b[k]), k
+
+
+def test_rmsd_max_error_per_config(capsys):
+    """Largest |rmsd_gpu - rmsd_oracle| per configuration (reduced sizes for
+    configs 2-4), printed, and within RMSD_TOL wherever the oracle's formula
+    is well conditioned (check_rmsd)."""
+    from pyjess_gb300 import workloads as W
+
+    cases = [
+        ("config 0", W.config(0), {}),
+        ("config 1", W.config(1), {}),
+        ("config 2 (40 x 300)", W.config(2, n_structures=40, n_templates=300), {}),
+        ("config 3 (40 x 300)", W.config(3, n_structures=40, n_templates=300), {}),
+        ("config 4 (3 x 6, best_match=False)", W.config(4, n_structures=3, n_templates=6, residues=(300, 500)),
+         {"max_candidates": 50}),
+        ("config 4 (3 x 6, best_match=True)", W.config(4, n_structures=3, n_templates=6, residues=(300, 500)),
+         {"max_candidates": 50, "best_match": True}),
+    ]
+    lines = []
+    for label, wl, extra in cases:
+        p = dict(wl.params)
+        p.update(extra)
+        res, ref = compare(wl.templates, wl.structures, mode="fp32", **p)
+        g = res.arrays()
+        err = float(np.abs(g["rmsd"] - ref["hits"]["rmsd"]).max()) if g["count"] else 0.0
+        lines.append(f"{label}: {g['count']} hits, identical; max |rmsd - oracle| = {err:.3g} A")
+    with capsys.disabled():
+        print("\n" + "\n".join(lines))
