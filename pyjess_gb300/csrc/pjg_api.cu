@@ -892,9 +892,14 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
 
     {
         // guard band: the requested width, widened if the FP32 rounding bound
-        // of the largest structure needs more (error of a squared distance is
-        // below 2^-24 (10.4 R d + 4 d^2) for coordinates within R of the
-        // centroid; see DESIGN)
+        // of the largest structure needs more.  Coordinates are stored
+        // relative to the structure's centroid, so each is within about
+        // 2^-24 R of its FP64 value (R = largest distance from the centroid)
+        // and the error of an FP32 squared distance d^2 is below
+        // 2^-24 (10.4 R d + 4 d^2); a band g in distance covers a band of
+        // about 2 b g in squared distance at radius b, so g must exceed
+        // 2^-24 (5.2 R + 2 b), with b at most 2 R + 1 for any pair of atoms
+        // (plus the tolerance) inside a structure.
         double g = P->guard_band > 0 ? P->guard_band : 1e-4;
         double bound = 2.0 * std::ldexp(1.0, -24) * (5.2 * sp->max_radius + 2.0 * (2.0 * sp->max_radius + 1.0));
         if (bound > g) g = bound;
