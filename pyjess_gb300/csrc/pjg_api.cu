@@ -1,18 +1,27 @@
 // pjg_api.cu — C ABI of libpjg (include/pjg.h): template / structure
-// upload, the query pipeline and its host-side automaton.
+// upload and the query pipeline.
 //
-// Pipeline of pjg_query (all on one CUDA stream owned by the call):
+// Pipeline of pjg_query (on one CUDA stream owned by the call):
 //   k_params                      annulus radii for the query's r and s
-//   k_candidates<count>           |C| and |R| of every (structure, signature)
+//   k_candidate_counts            |C| and |R| of every (structure, signature)
 //   k_struct_totals               candidate entries per structure
 //   per structure chunk (bounded entry budget):
-//     k_scan_*                    list offsets
-//     k_candidates<fill>          lists in candidate order
-//     k_leaf_order                lists in kd leaf order
-//     k_search                    complete assignments, ordered per pair
-//     k_superpose                 rmsd / rotation / centroids, rmsd filter
-//   host: order by (structure, template descending, ordinal) and replay the
-//   Query.__next__ automaton (src/pyjess/_jess.pyx:2197-2283) per pair.
+//     k_scan_*, k_block_counts    list offsets, blocks of 32 leaves
+//     k_candidates                lists in candidate order
+//     k_demand_levels             requests the lists of the first levels
+//     k_leaf_order, k_leaf_sorted, k_leaf_exact, k_mark_ordered
+//                                 requested lists in kd leaf order
+//     k_search                    complete assignments, ordered per pair;
+//                                 pairs that reach a list without leaf order
+//                                 request it and are suspended, the lists are
+//                                 ordered (as above) and a second k_search
+//                                 round resumes them
+//     k_superpose                 rmsd / rotation / centroids per row
+//     k_order_counts, k_automaton, k_gather_hits
+//                                 rows in (structure, template descending,
+//                                 ordinal) order, the Query.__next__
+//                                 automaton (src/pyjess/_jess.pyx:2197-2283)
+//                                 per pair, hits and warnings compacted
 
 #include <cuda_runtime.h>
 

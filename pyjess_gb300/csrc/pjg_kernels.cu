@@ -175,11 +175,9 @@ __device__ __forceinline__ bool sig_match_regs(const SigView &sv, const SigRegs 
     return false;
 }
 
-// One warp per (structure, signature).  FILL=false: lengths and scanned
-// counts; FILL=true: write the list in candidate order.
-template <bool FILL>
-__global__ void k_candidates(ChunkView cv, SigView sv, int32_t *count, int32_t *scanned,
-                             const int64_t *offset, int32_t *cand_atom) {
+// One warp per (structure, signature): the list's atoms in candidate order
+// at offset[w] (its length comes from k_candidate_counts).
+__global__ void k_candidates(ChunkView cv, SigView sv, const int64_t *offset, int32_t *cand_atom) {
     int lane = lane_id();
     int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -191,8 +189,8 @@ __global__ void k_candidates(ChunkView cv, SigView sv, int32_t *count, int32_t *
         const SigRegs sr = load_sig(sv, g);
         int64_t abase = cv.atom_base[s];
         int nat = cv.atom_count[s];
-        int cnt = 0, sc = 0;
-        int64_t out0 = FILL ? offset[w] : 0;
+        int cnt = 0;
+        const int64_t out0 = offset[w];
         // atoms p_lo..p_hi of the residue bucket `rn` (via_sorted) or of
         // the molecule in order
         auto visit = [&](int p_lo, int p_hi, bool via_sorted, uint32_t rn) {
@@ -207,13 +205,9 @@ __global__ void k_candidates(ChunkView cv, SigView sv, int32_t *count, int32_t *
                     ok = sig_match_regs(sv, sr, cv.name[abase + atom], res);
                 }
                 unsigned m = __ballot_sync(FULL_MASK, ok);
-                if (FILL && ok) {
-                    int pos = cnt + __popc(m & ((1u << lane) - 1u));
-                    cand_atom[out0 + pos] = atom;
-                }
+                if (ok) cand_atom[out0 + cnt + __popc(m & ((1u << lane) - 1u))] = atom;
                 cnt += __popc(m);
             }
-            sc += p_hi - p_lo;
         };
         if (code >= -1 && code <= 8) {
             int b0 = cv.bucket_begin[s], b1 = cv.bucket_begin[s + 1];
@@ -242,7 +236,6 @@ __global__ void k_candidates(ChunkView cv, SigView sv, int32_t *count, int32_t *
                 const uint64_t mask =
                     (uint64_t)__ballot_sync(FULL_MASK, m0) | ((uint64_t)__ballot_sync(FULL_MASK, m1) << 32);
                 const int p_lo = cv.bucket_lo[found], p_hi = cv.bucket_hi[found];
-                sc += p_hi - p_lo;
                 if (!mask) continue;
                 for (int p0 = p_lo; p0 < p_hi; p0 += 32) {
                     const int p = p0 + lane;
@@ -253,16 +246,12 @@ __global__ void k_candidates(ChunkView cv, SigView sv, int32_t *count, int32_t *
                         ok = (mask >> cv.name_id[abase + atom]) & 1ull;
                     }
                     const unsigned m = __ballot_sync(FULL_MASK, ok);
-                    if (FILL && ok) cand_atom[out0 + cnt + __popc(m & ((1u << lane) - 1u))] = atom;
+                    if (ok) cand_atom[out0 + cnt + __popc(m & ((1u << lane) - 1u))] = atom;
                     cnt += __popc(m);
                 }
             }
         } else {
             visit(0, nat, false, 0u);
-        }
-        if (!FILL && lane == 0) {
-            count[w] = cnt;
-            scanned[w] = sc;
         }
     }
 }
@@ -2754,7 +2743,7 @@ void launch_params(cudaStream_t st, int n_templates, const int32_t *atom_begin, 
 
 void launch_candidates(cudaStream_t st, int blocks, bool fill, const ChunkView &cv, const SigView &sv,
                        int32_t *count, int32_t *scanned, const int64_t *offset, int32_t *cand_atom) {
-    if (fill) k_candidates<true><<<blocks, 256, 0, st>>>(cv, sv, count, scanned, offset, cand_atom);
+    if (fill) k_candidates<<<blocks, 256, 0, st>>>(cv, sv, offset, cand_atom);
     else k_candidate_counts<<<blocks, 256, 0, st>>>(cv, sv, count, scanned);
 }
 
