@@ -169,3 +169,211 @@ class PDBMoleculeWriter:
                 f.write(f"{'HEADER':<6}{'':4}{name:40}{date:9}{'':3}{id_:4}\n")
             for atom in molecule:
                 atom.dump(f, format="pdb")
+
+
+# ---------------------------------------------------------------------------
+# mmCIF input.  The reference reads mmCIF through the gemmi module
+# (``CIFMoleculeParser``, ``src/pyjess/_io.py:106-233``), which is not
+# available here; this is a reader of the CIF syntax the atom records need
+# (data blocks, tag-value pairs, ``loop_`` tables, quoted and semicolon
+# text values, comments) followed by the reference's column mapping.  Values
+# are kept as raw tokens, quotes included, as gemmi's table rows are; the
+# mapping strips them where the reference does.
+
+_CIF_TOKEN = __import__("re").compile(
+    r"""'(?:[^']|'(?=\S))*'(?=\s|$)|"(?:[^"]|"(?=\S))*"(?=\s|$)|#.*|\S+""")
+
+
+class CIFBlock:
+    """One ``data_`` block: single values by tag and ``loop_`` tables."""
+
+    def __init__(self, name: str):
+        self.name = name
+        self.values: dict = {}
+        self.loops: list = []  # (tags, rows)
+
+    def find_value(self, tag: str):
+        return self.values.get(tag.lower())
+
+    def find(self, prefix: str, columns):
+        """Rows of the columns `prefix + c` (a leading ``?`` marks an optional
+        column): a list of rows (None for an absent optional column), or
+        None when a required column is missing."""
+        prefix = prefix.lower()
+        names = [(c[1:] if c.startswith("?") else c, c.startswith("?")) for c in columns]
+        for tags, rows in self.loops:
+            pos = {t: i for i, t in enumerate(tags)}
+            if not any(t.startswith(prefix) for t in tags):
+                continue
+            idx = []
+            for c, optional in names:
+                i = pos.get(prefix + c.lower())
+                if i is None and not optional:
+                    return None
+                idx.append(i)
+            return [[None if i is None else row[i] for i in idx] for row in rows]
+        # a category written as single values is a one-row table
+        row = []
+        for c, optional in names:
+            v = self.values.get(prefix + c.lower())
+            if v is None and not optional:
+                return None
+            row.append(v)
+        return [row]
+
+
+def read_cif(text: str) -> typing.List[CIFBlock]:
+    """The data blocks of a CIF text."""
+    blocks: typing.List[CIFBlock] = []
+    tokens: typing.List[str] = []
+    lines = text.splitlines()
+    i = 0
+    while i < len(lines):
+        line = lines[i]
+        if line.startswith(";"):
+            # text field: up to the next line starting with ';'
+            body = [line[1:]]
+            i += 1
+            while i < len(lines) and not lines[i].startswith(";"):
+                body.append(lines[i])
+                i += 1
+            tokens.append("\n".join(body).strip())
+            i += 1
+            continue
+        for m in _CIF_TOKEN.finditer(line):
+            tok = m.group(0)
+            if tok.startswith("#"):
+                break
+            tokens.append(tok)
+        i += 1
+
+    block = None
+    k = 0
+    while k < len(tokens):
+        tok = tokens[k]
+        low = tok.lower()
+        if low.startswith("data_"):
+            block = CIFBlock(tok[5:])
+            blocks.append(block)
+            k += 1
+        elif block is None:
+            raise ValueError("CIF text without a data block")
+        elif low == "loop_":
+            k += 1
+            tags = []
+            while k < len(tokens) and tokens[k].startswith("_"):
+                tags.append(tokens[k].lower())
+                k += 1
+            values = []
+            while k < len(tokens) and not tokens[k].startswith("_") and \
+                    tokens[k].lower() not in ("loop_",) and not tokens[k].lower().startswith("data_"):
+                values.append(tokens[k])
+                k += 1
+            if tags:
+                if len(values) % len(tags):
+                    raise ValueError(f"loop of {tags[0]}: {len(values)} values for {len(tags)} columns")
+                n = len(tags)
+                block.loops.append((tags, [values[j:j + n] for j in range(0, len(values), n)]))
+        elif tok.startswith("_"):
+            if k + 1 >= len(tokens):
+                raise ValueError(f"tag {tok} without a value")
+            block.values[low] = tokens[k + 1]
+            k += 2
+        else:
+            raise ValueError(f"unexpected CIF token {tok!r}")
+    return blocks
+
+
+class CIFMoleculeParser:
+    """Parse a molecule from mmCIF text (``src/pyjess/_io.py:106-233``)."""
+
+    _PRIMARY_COLUMNS = [
+        "id", "type_symbol", "label_atom_id", "label_alt_id", "label_comp_id", "label_asym_id",
+        "label_seq_id", "?pdbx_PDB_ins_code", "Cartn_x", "Cartn_y", "Cartn_z", "occupancy",
+        "B_iso_or_equiv", "?pdbx_formal_charge", "?group_PDB", "pdbx_PDB_model_num",
+    ]
+    _AUTH_COLUMNS = [
+        "id", "type_symbol", "auth_atom_id", "label_alt_id", "auth_comp_id", "auth_asym_id",
+        "auth_seq_id", "?pdbx_PDB_ins_code", "Cartn_x", "Cartn_y", "Cartn_z", "occupancy",
+        "B_iso_or_equiv", "?pdbx_formal_charge", "?group_PDB", "pdbx_PDB_model_num",
+    ]
+
+    def __init__(self, id=None, date=None, name=None, use_author=False, skip_hetatm=False,
+                 ignore_endmdl=False):
+        self.id = id
+        self.date = date
+        self.name = name
+        self.use_author = use_author
+        self.skip_hetatm = skip_hetatm
+        self.ignore_endmdl = ignore_endmdl
+
+    def _load_block(self, blocks, molecule_type):
+        from ._jess import Atom
+
+        if len(blocks) != 1:
+            raise ValueError(f"expected one data block in the CIF text, found {len(blocks)}")
+        block = blocks[0]
+        table = block.find("_atom_site.", self._AUTH_COLUMNS if self.use_author else self._PRIMARY_COLUMNS)
+        if not table:
+            raise ValueError("missing columns in CIF files")
+        atoms = []
+        max_residue_number = 0
+        for row in table:
+            # column 15 is the model number: the first model only, unless
+            # ENDMDL is ignored
+            if not self.ignore_endmdl and row[15] != "1":
+                break
+            if row[14] != "ATOM" and (row[14] != "HETATM" or self.skip_hetatm):
+                continue
+            if row[6] == "." and row[14] == "HETATM":
+                warnings.warn(
+                    "HETATM line found without residue number. Consider parsing with use_author=True to "
+                    "use author-defined residue numbers, or skip_hetatm=True to disable parsing of HETATM "
+                    "altogether.", UserWarning, stacklevel=3)
+                residue_number = max_residue_number
+                max_residue_number += 1
+            else:
+                residue_number = int(row[6])
+                max_residue_number = max(residue_number, max_residue_number)
+            atoms.append(Atom(
+                serial=int(row[0]),
+                element=row[1],
+                name=row[2].strip('"'),
+                altloc=" " if row[3] == "." else row[3],
+                residue_name=row[4],
+                chain_id=row[5],
+                residue_number=residue_number,
+                insertion_code=" " if row[7] is None or row[7] == "?" else row[7],
+                x=float(row[8]),
+                y=float(row[9]),
+                z=float(row[10]),
+                occupancy=0.0 if row[11] == "." else float(row[11]),
+                temperature_factor=0.0 if row[12] == "." else float(row[12]),
+                charge=0 if row[13] is None or row[13] == "?" else int(row[13]),
+            ))
+        id_ = block.name if self.id is None else self.id
+        entry_id = block.find_value("_entry.id")
+        keywords = block.find_value("_struct_keywords.pdbx_keywords")
+        title = block.find_value("_struct.title")
+        name = keywords or title or entry_id
+        name = name.strip("'") if name else None
+        date = None
+        revisions = block.find("_pdbx_audit_revision_history.", ["revision_date"])
+        if revisions:
+            # the earliest revision is the deposition
+            date = min(datetime.datetime.strptime(r[0], "%Y-%m-%d") for r in revisions).date()
+        return molecule_type(
+            atoms,
+            id=id_,
+            date=self.date if self.date is not None else date,
+            name=self.name if self.name is not None else name,
+        )
+
+    def loads(self, text, molecule_type):
+        return self._load_block(read_cif(text), molecule_type)
+
+    def load(self, file, molecule_type):
+        if hasattr(file, "read"):
+            return self.loads(file.read(), molecule_type)
+        with open(file) as f:
+            return self.loads(f.read(), molecule_type)

@@ -23,7 +23,7 @@ from datetime import date as _date
 import numpy as np
 
 from . import _records as R
-from ._io import PDBMoleculeParser, PDBMoleculeWriter, nullcontext
+from ._io import CIFMoleculeParser, PDBMoleculeParser, PDBMoleculeWriter, nullcontext
 
 __all__ = ["Mat4", "Molecule", "Atom", "TemplateAtom", "Template", "Query", "Hit", "Jess"]
 
@@ -359,10 +359,23 @@ class Molecule:
              ignore_endmdl=False, use_author=False, skip_hetatm=False):
         if format not in ("detect", "pdb", "cif"):
             raise ValueError(f"invalid value for `format` argument: {format!r}")
+        if format == "detect":
+            # mmCIF when the first line after leading '#' comment lines
+            # starts a data block or a loop (``_jess.pyx:407-434``)
+            if hasattr(file, "read"):
+                text = file.read()
+            else:
+                with open(file) as f:
+                    text = f.read()
+            first = next((line for line in text.splitlines() if not line.startswith("#")), "")
+            format = "cif" if first.startswith(("data_", "loop_")) else "pdb"
+            file = io.StringIO(text)
         if format == "cif":
-            raise ValueError("mmCIF parsing needs the gemmi module, which is not available")
-        parser = PDBMoleculeParser(id=id, date=date, name=name, ignore_endmdl=ignore_endmdl,
-                                   skip_hetatm=skip_hetatm)
+            parser = CIFMoleculeParser(id=id, date=date, name=name, use_author=use_author,
+                                       skip_hetatm=skip_hetatm, ignore_endmdl=ignore_endmdl)
+        else:
+            parser = PDBMoleculeParser(id=id, date=date, name=name, ignore_endmdl=ignore_endmdl,
+                                       skip_hetatm=skip_hetatm)
         return parser.load(file, molecule_type=cls)
 
     @classmethod

@@ -16,13 +16,14 @@ Files copied (all used by the parity tests):
 - ``1sur.qry``        12-atom two-chain template (dimension test)
 - ``5ayx.EF.pdb``     two-chain fragment for the ``ignore_chain`` tests
 - ``1AMY+1.3.3.txt``  Jess's own output, 156 hits in scanner order
+- ``1AMY.cif``        the same structure in mmCIF (the mmCIF reader's tests)
 """
 
 import pathlib
 import shutil
 
 SOURCE = pathlib.Path("/root/reference/src/pyjess/tests/data")
-FILES = ["1AMY.pdb", "1.3.3.tpl", "4.1.2.tpl", "1sur.qry", "5ayx.EF.pdb", "1AMY+1.3.3.txt"]
+FILES = ["1AMY.pdb", "1.3.3.tpl", "4.1.2.tpl", "1sur.qry", "5ayx.EF.pdb", "1AMY+1.3.3.txt", "1AMY.cif"]
 
 
 def main() -> None:
