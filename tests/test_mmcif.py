@@ -130,3 +130,19 @@ def test_cif_errors():
         Molecule.loads("data_X\ndata_Y\n", format="cif")
     with pytest.raises(ValueError, match="missing columns"):
         Molecule.loads("data_X\n_entry.id X\n", format="cif")
+
+
+@pytest.mark.parametrize("use_author", [False, True])
+@pytest.mark.parametrize("skip_hetatm", [False, True])
+def test_load_consistency(golden, use_author, skip_hetatm):
+    """The four PDB/mmCIF consistency cases of the reference: ATOM records
+    identical, HETATM records identical but for serial, chain and residue
+    number (label columns number hetero groups differently)."""
+    pdb = _load(golden, "1AMY.pdb", format="pdb", skip_hetatm=skip_hetatm)
+    cif = _load(golden, "1AMY.cif", format="cif", use_author=use_author, skip_hetatm=skip_hetatm)
+    n = 3184 if skip_hetatm else 3339
+    assert len(cif) == len(pdb) == n
+    for a, b in itertools.islice(zip(pdb, cif), 3184):
+        _same_atom(a, b)
+    for a, b in itertools.islice(zip(pdb, cif), 3184, n):
+        _same_atom(a, b, hetero=True)
