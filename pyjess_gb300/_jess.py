@@ -1049,6 +1049,69 @@ def _materialize(result, jess, molecules):
     return per
 
 
+class HitArrays:
+    """Hits of a batched query as NumPy columns, without `Hit` objects.
+
+    An addition (PyJess materialises every hit as an object): for queries
+    with millions of hits, building Python objects costs more than the
+    search.  Row ``i`` is the hit `Jess.query_many` would return at the same
+    position; rows are grouped by molecule (``molecule``, ascending) and, per
+    molecule, in ``query()`` order.
+
+    Attributes:
+        molecule (`numpy.ndarray` of int32): index of the hit's molecule.
+        template (`numpy.ndarray` of int32): index of the template in `Jess`.
+        ordinal (`numpy.ndarray` of int64): position of the hit in its
+            (molecule, template) candidate stream.
+        rmsd (`numpy.ndarray` of float64).
+        rotation (`numpy.ndarray` of float64, shape (n, 3, 3)): maps molecule
+            coordinates onto the template frame, about the centroids.
+        centres (`numpy.ndarray` of float64, shape (n, 2, 3)): molecule and
+            template centroids.
+        atom_offset (`numpy.ndarray` of int64, n + 1): hit ``i``'s matched
+            atoms are ``atoms[atom_offset[i]:atom_offset[i + 1]]``.
+        atoms (`numpy.ndarray` of int32): molecule atom indices, in template
+            atom order.
+    """
+
+    __slots__ = ("molecule", "template", "ordinal", "rmsd", "rotation", "centres", "atom_offset", "atoms",
+                 "_jess", "_molecules")
+
+    def __init__(self, data, jess, molecules):
+        n = data["count"]
+        self.molecule = data["structure"]
+        self.template = data["template"]
+        self.ordinal = data["ordinal"]
+        self.rmsd = data["rmsd"]
+        self.rotation = data["rotation"].reshape(n, 3, 3)
+        self.centres = data["centres"].reshape(n, 2, 3)
+        self.atom_offset = data["atom_offset"]
+        self.atoms = data["atoms"]
+        self._jess = jess
+        self._molecules = molecules
+
+    def __len__(self):
+        return len(self.rmsd)
+
+    def molecule_offsets(self) -> np.ndarray:
+        """Row offsets per molecule: the hits of molecule ``m`` are rows
+        ``offsets[m]:offsets[m + 1]``."""
+        return np.searchsorted(self.molecule, np.arange(len(self._molecules) + 1), side="left")
+
+    def hit(self, i: int) -> "Hit":
+        """Row ``i`` as a `Hit` object."""
+        mol = self._molecules[int(self.molecule[i])]
+        a0, a1 = int(self.atom_offset[i]), int(self.atom_offset[i + 1])
+        hit = Hit.__new__(Hit)
+        hit.rmsd = float(self.rmsd[i])
+        hit._rotation = self.rotation[i].reshape(9).copy()
+        hit._centre = self.centres[i].copy()
+        hit._atoms = mol._atoms[self.atoms[a0:a1]].copy()
+        hit._template = self._jess._templates[int(self.template[i])]
+        hit._molecule = mol
+        return hit
+
+
 # --- Jess ---------------------------------------------------------------------
 
 
@@ -1157,3 +1220,22 @@ class Jess:
             for _ in ws:
                 warnings.warn("Jess returned a superposition matrix with NaN values", UserWarning, 2)
         return per
+
+    def query_arrays(self, molecules, rmsd_threshold, distance_cutoff, max_dynamic_distance, *,
+                     max_candidates=None, ignore_chain=None, best_match=False, reorder=True,
+                     precision="fp32") -> HitArrays:
+        """`query_many` with the hits returned as NumPy columns (`HitArrays`)
+        instead of `Hit` objects; the same search, hits and order."""
+        from . import _native
+
+        molecules = list(molecules)
+        q = Query(self, Molecule(), rmsd_threshold, distance_cutoff, max_dynamic_distance,
+                  max_candidates, ignore_chain, best_match, reorder)
+        mode = {"fp32": _native.MODE_BATCHED_FP32, "fp64": _native.MODE_BATCHED_FP64,
+                "plain": _native.MODE_PLAIN_FP64}[precision]
+        result = _native.query(self._device_templates(), _native.structures_for(molecules),
+                               q._params(mode))
+        for s, ws in enumerate(result.warnings_by_structure(len(molecules))):
+            for _ in ws:
+                warnings.warn("Jess returned a superposition matrix with NaN values", UserWarning, 2)
+        return HitArrays(result.arrays(), self, molecules)
