@@ -141,7 +141,9 @@ typedef struct {
     int64_t suspensions;             /* pair searches stopped at a list
                                         with no leaf order yet (rerun)     */
     int32_t search_rounds;           /* search launches                    */
-    int32_t pad;
+    int32_t row_splits;              /* chunks redone on fewer structures
+                                        because their complete rows did
+                                        not fit in memory                  */
 } pjg_stats;
 
 typedef struct pjg_templates pjg_templates;

@@ -76,7 +76,7 @@ class Stats(C.Structure):
         ("leaf_entries", C.c_int64),
         ("suspensions", C.c_int64),
         ("search_rounds", C.c_int32),
-        ("pad", C.c_int32),
+        ("row_splits", C.c_int32),
     ]
 
     def as_dict(self) -> dict:

@@ -849,7 +849,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     unsigned long long counters[C_NUM] = {};
     float ms = 0.f;
     double ms_cand = 0, ms_exp = 0, ms_sup = 0, ms_total = 0, ms_search = 0;
-    int launches = 0, chunks = 0, search_rounds = 0;
+    int launches = 0, chunks = 0, search_rounds = 0, row_splits = 0;
     t_scan_launches = 0;
     int64_t suspensions = 0;
     // levels whose lists are put in kd leaf order before the search (deeper
@@ -974,6 +974,9 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             if (v && atoll(v) > 0) ENTRY_BUDGET = atoll(v);
         }
         const int max_chunk = P->mode == PJG_MODE_PLAIN_FP64 ? 1 : 4096;
+        // structures a chunk may take; halved when a chunk's complete rows
+        // outgrow the memory of the per-row stages (see below)
+        int chunk_cap = max_chunk;
         int s0 = 0;
         int64_t c_cap = 1 << 20;
         CUDA_TRY(dalloc(d_c_pair, c_cap, st));
@@ -984,12 +987,16 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
         while (s0 < S) {
             int s1 = s0;
             int64_t entries = 0;
-            while (s1 < S && (s1 == s0 || (entries + totals[s1] <= ENTRY_BUDGET && s1 - s0 < max_chunk))) {
+            while (s1 < S && (s1 == s0 || (entries + totals[s1] <= ENTRY_BUDGET && s1 - s0 < chunk_cap))) {
                 entries += totals[s1];
                 s1++;
             }
             chunks++;
             const double ms_search_chunk0 = ms_search;
+            // counters before this chunk (restored if it is redone smaller)
+            unsigned long long chunk_snap[C_NUM];
+            CUDA_TRY(cudaMemcpyAsync(chunk_snap, d_counters.p, sizeof chunk_snap, cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(cudaStreamSynchronize(st));
             const int Sc = s1 - s0;
             const int64_t Wc = (int64_t)Sc * G;
             ChunkView cv{Sc, sp->d_atom_base + s0, sp->d_atom_count + s0, sp->d_xyz64, sp->d_xyz32, sp->d_name,
@@ -1273,6 +1280,28 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 CUDA_TRY(cudaMemcpyAsync(&nc, d_ccount.p, sizeof nc, cudaMemcpyDeviceToHost, st));
                 CUDA_TRY(cudaStreamSynchronize(st));
                 const int64_t rows = (int64_t)nc;
+                {
+                    // the per-row stages below hold ~360 + 4 * stride bytes a
+                    // complete row (superposition, automaton, compaction and
+                    // the hits they may append): when the chunk's rows need
+                    // more than 70% of the free memory, the chunk is redone
+                    // on half its structures (PJG_ROW_BUDGET sets the limit)
+                    int64_t row_budget = INT64_MAX;
+                    size_t free_b = 0, total_b = 0;
+                    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+                        row_budget = (int64_t)((double)free_b * 0.7 / (360.0 + 4.0 * stride));
+                    cudaGetLastError();
+                    const char *v = getenv("PJG_ROW_BUDGET");
+                    if (v && atoll(v) > 0) row_budget = atoll(v);
+                    if (rows > row_budget && Sc > 1) {
+                        chunk_cap = std::max(1, Sc / 2);
+                        chunks--;
+                        row_splits++;
+                        CUDA_TRY(cudaMemcpyAsync(d_counters.p, chunk_snap, sizeof chunk_snap, cudaMemcpyHostToDevice,
+                                                 st));
+                        continue;
+                    }
+                }
                 CompleteRows cr{d_ccount.p, c_cap, stride, d_c_pair.p, d_c_ord.p, d_c_atoms.p,
                                 cut_inline ? d_c_rmsd.p : nullptr, d_pair_rows.p};
                 if (rows > 0) {
@@ -1374,6 +1403,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     res->stats.leaf_entries = (int64_t)counters[C_LEAF_ENTRIES];
     res->stats.suspensions = suspensions;
     res->stats.search_rounds = search_rounds;
+    res->stats.row_splits = row_splits;
 
 done:
     if (st) {

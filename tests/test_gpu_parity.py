@@ -393,6 +393,19 @@ def test_leaf_arrays_grow(monkeypatch, levels):
     assert res.stats()["chunks"] == 12
 
 
+def test_row_budget_split(monkeypatch):
+    """A chunk whose complete rows exceed the row budget is redone on half
+    its structures (down to one): the same hits and search counters as the
+    oracle's."""
+    from pyjess_gb300 import workloads as W
+
+    monkeypatch.setenv("PJG_ROW_BUDGET", "50")
+    wl = W.config(3, n_structures=12, n_templates=300)
+    res, ref = compare(wl.templates, wl.structures, mode="fp32", **wl.params)
+    st = res.stats()
+    assert st["row_splits"] > 0 and st["chunks"] > 1
+
+
 def test_large_result_copy_out():
     """Results of several MiB come back through the threaded copy (one host
     thread per MiB, each touching then copying its range of the caller's
