@@ -76,3 +76,20 @@ def test_cli_golden_1amy(tmp_path, monkeypatch, golden, golden_blocks, batch):
             assert gl[:30] == wl[:30]
             for c0, c1 in ((30, 38), (38, 46), (46, 54)):
                 assert float(gl[c0:c1]) == pytest.approx(float(wl[c0:c1]), abs=1.5e-3)
+
+
+@pytest.mark.parametrize("codec", ["gzip", "bz2", "lzma", None])
+def test_zopen_decompresses_by_magic(tmp_path, codec):
+    import importlib
+
+    from pyjess_gb300.cli import zopen
+
+    text = "template.pdb\nother.pdb\n"
+    path = tmp_path / "list.txt"
+    if codec is None:
+        path.write_text(text)
+    else:
+        with importlib.import_module(codec).open(path, "wt") as f:
+            f.write(text)
+    with zopen(path) as f:
+        assert f.read() == text
