@@ -48,12 +48,18 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--structures", type=int, default=2000)
-    ap.add_argument("--templates", type=int, default=5000)
-    ap.add_argument("--cpu-structures", type=int, default=0, help="structures in the CPU sample (0: auto)")
-    ap.add_argument("--plain-structures", type=int, default=100,
-                    help="structures timed with the plain FP64 per-structure path")
+    ap.add_argument("--config", type=int, default=3, choices=[2, 3],
+                    help="workload: 3 (default, 2,000 x 5,000) or 2 (1,000 x 2,000)")
+    ap.add_argument("--structures", type=int, default=0, help="structures (0: the configuration's)")
+    ap.add_argument("--templates", type=int, default=0, help="templates (0: the configuration's)")
+    ap.add_argument("--cpu-stride", type=int, default=31,
+                    help="the CPU arms time every k-th structure (all templates)")
+    ap.add_argument("--plain-structures", type=int, default=-1,
+                    help="structures run through the plain FP64 per-structure path (-1: all, 0: none)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--search-profile", action="store_true",
+                    help="run the search-profile build of the library and print k_search's event counts "
+                         "and section cycles (not a bench line)")
     return ap.parse_args()
 
 
@@ -128,13 +134,14 @@ def measured_peaks():
 
 
 def workload(args, rank=0, world=1):
-    """This rank's share of a multi-GPU run: rank 0 takes config 3 itself,
-    rank r an independent instance drawn with the same distributions (weak
-    scaling: the pairs of every rank are independent, no data-path
+    """This rank's share of a multi-GPU run: rank 0 takes the configuration
+    itself, rank r an independent instance drawn with the same distributions
+    (weak scaling: the pairs of every rank are independent, no data-path
     collective)."""
     from pyjess_gb300 import workloads as W
 
-    return W.config(3, n_structures=args.structures, n_templates=args.templates, shard=rank if world > 1 else 0)
+    return W.config(args.config, n_structures=args.structures or None, n_templates=args.templates or None,
+                    shard=rank if world > 1 else 0)
 
 
 def max_over_ranks(value, dist):
@@ -148,16 +155,30 @@ def max_over_ranks(value, dist):
     return float(t.item())
 
 
-def cpu_sample(wl, n_structures, threads):
-    """Time the CPU oracle on the first `n_structures` structures x all templates."""
+def cpu_structures(wl, stride):
+    """The CPU arms' sample: every `stride`-th structure (ordinary and
+    adversarial ones in the set's proportions) against every template."""
+    return list(range(0, wl.structures.n_structures, max(1, stride)))
+
+
+def cpu_sample(wl, idx, threads):
+    """Time the CPU oracle on structures `idx` x all templates."""
     from oracle import oracle
 
-    sub = wl.structures.subset(list(range(min(n_structures, wl.structures.n_structures))))
+    sub = wl.structures.subset(idx)
     t0 = time.perf_counter()
     r = oracle.query(wl.templates, sub, threads=threads, **wl.params)
     dt = time.perf_counter() - t0
     pairs = wl.templates.n_templates * sub.n_structures
     return pairs / dt, dt, pairs, r["hits"]["count"]
+
+
+def sample_text(wl, idx, stride):
+    pairs = len(idx) * wl.templates.n_templates
+    n_adv = wl.n_adversarial
+    return (f"every {stride}th structure ({len(idx)} of {wl.structures.n_structures}, "
+            f"{sum(1 for i in idx if i < n_adv)} of them adversarial) x {wl.templates.n_templates} templates = "
+            f"{pairs} pairs per step; pairs/s of the sample stands for the whole set")
 
 
 def run_reference(args):
@@ -166,14 +187,14 @@ def run_reference(args):
         return
     wl = workload(args)
     threads = os.cpu_count() or 1
-    n = args.cpu_structures or 32
+    idx = cpu_structures(wl, args.cpu_stride)
     vals = []
     for i in range(args.warmup + args.steps):
-        v, dt, pairs, hits = cpu_sample(wl, n, threads)
+        v, dt, pairs, hits = cpu_sample(wl, idx, threads)
         if i >= args.warmup:
             vals.append(v)
     value = statistics.median(vals)
-    sample = f"{n} structures x {wl.templates.n_templates} templates = {n * wl.templates.n_templates} pairs per step"
+    sample = sample_text(wl, idx, args.cpu_stride)
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
@@ -186,16 +207,74 @@ def run_reference(args):
     }))
 
 
+def query_params(wl, mode, guard_band=1e-4):
+    from pyjess_gb300._abi import QueryParams
+
+    return QueryParams(rmsd_threshold=wl.params["rmsd_threshold"], distance_cutoff=wl.params["distance_cutoff"],
+                       max_dynamic_distance=wl.params["max_dynamic_distance"], max_candidates=-1, ignore_chain=0,
+                       best_match=0, reorder=1, mode=mode, guard_band=guard_band)
+
+
+def same_arrays(a, b):
+    """Every field of two hit-array dicts equal (bit for bit)."""
+    import numpy as np
+
+    if a["count"] != b["count"]:
+        return False
+    return all(np.array_equal(a[k], b[k]) for k in a if k != "count")
+
+
+def search_profile(args):
+    """k_search's event counts and section cycles on this workload, from the
+    search-profile build of the library (one query after one warm-up)."""
+    import tempfile
+
+    os.environ["PJG_LIB_VARIANT"] = "prof"
+    from pyjess_gb300 import _build, _native
+
+    _build.build(variant="prof")
+    _native.init(dist_env()[2])
+    wl = workload(args)
+    tpl = _native.Templates(wl.templates)
+    sts = _native.Structures(wl.structures)
+    P = query_params(wl, _native.MODE_BATCHED_FP32)
+    _native.query(tpl, sts, P).arrays()
+    with tempfile.NamedTemporaryFile("r", suffix=".jsonl") as f:
+        os.environ["PJG_PROF_OUT"] = f.name
+        st = _native.query(tpl, sts, P).stats()
+        prof = json.loads(f.read().strip().splitlines()[-1])
+    pairs_run = prof["pairs"] - prof["empty"]
+    derived = {
+        "cycles_per_pair_run": prof["cyc_pair"] / max(1, pairs_run),
+        "share_setup": prof["cyc_setup"] / max(1, prof["cyc_pair"]),
+        "share_seed": prof["cyc_seed"] / max(1, prof["cyc_pair"]),
+        "share_block": prof["cyc_block"] / max(1, prof["cyc_pair"]),
+        "share_product": prof["cyc_prod"] / max(1, prof["cyc_pair"]),
+        "share_emit": prof["cyc_emit"] / max(1, prof["cyc_pair"]),
+        "blocks_hit_per_tested": prof["blocks_hit"] / max(1, prof["blocks_tested"]),
+        "inbox_per_leaf_loaded": prof["leaves_inbox"] / max(1, 32 * prof["blocks_hit"]),
+        "children_per_block_test": prof["child_block"] / max(1, prof["batch_lanes"]),
+        "lanes_per_batch": prof["batch_lanes"] / max(1, prof["batches"]),
+        "children_per_product_test": prof["child_prod"] / max(1, prof["prod_lanes"]),
+        "lanes_per_product_batch": prof["prod_lanes"] / max(1, prof["prod_batches"]),
+        "block_visits_per_partial": prof["block_visits"] / max(1, st["partials"]),
+    }
+    print(json.dumps({"search_profile": prof, "derived": derived, "workload": wl.name,
+                      "partials": st["partials"], "complete": st["complete"],
+                      "ms_expansion_profile_build": st["ms_expansion"]}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.search_profile:
+        return search_profile(args)
     rank, world, local = dist_env()
     import __graft_entry__
 
     __graft_entry__.build()
     from pyjess_gb300 import _native
-    from pyjess_gb300._abi import QueryParams
 
     _native.init(local)
     dist = None
@@ -207,9 +286,7 @@ def main():
     t0 = time.time()
     wl = workload(args, rank, world)
     gen_s = time.time() - t0
-    P = QueryParams(rmsd_threshold=wl.params["rmsd_threshold"], distance_cutoff=wl.params["distance_cutoff"],
-                    max_dynamic_distance=wl.params["max_dynamic_distance"], max_candidates=-1, ignore_chain=0,
-                    best_match=0, reorder=1, mode=_native.MODE_BATCHED_FP32, guard_band=1e-4)
+    P = query_params(wl, _native.MODE_BATCHED_FP32)
     tpl = _native.Templates(wl.templates)
     sts = _native.Structures(wl.structures)
 
@@ -252,23 +329,26 @@ def main():
             launches_k = max(1, sum(s["search_rounds"] for s in stats))
             traffic = tr["dram_per_expansion_byte"] * exp_bytes / launches_k
 
-    # ---- plain FP64 per-structure path on a subset (the method the batched
-    # path is measured against)
+    # ---- plain FP64 per-structure path (the method the batched path is
+    # measured against) over the structures asked for (default: all), its
+    # hits compared field by field with the batched query's
     plain = None
-    if args.plain_structures > 0 and rank == 0:
-        sub = wl.structures.subset(list(range(min(args.plain_structures, wl.structures.n_structures))))
-        ssub = _native.Structures(sub)
-        Pp = QueryParams(rmsd_threshold=P.rmsd_threshold, distance_cutoff=P.distance_cutoff,
-                         max_dynamic_distance=P.max_dynamic_distance, max_candidates=-1, ignore_chain=0,
-                         best_match=0, reorder=1, mode=_native.MODE_PLAIN_FP64)
-        _native.query(tpl, ssub, Pp).arrays()
+    if args.plain_structures != 0 and rank == 0:
+        ns = wl.structures.n_structures
+        k = ns if args.plain_structures < 0 else min(args.plain_structures, ns)
+        Pp = query_params(wl, _native.MODE_PLAIN_FP64)
+        if k == ns:
+            ssub, batched = sts, arr
+        else:
+            ssub = _native.Structures(wl.structures.subset(list(range(k))))
+            batched = _native.query(tpl, ssub, P).arrays()
         rp = _native.query(tpl, ssub, Pp)
         ms = rp.stats()["ms_total"]
-        rb = _native.query(tpl, ssub, P)
-        same = rp.arrays()["count"] == rb.arrays()["count"] and \
-            (rp.arrays()["atoms"] == rb.arrays()["atoms"]).all()
-        plain = {"value": wl.templates.n_templates * sub.n_structures / (ms / 1e3), "unit": UNIT,
-                 "structures": sub.n_structures, "same_hits_as_batched": bool(same)}
+        plain = {"value": wl.templates.n_templates * k / (ms / 1e3), "unit": UNIT, "structures": k,
+                 "ms": ms, "identical_to_batched": same_arrays(rp.arrays(), batched),
+                 "compared": "every field of every hit (structure, template, ordinal, atoms, rmsd, rotation, "
+                             "centres), bit for bit"}
+        del rp
 
     # ---- end to end through the C ABI with host buffers
     e2e = None
@@ -299,14 +379,17 @@ def main():
         e2e = {"value": pairs_step * world * args.steps / tot, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "phases_ms": {k: round(v, 1) for k, v in phases.items()}}
 
-    # ---- CPU baseline (rank 0, N=1)
+    # ---- CPU baseline (rank 0, N=1): the same strided sample as the
+    # reference arm, median of three runs
     cpu = None
     if rank == 0 and world == 1:
         threads = os.cpu_count() or 1
-        n = args.cpu_structures or 64
-        v, dt, pairs, _ = cpu_sample(wl, n, threads)
+        idx = cpu_structures(wl, args.cpu_stride)
+        runs = [cpu_sample(wl, idx, threads) for _ in range(3)]
+        v = statistics.median(r[0] for r in runs)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{n} structures x {wl.templates.n_templates} templates ({pairs} pairs, {dt:.1f} s)"}
+               "sample": sample_text(wl, idx, args.cpu_stride) + f" (median of 3 runs of "
+                                                                  f"{statistics.median(r[1] for r in runs):.1f} s)"}
 
     if rank != 0:
         return
@@ -330,6 +413,7 @@ def main():
         "hits_per_s": hits_per_s,
         "hits_per_step": s0["hits"],
         "plain_fp64": plain,
+        "batched_over_plain": value / plain["value"] if plain else None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
                      "kernel": "k_search", "peak_kind": peak_kind,
@@ -339,7 +423,7 @@ def main():
                      "superposition": s0["ms_superposition"], "total": s0["ms_total"]},
         "counters": {k: s0[k] for k in ("pairs", "candidate_entries", "partials", "complete", "passing", "hits",
                                         "fp64_rechecks", "leaf_lists", "leaf_entries", "leaf_exact", "suspensions",
-                                        "search_rounds", "chunks")},
+                                        "search_rounds", "chunks", "row_splits")},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": launches,

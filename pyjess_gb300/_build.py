@@ -28,6 +28,14 @@ NVCC_FLAGS = [
     "-I", str(INCLUDE),
 ]
 SOURCES = ["pjg_kernels.cu", "pjg_api.cu"]
+# library variants: "" the product library; "prof" adds the search profile
+# (event counts and section cycles of k_search, written per query to the
+# file named by PJG_PROF_OUT) and is never the timed build
+VARIANTS = {"": [], "prof": ["-DPJG_SEARCH_PROF=1"]}
+
+
+def lib_path(variant: str = "") -> pathlib.Path:
+    return LIB if not variant else LIBDIR / f"libpjg_{variant}.so"
 
 
 def nvcc() -> str:
@@ -40,19 +48,21 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libpjg")
 
 
-def _stale() -> bool:
-    if not LIB.exists():
+def _stale(lib: pathlib.Path = LIB) -> bool:
+    if not lib.exists():
         return True
-    t = LIB.stat().st_mtime
+    t = lib.stat().st_mtime
     deps = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + [INCLUDE / "pjg.h", pathlib.Path(__file__)]
     return any(p.stat().st_mtime > t for p in deps)
 
 
-def build(force: bool = False, verbose: bool = False, extra=()) -> pathlib.Path:
-    if not force and not _stale():
-        return LIB
+def build(force: bool = False, verbose: bool = False, extra=(), variant: str = "") -> pathlib.Path:
+    lib = lib_path(variant)
+    if not force and not _stale(lib):
+        return lib
+    extra = [*VARIANTS[variant], *extra]
     LIBDIR.mkdir(exist_ok=True)
-    objdir = LIBDIR / "obj"
+    objdir = LIBDIR / ("obj" if not variant else f"obj_{variant}")
     objdir.mkdir(exist_ok=True)
     cc = nvcc()
 
@@ -70,13 +80,13 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> pathlib.Path:
 
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-    tmp = LIB.with_suffix(".so.tmp")
+    tmp = lib.with_suffix(".so.tmp")
     cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

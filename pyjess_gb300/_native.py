@@ -13,7 +13,7 @@ import threading
 import numpy as np
 
 from ._abi import QueryParams, Stats, StructureSet, TemplateSet
-from ._build import LIB, build
+from ._build import build, lib_path
 
 MODE_PLAIN_FP64 = 0
 MODE_BATCHED_FP32 = 1
@@ -38,16 +38,19 @@ _initialized = False
 
 
 def load(build_if_missing: bool = True):
-    """Load the library (building it in-tree first if it is absent)."""
+    """Load the library (building it in-tree first if it is absent).
+    ``PJG_LIB_VARIANT=prof`` loads the search-profile build instead."""
     global _lib
     with _lock:
         if _lib is not None:
             return _lib
-        if not LIB.exists():
+        variant = os.environ.get("PJG_LIB_VARIANT", "")
+        lib = lib_path(variant)
+        if not lib.exists():
             if not build_if_missing:
-                raise RuntimeError(f"libpjg.so not built ({LIB}); run pyjess_gb300._build.build()")
-            build()
-        L = C.CDLL(str(LIB))
+                raise RuntimeError(f"{lib.name} not built ({lib}); run pyjess_gb300._build.build()")
+            build(variant=variant)
+        L = C.CDLL(str(lib))
         L.pjg_init.argtypes = [C.c_int32]
         L.pjg_init.restype = C.c_int
         L.pjg_last_error.restype = C.c_char_p

@@ -798,6 +798,31 @@ cudaError_t scan_exclusive(const T *in, int64_t n, int64_t *out, std::vector<DBu
     return cudaGetLastError();
 }
 
+#if PJG_SEARCH_PROF
+// Profile builds: append the query's search profile as one JSON line to the
+// file named by PJG_PROF_OUT (nothing when unset).
+void write_search_profile(const unsigned long long *d_prof, cudaStream_t st, const pjg_stats &stats) {
+    static const char *names[SP_NUM] = {
+        "pairs", "empty", "cyc_pair", "cyc_setup", "cyc_seed", "cyc_block", "cyc_prod", "cyc_emit",
+        "loop_iters", "block_visits", "block_visits_l0", "chain_full", "chain_sibling", "g0_iters",
+        "blocks_tested", "blocks_hit", "leaves_inbox", "batches", "batch_lanes", "child_block",
+        "prod_batches", "prod_batches_l0", "prod_lanes", "child_prod", "fp64", "rows"};
+    unsigned long long h[SP_NUM] = {};
+    if (cudaMemcpyAsync(h, d_prof, sizeof h, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return;
+    const char *path = getenv("PJG_PROF_OUT");
+    if (!path || !*path) return;
+    FILE *f = fopen(path, "a");
+    if (!f) return;
+    fprintf(f, "{\"ms_expansion\": %.3f, \"partials\": %lld, \"search_rounds\": %d", stats.ms_expansion,
+            (long long)stats.partials, stats.search_rounds);
+    for (int i = 0; i < SP_NUM; i++) fprintf(f, ", \"%s\": %llu", names[i], h[i]);
+    fprintf(f, "}\n");
+    fclose(f);
+}
+#endif
+
 }  // namespace
 
 extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *sp, const pjg_query_params *P,
@@ -839,6 +864,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     DBuf<unsigned long long> d_pool_used;
     int64_t pool_cap = 0;
     DBuf<double> d_c_rmsd;
+    DBuf<unsigned long long> d_prof;  // search profile (profile builds)
     // per complete row, in reference order
     DBuf<double> d_r_rmsd, d_r_rot, d_r_cen;
     DBuf<int32_t> d_r_nan, d_r_hit, d_r_warn, d_r_hatoms;
@@ -975,14 +1001,49 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
         }
         const int max_chunk = P->mode == PJG_MODE_PLAIN_FP64 ? 1 : 4096;
         // structures a chunk may take; halved when a chunk's complete rows
-        // outgrow the memory of the per-row stages (see below)
+        // outgrow the memory of the per-row stages (see below), then sized
+        // from the rows a structure of the last chunk produced
         int chunk_cap = max_chunk;
+        const bool cut_inline = !P->best_match && P->max_candidates >= 0;
+        // device bytes a complete row takes: its record in the row buffers
+        // (grown with a quarter of headroom) and the per-row stages after the
+        // search (superposition, automaton, compaction and the hits they may
+        // append)
+        const double row_buf_bytes = 12.0 + 4.0 * stride + (cut_inline ? 8.0 : 0.0);
+        const double row_stage_bytes = 360.0 + 4.0 * stride;
+        // memory a chunk's rows may use: free device memory, memory the
+        // stream-ordered pool holds unused, and the row buffers and per-row
+        // arrays of the previous chunk (reused)
+        auto row_memory = [&]() -> double {
+            double a = 0.0;
+            size_t free_b = 0, total_b = 0;
+            if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) a = (double)free_b;
+            cudaMemPool_t pool;
+            if (cudaDeviceGetDefaultMemPool(&pool, res->device) == cudaSuccess) {
+                uint64_t reserved = 0, used = 0;
+                if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess &&
+                    cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess &&
+                    reserved > used)
+                    a += (double)(reserved - used);
+            }
+            cudaGetLastError();
+            a += (double)(d_c_pair.n * 4 + d_c_ord.n * 8 + d_c_atoms.n * 4 + d_c_rmsd.n * 8);
+            a += (double)(d_r_rmsd.n * 8 + d_r_rot.n * 8 + d_r_cen.n * 8 + d_r_nan.n * 4 + d_r_src.n * 8 +
+                          d_r_hit.n * 4 + d_r_warn.n * 4 + d_r_hatoms.n * 4 + d_r_hidx.n * 8 + d_r_widx.n * 8 +
+                          d_r_aidx.n * 8);
+            return a;
+        };
+        // rows a chunk may produce (PJG_ROW_BUDGET sets it)
+        auto row_budget = [&]() -> int64_t {
+            const char *v = getenv("PJG_ROW_BUDGET");
+            if (v && atoll(v) > 0) return atoll(v);
+            return (int64_t)(0.7 * row_memory() / (row_buf_bytes * 1.25 + row_stage_bytes));
+        };
         int s0 = 0;
         int64_t c_cap = 1 << 20;
         CUDA_TRY(dalloc(d_c_pair, c_cap, st));
         CUDA_TRY(dalloc(d_c_ord, c_cap, st));
         CUDA_TRY(dalloc(d_c_atoms, (size_t)c_cap * stride, st));
-        const bool cut_inline = !P->best_match && P->max_candidates >= 0;
         if (cut_inline) CUDA_TRY(dalloc(d_c_rmsd, c_cap, st));
         while (s0 < S) {
             int s1 = s0;
@@ -993,7 +1054,10 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             }
             chunks++;
             const double ms_search_chunk0 = ms_search;
-            // counters before this chunk (restored if it is redone smaller)
+            // host statistics and device counters before this chunk (restored
+            // if it is redone on fewer structures)
+            const int search_rounds0 = search_rounds;
+            const int64_t suspensions0 = suspensions;
             unsigned long long chunk_snap[C_NUM];
             CUDA_TRY(cudaMemcpyAsync(chunk_snap, d_counters.p, sizeof chunk_snap, cudaMemcpyDeviceToHost, st));
             CUDA_TRY(cudaStreamSynchronize(st));
@@ -1173,6 +1237,14 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             }
             sa.cut_inline = cut_inline ? 1 : 0;
             sa.rmsd_threshold = P->rmsd_threshold;
+            sa.prof = nullptr;
+#if PJG_SEARCH_PROF
+            if (!d_prof.p) {
+                CUDA_TRY(dalloc(d_prof, SP_NUM, st));
+                CUDA_TRY(cudaMemsetAsync(d_prof.p, 0, SP_NUM * sizeof(unsigned long long), st));
+            }
+            sa.prof = d_prof.p;
+#endif
             {
                 const char *b = getenv("PJG_KERNEL_BUDGET_S");
                 double sec = b ? atof(b) : 120.0;
@@ -1194,6 +1266,9 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 CUDA_TRY(dalloc(d_c_atoms, (size_t)c_cap * stride, st));
                 if (cut_inline) CUDA_TRY(dalloc(d_c_rmsd, c_cap, st));
             }
+            // set when the chunk's complete rows cannot be held: the chunk is
+            // redone on half its structures
+            bool split = false;
             for (int attempt = 0; attempt < 8; attempt++) {
                 CUDA_TRY(cudaMemsetAsync(d_ccount.p, 0, sizeof(unsigned long long), st));
                 CUDA_TRY(cudaMemsetAsync(d_pair_rows.p, 0, (size_t)n_pairs * sizeof(int32_t), st));
@@ -1256,12 +1331,29 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 if ((int64_t)nc <= c_cap) break;
                 // the row buffer was too small: grow and run the chunk again
                 // (the search counters of the failed attempt are rolled back;
-                // lists ordered meanwhile stay ordered)
+                // lists ordered meanwhile stay ordered).  Rows beyond the
+                // chunk's row budget, or a growth that fails, split the chunk
+                // instead (down to one structure).
+                if (Sc > 1 && (int64_t)nc > row_budget()) {
+                    split = true;
+                    break;
+                }
                 c_cap = (int64_t)nc + nc / 4 + 1024;
-                CUDA_TRY(dalloc(d_c_pair, c_cap, st));
-                CUDA_TRY(dalloc(d_c_ord, c_cap, st));
-                CUDA_TRY(dalloc(d_c_atoms, (size_t)c_cap * stride, st));
-                if (cut_inline) CUDA_TRY(dalloc(d_c_rmsd, c_cap, st));
+                {
+                    cudaError_t eg = dalloc(d_c_pair, c_cap, st);
+                    if (eg == cudaSuccess) eg = dalloc(d_c_ord, c_cap, st);
+                    if (eg == cudaSuccess) eg = dalloc(d_c_atoms, (size_t)c_cap * stride, st);
+                    if (eg == cudaSuccess && cut_inline) eg = dalloc(d_c_rmsd, c_cap, st);
+                    if (eg == cudaErrorMemoryAllocation && Sc > 1) {
+                        cudaGetLastError();
+                        c_cap = std::min<int64_t>({(int64_t)d_c_pair.n, (int64_t)d_c_ord.n,
+                                                   (int64_t)(d_c_atoms.n / stride)});
+                        if (cut_inline) c_cap = std::min<int64_t>(c_cap, (int64_t)d_c_rmsd.n);
+                        split = true;
+                        break;
+                    }
+                    CUDA_TRY(eg);
+                }
                 {
                     unsigned long long cur[C_NUM];
                     CUDA_TRY(cudaMemcpyAsync(cur, d_counters.p, sizeof cur, cudaMemcpyDeviceToHost, st));
@@ -1280,27 +1372,20 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 CUDA_TRY(cudaMemcpyAsync(&nc, d_ccount.p, sizeof nc, cudaMemcpyDeviceToHost, st));
                 CUDA_TRY(cudaStreamSynchronize(st));
                 const int64_t rows = (int64_t)nc;
-                {
-                    // the per-row stages below hold ~360 + 4 * stride bytes a
-                    // complete row (superposition, automaton, compaction and
-                    // the hits they may append): when the chunk's rows need
-                    // more than 70% of the free memory, the chunk is redone
-                    // on half its structures (PJG_ROW_BUDGET sets the limit)
-                    int64_t row_budget = INT64_MAX;
-                    size_t free_b = 0, total_b = 0;
-                    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
-                        row_budget = (int64_t)((double)free_b * 0.7 / (360.0 + 4.0 * stride));
-                    cudaGetLastError();
-                    const char *v = getenv("PJG_ROW_BUDGET");
-                    if (v && atoll(v) > 0) row_budget = atoll(v);
-                    if (rows > row_budget && Sc > 1) {
-                        chunk_cap = std::max(1, Sc / 2);
-                        chunks--;
-                        row_splits++;
-                        CUDA_TRY(cudaMemcpyAsync(d_counters.p, chunk_snap, sizeof chunk_snap, cudaMemcpyHostToDevice,
-                                                 st));
-                        continue;
-                    }
+                // the per-row stages below hold ~360 + 4 * stride bytes a
+                // complete row: when the chunk's rows need more than 70% of
+                // the memory they may use, or the row buffers could not hold
+                // them, the chunk is redone on half its structures
+                if (Sc > 1 && (split || rows > row_budget())) {
+                    chunk_cap = std::max(1, Sc / 2);
+                    chunks--;
+                    row_splits++;
+                    search_rounds = search_rounds0;
+                    suspensions = suspensions0;
+                    ms_search = ms_search_chunk0;
+                    CUDA_TRY(cudaMemcpyAsync(d_counters.p, chunk_snap, sizeof chunk_snap, cudaMemcpyHostToDevice,
+                                             st));
+                    continue;
                 }
                 CompleteRows cr{d_ccount.p, c_cap, stride, d_c_pair.p, d_c_ord.p, d_c_atoms.p,
                                 cut_inline ? d_c_rmsd.p : nullptr, d_pair_rows.p};
@@ -1357,6 +1442,16 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 ms_cand += m1 + (m2 - (float)(ms_search - ms_search_chunk0));
                 ms_exp += ms_search - ms_search_chunk0;
                 ms_sup += m3;
+                // next chunk: as many structures as the row budget takes at
+                // this chunk's rows per structure (a dense chunk early in the
+                // set does not keep every later chunk small)
+                if (rows > 0 && max_chunk > 1) {
+                    const double per = (double)rows / (double)Sc;
+                    const double fit = 0.8 * (double)row_budget() / per;
+                    chunk_cap = (int)std::max(1.0, std::min((double)max_chunk, fit));
+                } else {
+                    chunk_cap = max_chunk;
+                }
             }
             s0 = s1;
         }
@@ -1404,6 +1499,9 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     res->stats.suspensions = suspensions;
     res->stats.search_rounds = search_rounds;
     res->stats.row_splits = row_splits;
+#if PJG_SEARCH_PROF
+    if (d_prof.p) write_search_profile(d_prof.p, st, res->stats);
+#endif
 
 done:
     if (st) {
@@ -1419,6 +1517,7 @@ done:
         dfree(d_r_warn, st); dfree(d_r_hatoms, st); dfree(d_r_src, st); dfree(d_r_hidx, st); dfree(d_r_widx, st);
         dfree(d_r_aidx, st); dfree(d_lstate, st); dfree(d_work, st); dfree(d_nwork, st); dfree(d_nsusp, st);
         dfree(d_susp_a, st); dfree(d_susp_b, st); dfree(d_pool_a, st); dfree(d_pool_b, st); dfree(d_pool_used, st);
+        dfree(d_prof, st);
         for (auto &b : scan_tmp) dfree(b, st);
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);

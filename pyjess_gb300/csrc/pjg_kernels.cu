@@ -1802,6 +1802,25 @@ __device__ __noinline__ bool decide_fp64(unsigned exact_mask, int lev, const int
     return kd_path_reaches(leaf_atom_list, mc, cr, xyz, Bmin, Bmax);
 }
 
+// Search profile probes (PJG_SEARCH_PROF builds): lane 0 of each warp adds
+// to its row of a shared array, flushed to sa.prof when the warp exits.
+#if PJG_SEARCH_PROF
+#define SPROF_ADD(i, v)                                                     \
+    do {                                                                    \
+        if (lane == 0) sprof[wib][i] += (unsigned long long)(v);            \
+    } while (0)
+#define SPROF_T(name) const long long name = clock64()
+#define SPROF_CYC(i, t0) SPROF_ADD(i, clock64() - (t0))
+#else
+#define SPROF_ADD(i, v) \
+    do {                \
+    } while (0)
+#define SPROF_T(name)
+#define SPROF_CYC(i, t0) \
+    do {                 \
+    } while (0)
+#endif
+
 template <typename PosT, bool FP32>
 __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
     k_search(ChunkView cv, TemplateView tv, CandView cd, SearchArgs sa, int32_t *pair_counter,
@@ -1810,6 +1829,12 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
     using E = Entry<PosT>;
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
+#if PJG_SEARCH_PROF
+    __shared__ unsigned long long sprof[SEARCH_WARPS][SP_NUM];
+    if (lane < SP_NUM) sprof[wib][lane] = 0;
+    __syncwarp();
+    unsigned long long sp_fp64 = 0;  // this lane's FP64 decisions
+#endif
     unsigned char *wbase = smem + (size_t)wib * sa.warp_smem;
     PairState &st = *reinterpret_cast<PairState *>(wbase);
     const size_t o2 = (sizeof(PairState) + 15) & ~size_t(15);
@@ -1844,6 +1869,8 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
         if (lane == 0) item = atomicAdd(pair_counter, 1);
         item = __shfl_sync(FULL_MASK, item, 0);
         if (item >= n_items || timed_out) break;
+        SPROF_T(t_pair);
+        SPROF_ADD(SP_PAIRS, 1);
         const int pair = fresh ? item : dm.resume[item].pair;
         const int64_t skip = fresh ? 0 : dm.resume[item].skip;
         const int64_t saved = fresh ? -1 : dm.resume[item].state;
@@ -1878,7 +1905,11 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                 atomicAdd(&counters[C_CAND], (unsigned long long)cc);
             }
         }
-        if (zero) continue;
+        if (zero) {
+            SPROF_ADD(SP_EMPTY, 1);
+            SPROF_CYC(SP_CYC_PAIR, t_pair);
+            continue;
+        }
         if (n > 32) {
             if (lane == 0) atomicMax(&counters[C_ERROR], 1ull);
             continue;
@@ -1951,6 +1982,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
         auto emit = [&](bool pass, const int32_t *pos, int lastpos) -> void {
             unsigned m = __ballot_sync(FULL_MASK, pass);
             if (!m) return;
+            SPROF_T(t_emit);
             double rm = 0.0;
             int32_t at[32];
             if (pass) {
@@ -2006,8 +2038,11 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
             }
             emitted += np;
             if (stop_at >= 0 && emitted >= stop_at) stop = true;
+            SPROF_ADD(SP_ROWS, np);
+            SPROF_CYC(SP_CYC_EMIT, t_emit);
         };
 
+        SPROF_CYC(SP_CYC_SETUP, t_pair);
         if (n == 1) {
             // Scanner_next with one level advances the seed index before
             // reporting (patches/Scanner.c.patch:244-263): seeds 1..m0-1
@@ -2056,8 +2091,10 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
             }
             while (!stop) {
                 if (over_budget()) break;
+                SPROF_ADD(SP_LOOP_ITERS, 1);
                 if (lev < 0) {
                     if (root >= m0) break;
+                    SPROF_T(t_seed);
                     int kk = min(cap, m0 - root);
                     E *t0 = tiles + st.tile[0];
                     for (int i = lane; i < kk; i += 32) {
@@ -2077,6 +2114,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                     __syncwarp();
                     lev = 0;
                     chain_lev = -1;
+                    SPROF_CYC(SP_CYC_SEED, t_seed);
                     continue;
                 }
                 const int child = lev + 1;
@@ -2171,6 +2209,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                 int cr = 0;
                 int my_parent = 0;      // product mode: this lane's parent entry
                 int32_t chainpos[32];   // product mode: this lane's parent chain
+                SPROF_T(t_exp);
                 if (mc >= PJG_BLOCK_MIN) {
                     // ---------------- block mode ----------------
                     if (!last && cap - ccnt < 32) {
@@ -2195,6 +2234,8 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                     // tile cannot take another batch.  The boxes of the first
                     // 32 blocks do not depend on the chain: their loads are
                     // issued before the chain is gathered.
+                    SPROF_ADD(SP_BLOCK_VISITS, 1);
+                    SPROF_ADD(SP_BLOCK_VISITS_L0, lev == 0);
                     const int nblk = (mc + 31) >> 5;
                     const int pstart = st.cnd[lev];
                     const int gfirst = pstart >> 5;
@@ -2211,6 +2252,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                             // a sibling of the previous parent: levels below
                             // lev are unchanged, only this parent's point
                             // and box are new
+                            SPROF_ADD(SP_CHAIN_SIBLING, 1);
                             if (lane == lev) {
                                 const float4 cj = level_xyz(lev, (int)pe.pos);
                                 st.cxyz[lev] = cj;
@@ -2225,6 +2267,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                             }
                         } else {
                             // positions of the parent's chain, by walking the tiles
+                            SPROF_ADD(SP_CHAIN_FULL, 1);
                             __syncwarp();
                             if (lane == 0) {
                                 int idx = ppar;
@@ -2286,6 +2329,8 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                     // full test of queue entries 0..k-1 (lane i takes entry i),
                     // then the entries after them move to the queue's front
                     auto run_batch = [&](int k) {
+                        SPROF_ADD(SP_BATCHES, 1);
+                        SPROF_ADD(SP_BATCH_LANES, k);
                         cr = lane < k ? st.qpos[lane] : 0;
                         const float4 xc = lane < k ? st.qxyz[lane] : make_float4(0.f, 0.f, 0.f, 0.f);
                         pass = false;
@@ -2314,6 +2359,9 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                             }
                             if (pass && exact) {
                                 if (FP32) rechecks += __popc(exact);
+#if PJG_SEARCH_PROF
+                                sp_fp64++;
+#endif
                                 int32_t atoms[32];
                                 for (int j = 0; j <= lev; j++) atoms[j] = level_atom(j, st.cpos[j]);
                                 pass = decide_fp64(exact, lev, atoms, cd.leaf_atom[coff + cr], xyz64, prm, st.order,
@@ -2321,6 +2369,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                             }
                         }
                         const unsigned m = __ballot_sync(FULL_MASK, pass);
+                        SPROF_ADD(SP_CHILD_BLOCK, __popc(m));
                         if (last) {
                             int32_t pos[32];
                             for (int j = 0; j <= lev; j++) pos[j] = st.cpos[j];
@@ -2363,6 +2412,9 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                             bh = cd.blk_hi[boff + b + 32];
                         }
                         unsigned hm = __ballot_sync(FULL_MASK, hit);
+                        SPROF_ADD(SP_G0_ITERS, 1);
+                        SPROF_ADD(SP_BLOCKS_TESTED, min(32, nblk - g0));
+                        SPROF_ADD(SP_BLOCKS_HIT, __popc(hm));
                         // hit blocks in order; the leaves of the next hit
                         // block are loaded while the current one is queued
                         int nxt = -1;
@@ -2386,6 +2438,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                                              !(xc.x < box_lo[0] || xc.x > box_hi[0] || xc.y < box_lo[1] ||
                                                xc.y > box_hi[1] || xc.z < box_lo[2] || xc.z > box_hi[2]);
                             const unsigned im = __ballot_sync(FULL_MASK, inb);
+                            SPROF_ADD(SP_LEAVES_INBOX, __popc(im));
                             if (inb) {
                                 const int qi = queued + __popc(im & ((1u << lane) - 1u));
                                 st.qpos[qi] = q;
@@ -2425,6 +2478,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                     }
                     __syncwarp();
                     if (resume >= 0) lev = child;
+                    SPROF_CYC(SP_CYC_BLOCK, t_exp);
                     continue;
                 } else {
                     // ---------------- product mode ----------------
@@ -2444,6 +2498,9 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                     const int p = ppar + tt / mc;
                     cr = tt % mc;
                     const bool valid = lane < batch && p < pcnt;
+                    SPROF_ADD(SP_PROD_BATCHES, 1);
+                    SPROF_ADD(SP_PROD_BATCHES_L0, lev == 0);
+                    SPROF_ADD(SP_PROD_LANES, __popc(__ballot_sync(FULL_MASK, valid)));
                     if (valid) {
                         int idx = p;
                         for (int j = lev; j >= 0; j--) {
@@ -2476,6 +2533,9 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         }
                         if (pass && exact) {
                             if (FP32) rechecks += __popc(exact);
+#if PJG_SEARCH_PROF
+                            sp_fp64++;
+#endif
                             int32_t atoms[32];
                             for (int j = 0; j <= lev; j++) atoms[j] = level_atom(j, chainpos[j]);
                             pass = decide_fp64(exact, lev, atoms, cd.leaf_atom[coff + cr], xyz64, prm, st.order, n,
@@ -2501,6 +2561,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                 // ---- children / complete rows
                 const bool block_mode = mc >= PJG_BLOCK_MIN;
                 unsigned m = __ballot_sync(FULL_MASK, pass);
+                SPROF_ADD(SP_CHILD_PROD, __popc(m));
                 if (last) {
                     if (block_mode) {
                         int32_t pos[32];
@@ -2548,9 +2609,11 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         lev = child;
                     }
                 }
+                SPROF_CYC(SP_CYC_PROD, t_exp);
             }
         }
         __syncwarp();
+        SPROF_CYC(SP_CYC_PAIR, t_pair);
         if (suspended) continue;
         if (lane == 0 && emitted > 0) out.pair_rows[pair] = (int32_t)emitted;
         // ---- statistics of the pair
@@ -2567,6 +2630,12 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
         }
         __syncwarp();
     }
+#if PJG_SEARCH_PROF
+    for (int o = 16; o; o >>= 1) sp_fp64 += __shfl_xor_sync(FULL_MASK, sp_fp64, o);
+    SPROF_ADD(SP_FP64, sp_fp64);
+    __syncwarp();
+    if (sa.prof && lane < SP_NUM) atomicAdd(&sa.prof[lane], sprof[wib][lane]);
+#endif
 }
 
 

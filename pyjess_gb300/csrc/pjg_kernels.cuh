@@ -34,6 +34,43 @@ constexpr int LEAF_SORTED_MAX = 2048;  // longest list ordered by sorted axes
 constexpr int LEAF_SORT_MAX = 1024;    // longest list ordered by presorted axes
 constexpr int EXACT_MAX = 4096;        // longest list replayed warp-parallel
 
+// Search profile: event counts and clock64 cycles of k_search's sections,
+// summed over warps.  Compiled only with -DPJG_SEARCH_PROF=1 (a separate
+// library variant used to explain the kernel's cost; the timed build has
+// none of it).
+#ifndef PJG_SEARCH_PROF
+#define PJG_SEARCH_PROF 0
+#endif
+enum SearchProf : int {
+    SP_PAIRS = 0,        // pairs taken from the queue
+    SP_EMPTY,            // pairs with an empty candidate list
+    SP_CYC_PAIR,         // cycles from taking a pair to finishing it
+    SP_CYC_SETUP,        // cycles of a pair's set-up (lengths, order, levels)
+    SP_CYC_SEED,         // cycles filling level-0 tiles
+    SP_CYC_BLOCK,        // cycles in block-mode expansions
+    SP_CYC_PROD,         // cycles in product-mode expansions
+    SP_CYC_EMIT,         // cycles in emit (inside the two above)
+    SP_LOOP_ITERS,       // iterations of the depth-first loop
+    SP_BLOCK_VISITS,     // block-mode visits of a parent
+    SP_BLOCK_VISITS_L0,  //   of which from level 0
+    SP_CHAIN_FULL,       // parent chains gathered by walking the tiles
+    SP_CHAIN_SIBLING,    // parent chains reused from a sibling
+    SP_G0_ITERS,         // 32-block steps of the block scan
+    SP_BLOCKS_TESTED,    // block boxes tested against the join box
+    SP_BLOCKS_HIT,       // blocks whose box meets the join box
+    SP_LEAVES_INBOX,     // leaves inside the join box (queued)
+    SP_BATCHES,          // full-test batches
+    SP_BATCH_LANES,      // queued leaves fully tested
+    SP_CHILD_BLOCK,      // children / rows from block mode
+    SP_PROD_BATCHES,     // product-mode batches
+    SP_PROD_BATCHES_L0,  //   of which from level 0
+    SP_PROD_LANES,       // (parent, candidate) tests in product mode
+    SP_CHILD_PROD,       // children / rows from product mode
+    SP_FP64,             // candidates decided in FP64
+    SP_ROWS,             // complete rows emitted
+    SP_NUM
+};
+
 struct SearchArgs {
     int32_t n_pairs;                   // chunk structures x templates
     int32_t ignore_chain;
@@ -45,6 +82,8 @@ struct SearchArgs {
                                        // searching (non-best mode)
     double rmsd_threshold;
     uint64_t budget_ns;                // per-warp wall-time budget (globaltimer)
+    unsigned long long *prof;          // [SP_NUM] search profile (profile
+                                       // builds only, else nullptr)
 };
 
 // A pair whose search stopped at a level whose candidate list had no kd

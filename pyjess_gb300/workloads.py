@@ -311,6 +311,7 @@ class Workload:
     structures: PackedStructures
     params: dict
     notes: str = ""
+    n_adversarial: int = 0      # structures 0 .. n_adversarial-1 are adversarial
 
     @property
     def pairs(self) -> int:
@@ -361,7 +362,7 @@ def config(index: int, *, scale: float = 1.0, n_structures=None, n_templates=Non
             notes = f"{n_adv} adversarial structures"
         label = "cfg2" if index == 2 else "cfg3"
         return Workload(f"{label}: {ns} structures x {nt} templates", pack_templates(specs), pack(structs),
-                        params, notes)
+                        params, notes, n_adv)
     if index == 4:
         ns = n_structures or max(1, int(round(500 * scale)))
         nt = n_templates or max(1, int(round(500 * scale)))

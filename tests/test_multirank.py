@@ -25,7 +25,7 @@ def _rank(rank, world, port, out):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
-        args = argparse.Namespace(structures=3, templates=4)
+        args = argparse.Namespace(config=3, structures=3, templates=4)
         wl = bench.workload(args, rank, world)
         out[rank] = {
             "max": bench.max_over_ranks(10.0 + rank, dist),
@@ -59,7 +59,7 @@ def test_single_rank_is_config3():
     import bench
     from pyjess_gb300 import workloads as W
 
-    args = argparse.Namespace(structures=3, templates=4)
+    args = argparse.Namespace(config=3, structures=3, templates=4)
     a = bench.workload(args, 0, 1)
     b = W.config(3, n_structures=3, n_templates=4)
     assert (a.structures.xyz == b.structures.xyz).all()
