@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--plain-structures", type=int, default=-1,
                     help="structures run through the plain FP64 per-structure path (-1: all, 0: none)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--search-profile", action="store_true",
                     help="run the search-profile build of the library and print k_search's event counts "
                          "and section cycles (not a bench line)")
@@ -382,7 +383,7 @@ def main():
     # ---- CPU baseline (rank 0, N=1): the same strided sample as the
     # reference arm, median of three runs
     cpu = None
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         idx = cpu_structures(wl, args.cpu_stride)
         runs = [cpu_sample(wl, idx, threads) for _ in range(3)]

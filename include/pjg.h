@@ -252,8 +252,11 @@ void pjg_results_destroy(pjg_results *r);
  * argument, return PJG_ERR_INVALID with a message from
  * pjg_noalloc_last_error().  The first call on each device looks up that
  * array's device address with the device current; make that first call
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race, so serialise them. */
+ * before any stream capture.  The address is kept per device together with
+ * the id of the CUDA context it belongs to: after the context is reset
+ * (cudaDeviceReset), the next call looks it up again, so that call too
+ * should come before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU race, so serialise them. */
 #define PJG_NOALLOC_MAX_ROWS (1 << 20)
 pjg_status pjg_superpose_noalloc(const double *mol_xyz, const double *tpl_xyz, int32_t n_rows, int32_t n_atoms,
                                  double rmsd_threshold, double *rmsd, double *rotation, double *centres,

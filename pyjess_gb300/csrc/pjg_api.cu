@@ -162,6 +162,9 @@ struct pjg_templates {
     uint32_t *d_names = nullptr, *d_resnames = nullptr, *d_partner_res = nullptr, *d_partner_name = nullptr;
     int64_t n_params = 0;
     int device = 0;
+    // templates of more than 32 atoms (searched by k_search_large)
+    std::vector<int32_t> large;
+    int32_t *d_large = nullptr;
 };
 
 struct pjg_structures {
@@ -384,10 +387,12 @@ pjg_status pjg_templates_create(const pjg_template_set *set, pjg_templates **out
             delete h;
             return fail(PJG_ERR_INVALID, "template %d: decreasing atom offsets", t);
         }
-        if (a1 - a0 > 32) {
+        if (a1 - a0 > MAX_TEMPLATE_ATOMS) {
             delete h;
-            return fail(PJG_ERR_INVALID, "template %d has %d atoms; at most 32 are supported", t, a1 - a0);
+            return fail(PJG_ERR_INVALID, "template %d has %d atoms; at most %d are supported", t, a1 - a0,
+                        MAX_TEMPLATE_ATOMS);
         }
+        if (a1 - a0 > 32) h->large.push_back(t);
         h->nmax = std::max(h->nmax, a1 - a0);
     }
     for (int a = 0; a < A; a++) {
@@ -472,6 +477,11 @@ pjg_status pjg_templates_create(const pjg_template_set *set, pjg_templates **out
             }
         h->param_begin.push_back((int32_t)dist.size());
     }
+    if (dist.size() > (size_t)INT32_MAX) {
+        delete h;
+        return fail(PJG_ERR_INVALID, "templates too large: %zu distance-matrix entries (at most %d)", dist.size(),
+                    INT32_MAX);
+    }
     h->n_params = (int64_t)dist.size();
     if (set->dim) h->dim.assign(set->dim, set->dim + T);
     {
@@ -493,6 +503,7 @@ pjg_status pjg_templates_create(const pjg_template_set *set, pjg_templates **out
         if (e == cudaSuccess) e = upload(&h->d_partner_begin, s_pb);
         if (e == cudaSuccess) e = upload(&h->d_partner_res, s_pres);
         if (e == cudaSuccess) e = upload(&h->d_partner_name, s_pname);
+        if (e == cudaSuccess && !h->large.empty()) e = upload(&h->d_large, h->large);
         if (e != cudaSuccess) {
             status = fail(e == cudaErrorMemoryAllocation ? PJG_ERR_OOM : PJG_ERR_CUDA, "template upload: %s",
                           cudaGetErrorString(e));
@@ -508,7 +519,7 @@ void pjg_templates_destroy(pjg_templates *h) {
     if (!h) return;
     void *ptrs[] = {h->d_atom_begin, h->d_sig, h->d_key, h->d_param_begin, h->d_pos, h->d_weight, h->d_dist,
                     h->d_code, h->d_rule, h->d_mainchain, h->d_name_begin, h->d_names, h->d_res_begin,
-                    h->d_resnames, h->d_partner_begin, h->d_partner_res, h->d_partner_name};
+                    h->d_resnames, h->d_partner_begin, h->d_partner_res, h->d_partner_name, h->d_large};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete h;
@@ -1039,6 +1050,16 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             if (v && atoll(v) > 0) return atoll(v);
             return (int64_t)(0.7 * row_memory() / (row_buf_bytes * 1.25 + row_stage_bytes));
         };
+        // best_match with max_candidates: a pair stops after max_candidates
+        // + 2 complete rows, so a structure yields at most T times that; the
+        // chunks are sized from this bound before any search (no chunk then
+        // needs a split)
+        int bound_cap = max_chunk;
+        if (P->best_match && P->max_candidates >= 0 && max_chunk > 1) {
+            const double per = (double)T * ((double)P->max_candidates + 2.0);
+            bound_cap = (int)std::max(1.0, std::min((double)max_chunk, (double)row_budget() / per));
+            chunk_cap = bound_cap;
+        }
         int s0 = 0;
         int64_t c_cap = 1 << 20;
         CUDA_TRY(dalloc(d_c_pair, c_cap, st));
@@ -1229,8 +1250,9 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             sa.max_candidates = P->max_candidates;
             {
                 // shared memory per warp: pair state + tiles of >= 64
-                // entries for every level but the last
-                int levels = std::max(1, tp->nmax - 1);
+                // entries for every level but the last (k_search takes
+                // templates of up to 32 atoms)
+                int levels = std::max(1, std::min(tp->nmax, 32) - 1);
                 size_t entry = sp->max_atoms > 65535 ? 8 : 4;
                 size_t need = 4096 + entry * 64 * (size_t)levels;
                 sa.warp_smem = (int)((std::max<size_t>(need, 9472) + 15) & ~size_t(15));
@@ -1296,8 +1318,16 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                     CUDA_TRY(cudaEventRecord(ev[6], st));
                     CUDA_TRY(launch_search(st, grid, wide, fp32, cv, tv, cd, sa, d_pair_counter.p, scn_c, cr,
                                            d_counters.p, dm));
-                    CUDA_TRY(cudaEventRecord(ev[7], st));
                     launches++;
+                    if (round == 0 && !tp->large.empty()) {
+                        // pairs of templates over 32 atoms (every list of
+                        // theirs was ordered before this round)
+                        CUDA_TRY(cudaMemsetAsync(d_pair_counter.p, 0, sizeof(int32_t), st));
+                        CUDA_TRY(launch_search_large(st, cv, tv, cd, sa, tp->d_large, (int32_t)tp->large.size(),
+                                                     d_pair_counter.p, scn_c, cr, d_counters.p, dm.state));
+                        launches++;
+                    }
+                    CUDA_TRY(cudaEventRecord(ev[7], st));
                     CUDA_TRY(cudaGetLastError());
                     unsigned long long ns = 0, used = 0;
                     CUDA_TRY(cudaMemcpyAsync(&nc, d_ccount.p, sizeof nc, cudaMemcpyDeviceToHost, st));
@@ -1452,6 +1482,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 } else {
                     chunk_cap = max_chunk;
                 }
+                chunk_cap = std::max(chunk_cap, std::min(bound_cap, max_chunk));
             }
             s0 = s1;
         }
@@ -1468,8 +1499,9 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     if (counters[C_ERROR]) {
         const unsigned long long c = counters[C_ERROR];
         status = fail(PJG_ERR_CAPACITY, "kernel reported error %llu (%s)", c,
-                      c == 1 ? "template over 32 atoms" : c == 2 ? "template too large for the frontier tile"
+                      c == 2 ? "template too large for the frontier tile"
                       : c == 4 ? "leaf order: too many small subtrees" : c == 5 ? "leaf order: partition did not converge"
+                      : c == 7 ? "a list of a template over 32 atoms had no kd leaf order"
                       : "leaf order: inconsistent node partition");
         goto done;
     }

@@ -137,7 +137,8 @@ enum Counter : int {
     C_LEAF_REPLAY,    // kd nodes replayed by qselect in the sorted-axis path
     C_LEAF_LISTS,     // lists put in kd leaf order
     C_LEAF_ENTRIES,   // entries of those lists
-    C_ERROR,          // error code: 1 template > 32 atoms, 2 frontier tile too
+    C_ERROR,          // error code: 7 an unordered list of a template over
+                      // 32 atoms (internal), 2 frontier tile too
                       // small, 3 time budget exhausted, 4 leaf order: too many
                       // small subtrees, 5 a partition did not converge, 6 an
                       // inconsistent node partition (0 = none)

@@ -4,12 +4,25 @@
 // 110-336) + KdTree range queries (patches/KdTree.c.patch:226-298) +
 // superposition (patches/Super.c.patch) with:
 //
-//   k_params      annulus radii of every ordered template-atom pair
-//   k_candidates  candidate lists per (structure, signature), count + fill
-//   k_scan_*      exclusive scan of list lengths
-//   k_leaf_order  the kd-tree leaf order of each list (exact qselect replay)
-//   k_search      warp-per-pair, order-preserving frontier expansion
-//   k_superpose   warp-per-candidate FP64 quaternion superposition
+//   k_params            annulus radii of every ordered template-atom pair
+//   k_candidate_counts  candidate-list lengths per (structure, signature)
+//                       from the per-bucket histograms of atom names
+//   k_candidates        the lists themselves, in candidate (ResIndex) order
+//   k_scan_*            exclusive scans of list lengths and row counts
+//   k_axis_ranks        per-structure axis ranks (once, at upload)
+//   k_demand_levels     requests the kd leaf order of the lists a pair
+//                       reaches first
+//   k_leaf_order        kd leaf order of short tie-free lists by ranks (tied
+//                       or longer lists are passed on)
+//   k_leaf_sorted<M>    kd leaf order by sorted-axis splits, with a qselect
+//                       replay of tied nodes
+//   k_leaf_exact<M>     the literal qselect sequence, for the rest
+//   k_search            persistent warp per pair, order-preserving
+//                       depth-first-over-tiles frontier expansion
+//   k_superpose         thread per complete row, FP64 covariance and
+//                       quaternion eigen-solve
+//   k_order_counts, k_automaton, k_gather_hits
+//                       Query.__next__ per pair and compaction of the hits
 //
 // FP64 arithmetic that decides a hit is written with __dadd_rn/__dsub_rn/
 // __dmul_rn so it is never contracted into FMA and matches the reference's
@@ -1394,7 +1407,36 @@ __global__ void k_demand_levels(TemplateView tv, CandView cd, int32_t n_pairs, i
         const int s = (int)(pair / T), t = (int)(pair % T);
         const int ab = tv.atom_begin[t];
         const int n = tv.atom_begin[t + 1] - ab;
-        if (n < 2 || n > 32) continue;
+        if (n < 2) continue;
+        if (n > 32) {
+            // k_search_large: every list but the level-0 one, before the
+            // search (those pairs never suspend)
+            bool empty = false;
+            int best = INT_MAX, best_k = 0;  // the level-0 atom: smallest (length, index)
+            for (int k = lane; k < n; k += 32) {
+                const int c = cd.count[(int64_t)s * G + tv.sig[ab + k]];
+                if (c == 0) empty = true;
+                if (c < best) {
+                    best = c;
+                    best_k = k;
+                }
+            }
+            if (__any_sync(FULL_MASK, empty)) continue;
+            for (int o = 16; o; o >>= 1) {
+                const int ob = __shfl_xor_sync(FULL_MASK, best, o), ok = __shfl_xor_sync(FULL_MASK, best_k, o);
+                if (ob < best || (ob == best && ok < best_k)) {
+                    best = ob;
+                    best_k = ok;
+                }
+            }
+            const int k0 = reorder ? best_k : 0;
+            for (int k = lane; k < n; k += 32)
+                if (k != k0) {
+                    const int64_t w = (int64_t)s * G + tv.sig[ab + k];
+                    request_list(dm, w, cd.count[w]);
+                }
+            continue;
+        }
         int c = INT_MAX;
         int64_t w = 0;
         if (lane < n) {
@@ -1608,13 +1650,15 @@ __device__ void quaternion_fit(const double S[9], double E0, int n, double *rmsd
 }
 
 // Centroids, centred covariance S = sum a b^T and E0 = (|a|^2 + |b|^2) / 2
-// of one assignment, by one thread (sums in template atom order).
-__device__ void lane_covariance(int n, const int32_t *atoms, const double *xyz, const double *tpos, double ca[3],
-                                double cb[3], double S[9], double *E0) {
+// of one assignment, by one thread (sums in template atom order); atom(k)
+// is the molecule atom matched to template atom k.
+template <typename AtomOf>
+__device__ __forceinline__ void lane_covariance_by(int n, AtomOf atom, const double *xyz, const double *tpos,
+                                                   double ca[3], double cb[3], double S[9], double *E0) {
     for (int d = 0; d < 3; d++) ca[d] = cb[d] = 0.0;
     for (int k = 0; k < n; k++)
         for (int d = 0; d < 3; d++) {
-            ca[d] += xyz[3 * (int64_t)atoms[k] + d];
+            ca[d] += xyz[3 * (int64_t)atom(k) + d];
             cb[d] += tpos[3 * k + d];
         }
     for (int d = 0; d < 3; d++) {
@@ -1626,7 +1670,7 @@ __device__ void lane_covariance(int n, const int32_t *atoms, const double *xyz, 
     for (int k = 0; k < n; k++) {
         double a[3], b[3];
         for (int d = 0; d < 3; d++) {
-            a[d] = xyz[3 * (int64_t)atoms[k] + d] - ca[d];
+            a[d] = xyz[3 * (int64_t)atom(k) + d] - ca[d];
             b[d] = tpos[3 * k + d] - cb[d];
         }
         sumA += a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
@@ -1637,11 +1681,17 @@ __device__ void lane_covariance(int n, const int32_t *atoms, const double *xyz, 
     *E0 = 0.5 * (sumA + sumB);
 }
 
+__device__ void lane_covariance(int n, const int32_t *atoms, const double *xyz, const double *tpos, double ca[3],
+                                double cb[3], double S[9], double *E0) {
+    lane_covariance_by(n, [&](int k) { return atoms[k]; }, xyz, tpos, ca, cb, S, E0);
+}
+
 // RMSD of one assignment computed by a single thread, used where a lane
 // needs the value while searching (the same arithmetic as k_superpose).
-__device__ double lane_rmsd(int n, const int32_t *atoms, const double *xyz, const double *tpos) {
+template <typename AtomOf>
+__device__ double lane_rmsd_by(int n, AtomOf atom, const double *xyz, const double *tpos) {
     double ca[3], cb[3], S[9], E0;
-    lane_covariance(n, atoms, xyz, tpos, ca, cb, S, &E0);
+    lane_covariance_by(n, atom, xyz, tpos, ca, cb, S, &E0);
     double K[4][4];
     key_matrix(S, K);
     bool close = false;
@@ -1651,6 +1701,10 @@ __device__ double lane_rmsd(int n, const int32_t *atoms, const double *xyz, cons
         lam = jacobi4_top(K, v);
     }
     return rmsd_from_lambda(E0, lam, n);
+}
+
+__device__ double lane_rmsd(int n, const int32_t *atoms, const double *xyz, const double *tpos) {
+    return lane_rmsd_by(n, [&](int k) { return atoms[k]; }, xyz, tpos);
 }
 
 // ---------------------------------------------------------------------------
@@ -1804,6 +1858,8 @@ __device__ __noinline__ bool decide_fp64(unsigned exact_mask, int lev, const int
 
 // Search profile probes (PJG_SEARCH_PROF builds): lane 0 of each warp adds
 // to its row of a shared array, flushed to sa.prof when the warp exits.
+// The value argument is evaluated by lane 0 alone: it must not contain a
+// warp-collective (ballot, shuffle), which every lane has to execute.
 #if PJG_SEARCH_PROF
 #define SPROF_ADD(i, v)                                                     \
     do {                                                                    \
@@ -1878,7 +1934,8 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
         const int t = pair % T;
         const int ab = tv.atom_begin[t];
         const int n = tv.atom_begin[t + 1] - ab;
-        if (n <= 0) continue;
+        // templates of more than 32 atoms are searched by k_search_large
+        if (n <= 0 || n > 32) continue;
         const int64_t abase = cv.atom_base[s];
         const double *xyz64 = cv.xyz64 + 3 * abase;
 
@@ -1908,10 +1965,6 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
         if (zero) {
             SPROF_ADD(SP_EMPTY, 1);
             SPROF_CYC(SP_CYC_PAIR, t_pair);
-            continue;
-        }
-        if (n > 32) {
-            if (lane == 0) atomicMax(&counters[C_ERROR], 1ull);
             continue;
         }
 
@@ -2500,7 +2553,13 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                     const bool valid = lane < batch && p < pcnt;
                     SPROF_ADD(SP_PROD_BATCHES, 1);
                     SPROF_ADD(SP_PROD_BATCHES_L0, lev == 0);
-                    SPROF_ADD(SP_PROD_LANES, __popc(__ballot_sync(FULL_MASK, valid)));
+#if PJG_SEARCH_PROF
+                    {
+                        // every lane takes part in the ballot; lane 0 adds
+                        const unsigned vm = __ballot_sync(FULL_MASK, valid);
+                        SPROF_ADD(SP_PROD_LANES, __popc(vm));
+                    }
+#endif
                     if (valid) {
                         int idx = p;
                         for (int j = lev; j >= 0; j--) {
@@ -2638,6 +2697,297 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
 #endif
 }
 
+
+// ---------------------------------------------------------------------------
+// Search for templates of more than 32 atoms (k_search keeps one level per
+// lane, so it takes at most 32).  Warp per pair, the reference's
+// depth-first backtracking taken literally: one chain of atoms, and at each
+// level the next 32 leaf positions tested by the lanes at once, the passing
+// ones expanded one after the other in leaf order (their ballot mask is kept
+// per level, so every position is tested once per parent).  Every distance
+// test is the reference's FP64 arithmetic (annulus64, plus the kd path
+// check for a point outside an annulus box).  Every list of these pairs is
+// in kd leaf order before the first search round (k_demand_levels requests
+// them all), so they never suspend.  Per-warp state in dynamic shared
+// memory, 52 bytes a template atom (large_warp_bytes).
+
+__device__ __forceinline__ bool decide_fp64_chain(int levp, const int32_t *catom, int32_t an, const double *xyz,
+                                                  const AnnulusParam *prm, const int32_t *order, int n, int qn,
+                                                  const int32_t *leaf_atom_list, int mc, int cr) {
+    bool need_path = false;
+    const double *x = xyz + 3 * (int64_t)an;
+    for (int j = 0; j <= levp; j++) {
+        bool inb;
+        if (!annulus64(xyz + 3 * (int64_t)catom[j], x, prm[order[j] * n + qn], &inb)) return false;
+        if (!inb) need_path = true;
+    }
+    if (!need_path) return true;
+    double Bmin[3] = {-INFINITY, -INFINITY, -INFINITY};
+    double Bmax[3] = {INFINITY, INFINITY, INFINITY};
+    for (int j = 0; j <= levp; j++) {
+        const double *cj = xyz + 3 * (int64_t)catom[j];
+        const double bj = prm[order[j] * n + qn].b;
+        for (int i = 0; i < 3; i++) {
+            const double lo = __dsub_rn(cj[i], bj), hi = __dadd_rn(cj[i], bj);
+            Bmin[i] = Bmin[i] > lo ? Bmin[i] : lo;
+            Bmax[i] = Bmax[i] < hi ? Bmax[i] : hi;
+        }
+    }
+    return kd_path_reaches(leaf_atom_list, mc, cr, xyz, Bmin, Bmax);
+}
+
+__global__ void __launch_bounds__(LARGE_WARPS * 32)
+    k_search_large(ChunkView cv, TemplateView tv, CandView cd, SearchArgs sa, const int32_t *large, int32_t n_large,
+                   int32_t *item_counter, const int32_t *scanned, CompleteRows out, unsigned long long *counters,
+                   const int32_t *lstate) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = lane_id();
+    const int nmax = tv.max_atoms;
+    unsigned char *wb = smem + (size_t)(threadIdx.x >> 5) * large_warp_bytes(nmax);
+    int64_t *lvl_off = reinterpret_cast<int64_t *>(wb);  // list offset of each level
+    int64_t *F = lvl_off + nmax;                         // partial assignments per level
+    int32_t *lvl_cnt = reinterpret_cast<int32_t *>(F + nmax);
+    int32_t *order = lvl_cnt + nmax;                     // template atom of each level
+    int32_t *tkey = order + nmax;                        // its key bits
+    int32_t *catom = tkey + nmax;                        // chain: atom of each level
+    int32_t *ckey = catom + nmax;                        //   its key bits
+    int32_t *trow = ckey + nmax;                         //   atoms by template atom
+    int32_t *next = trow + nmax;                         // next untested position per level
+    int32_t *cbase = next + nmax;                        // first position of the last tested batch
+    uint32_t *rem = reinterpret_cast<uint32_t *>(cbase + nmax);  // its passing lanes not yet expanded
+    const int T = tv.n_templates, G = cd.n_sigs;
+    uint64_t t_start = 0;
+    if (lane == 0) t_start = global_ns();
+    bool timed_out = false;
+    uint32_t ticks = 0;
+    const int64_t n_items = (int64_t)cv.n_structures * n_large;
+    for (;;) {
+        int64_t item = 0;
+        if (lane == 0) item = atomicAdd(item_counter, 1);
+        item = __shfl_sync(FULL_MASK, item, 0);
+        if (item >= n_items || timed_out) break;
+        const int s = (int)(item / n_large);
+        const int t = large[item % n_large];
+        const int pair = s * T + t;
+        const int ab = tv.atom_begin[t];
+        const int n = tv.atom_begin[t + 1] - ab;
+        const int64_t abase = cv.atom_base[s];
+        const double *xyz64 = cv.xyz64 + 3 * abase;
+        // lengths, empty-set skip and statistics (template atom order), as
+        // k_search
+        int first_zero = n;
+        for (int k = lane; k < n; k += 32) {
+            const int c = cd.count[(int64_t)s * G + tv.sig[ab + k]];
+            next[k] = c;  // lengths by template atom, for the level order
+            if (c == 0) first_zero = min(first_zero, k);
+        }
+        for (int o = 16; o; o >>= 1) first_zero = min(first_zero, __shfl_xor_sync(FULL_MASK, first_zero, o));
+        {
+            const int kstop = first_zero < n ? first_zero : n - 1;
+            long long bc = 0, cc = 0;
+            for (int k = lane; k <= kstop; k += 32) {
+                const int64_t lw = (int64_t)s * G + tv.sig[ab + k];
+                bc += 8LL * scanned[lw] + 16LL * cd.count[lw];
+                cc += cd.count[lw];
+            }
+            for (int o = 16; o; o >>= 1) {
+                bc += __shfl_xor_sync(FULL_MASK, bc, o);
+                cc += __shfl_xor_sync(FULL_MASK, cc, o);
+            }
+            if (lane == 0) {
+                atomicAdd(&counters[C_PAIRS], 1ull);
+                atomicAdd(&counters[C_BYTES_CAND], (unsigned long long)bc);
+                atomicAdd(&counters[C_CAND], (unsigned long long)cc);
+            }
+        }
+        __syncwarp();
+        if (first_zero < n) continue;
+        // level order: stable by list length, ties by index
+        for (int k = lane; k < n; k += 32) {
+            int r = k;
+            if (sa.reorder) {
+                const int ck = next[k];
+                r = 0;
+                for (int j = 0; j < n; j++) {
+                    const int cj = next[j];
+                    r += (cj < ck || (cj == ck && j < k));
+                }
+            }
+            order[r] = k;
+        }
+        __syncwarp();
+        bool unordered = false;
+        for (int l = lane; l < n; l += 32) {
+            const int k = order[l];
+            const int64_t w2 = (int64_t)s * G + tv.sig[ab + k];
+            // every list but level 0's must be in kd leaf order by now
+            if (l > 0 && lstate && lstate[w2] != 2) unordered = true;
+            lvl_off[l] = l == 0 ? cd.offset[w2] : cd.leaf_offset[w2];
+            lvl_cnt[l] = cd.count[w2];
+            tkey[l] = tv.key[ab + k];
+            F[l] = 0;
+            next[l] = 0;
+            rem[l] = 0;
+            cbase[l] = 0;
+        }
+        if (__any_sync(FULL_MASK, unordered)) {
+            if (lane == 0) atomicMax(&counters[C_ERROR], 7ull);
+            continue;
+        }
+        __syncwarp();
+        const AnnulusParam *prm = tv.params + tv.param_begin[t];
+        const double *tpos = tv.pos + 3 * (int64_t)ab;
+        const int klast = order[n - 1];
+        const int m0 = lvl_cnt[0];
+        const int64_t off0 = lvl_off[0];
+        int64_t emitted = 0, cut_base = 0;
+        bool stop = false;
+        const int64_t stop_at = (sa.best_match && sa.max_candidates >= 0) ? (int64_t)sa.max_candidates + 2 : -1;
+        int lev = 0;
+        while (!stop) {
+            if ((++ticks & 255u) == 0) {
+                int over = 0;
+                if (lane == 0) over = (global_ns() - t_start) > sa.budget_ns;
+                if (__shfl_sync(FULL_MASK, over, 0)) {
+                    timed_out = true;
+                    if (lane == 0) atomicMax(&counters[C_ERROR], 3ull);
+                    break;
+                }
+            }
+            if (lev == 0) {
+                // next seed, in candidate order
+                const int p = next[0];
+                if (p >= m0) break;
+                const int32_t a = cd.cand_atom[off0 + p];
+                __syncwarp();
+                if (lane == 0) {
+                    next[0] = p + 1;
+                    catom[0] = a;
+                    ckey[0] = __float_as_int(cv.xyz32[abase + a].w);
+                    trow[order[0]] = a;
+                    F[0]++;
+                    next[1] = 0;
+                    rem[1] = 0;
+                }
+                __syncwarp();
+                lev = 1;
+                continue;
+            }
+            const bool last = lev == n - 1;
+            if (!last && rem[lev]) {
+                // the next passing leaf of the batch tested last
+                const unsigned r = rem[lev];
+                const int pos = cbase[lev] + __ffs(r) - 1;
+                const int32_t a = cd.leaf_atom[lvl_off[lev] + pos];
+                __syncwarp();
+                if (lane == 0) {
+                    rem[lev] = r & (r - 1);
+                    catom[lev] = a;
+                    ckey[lev] = __float_as_int(cv.xyz32[abase + a].w);
+                    trow[order[lev]] = a;
+                    next[lev + 1] = 0;
+                    rem[lev + 1] = 0;
+                }
+                __syncwarp();
+                lev++;
+                continue;
+            }
+            const int mc = lvl_cnt[lev];
+            const int base = next[lev];
+            if (base >= mc) {
+                lev--;
+                continue;
+            }
+            // full test of leaf positions base .. base + 31
+            const int p = base + lane;
+            const int qn = order[lev];
+            const int32_t tn = tkey[lev];
+            bool pass = false;
+            int32_t an = 0;
+            if (p < mc) {
+                an = cd.leaf_atom[lvl_off[lev] + p];
+                const int32_t kn = __float_as_int(cv.xyz32[abase + an].w);
+                pass = true;
+                for (int j = 0; j < lev; j++)
+                    if (!check_pair(ckey[j], kn, tkey[j], tn, sa.ignore_chain)) {
+                        pass = false;
+                        break;
+                    }
+                if (pass)
+                    pass = decide_fp64_chain(lev - 1, catom, an, xyz64, prm, order, n, qn,
+                                             cd.leaf_atom + lvl_off[lev], mc, p);
+            }
+            unsigned m = __ballot_sync(FULL_MASK, pass);
+            __syncwarp();
+            if (lane == 0) {
+                F[lev] += __popc(m);
+                next[lev] = base + 32;
+                if (!last) {
+                    rem[lev] = m;
+                    cbase[lev] = base;
+                }
+            }
+            __syncwarp();
+            if (!last || !m) continue;
+            // complete rows, in leaf order (Query.__next__'s max_candidates
+            // cut applied inline in non-best mode, as in k_search)
+            auto atom_of = [&](int k) -> int32_t { return k == klast ? an : trow[k]; };
+            double rm = 0.0;
+            if (sa.cut_inline) {
+                bool hitf = false;
+                if (pass) {
+                    rm = lane_rmsd_by(n, atom_of, xyz64, tpos);
+                    hitf = rm <= sa.rmsd_threshold && n >= 3;
+                }
+                const unsigned hl = __ballot_sync(FULL_MASK, hitf);
+                unsigned mm = m;
+                int r = 0, keep = 32;
+                while (mm) {
+                    const int ln = __ffs(mm) - 1;
+                    mm &= mm - 1;
+                    const int64_t q = emitted + r;
+                    if (q - cut_base == (int64_t)sa.max_candidates + 1) {
+                        keep = r;
+                        stop = true;
+                        break;
+                    }
+                    if ((hl >> ln) & 1u) cut_base = q + 1;
+                    r++;
+                }
+                pass = pass && __popc(m & ((1u << lane) - 1u)) <= keep;
+                m = __ballot_sync(FULL_MASK, pass);
+            }
+            const int np = __popc(m);
+            int64_t row0 = 0;
+            if (lane == 0) row0 = (int64_t)atomicAdd(out.count, (unsigned long long)np);
+            row0 = __shfl_sync(FULL_MASK, row0, 0);
+            if (pass) {
+                const int rk = __popc(m & ((1u << lane) - 1u));
+                const int64_t ri = row0 + rk;
+                if (ri < out.capacity) {
+                    int32_t *dst = out.atoms + ri * out.stride;
+                    for (int k = 0; k < n; k++) dst[k] = atom_of(k);
+                    out.pair[ri] = pair;
+                    out.ordinal[ri] = emitted + rk;
+                    if (out.rmsd) out.rmsd[ri] = rm;
+                }
+            }
+            emitted += np;
+            if (stop_at >= 0 && emitted >= stop_at) stop = true;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            if (emitted > 0) out.pair_rows[pair] = (int32_t)emitted;
+            int64_t partials = 0, bexp = 0;
+            for (int l = 0; l < n; l++) partials += F[l];
+            for (int l = 1; l < n; l++) bexp += 4LL * l * F[l - 1] + (4LL * (l + 1) + 16) * F[l];
+            atomicAdd(&counters[C_PARTIALS], (unsigned long long)partials);
+            atomicAdd(&counters[C_COMPLETE], (unsigned long long)F[n - 1]);
+            atomicAdd(&counters[C_BYTES_EXP], (unsigned long long)bexp);
+        }
+        __syncwarp();
+    }
+}
 
 // Superposition of every complete row, one thread per row (the FP64
 // eigen-solve fills all lanes), written to the row's slot in reference
@@ -2896,7 +3246,9 @@ void launch_axis_ranks(cudaStream_t st, int32_t n_structures, const int64_t *ato
 
 void launch_demand_levels(cudaStream_t st, int blocks, const TemplateView &tv, const CandView &cd, int32_t n_pairs,
                           int32_t max_level, int32_t reorder, const LeafDemand &dm) {
-    if (n_pairs > 0 && max_level > 0) k_demand_levels<<<blocks, 256, 0, st>>>(tv, cd, n_pairs, max_level, reorder, dm);
+    // (also with max_level 0: the pairs of templates over 32 atoms request
+    // every list here)
+    if (n_pairs > 0) k_demand_levels<<<blocks, 256, 0, st>>>(tv, cd, n_pairs, max_level, reorder, dm);
 }
 
 void launch_mark_ordered(cudaStream_t st, int blocks, const LeafDemand &dm) {
@@ -2937,6 +3289,25 @@ cudaError_t launch_search(cudaStream_t st, int grid, bool wide, bool fp32, const
                                                       dm);
     return fp32 ? search_variant<uint16_t, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm)
                 : search_variant<uint16_t, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm);
+}
+
+cudaError_t launch_search_large(cudaStream_t st, const ChunkView &cv, const TemplateView &tv, const CandView &cd,
+                                const SearchArgs &sa, const int32_t *large, int32_t n_large, int32_t *item_counter,
+                                const int32_t *scanned, const CompleteRows &out, unsigned long long *counters,
+                                const int32_t *lstate) {
+    if (n_large <= 0 || cv.n_structures <= 0) return cudaSuccess;
+    const size_t smem = (size_t)large_warp_bytes(tv.max_atoms) * LARGE_WARPS;
+    cudaError_t e = cudaFuncSetAttribute(k_search_large, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t items = (int64_t)cv.n_structures * n_large;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((items + LARGE_WARPS - 1) / LARGE_WARPS,
+                                                                 (int64_t)std::max(sms, 1) * 4));
+    k_search_large<<<grid, LARGE_WARPS * 32, smem, st>>>(cv, tv, cd, sa, large, n_large, item_counter, scanned, out,
+                                                         counters, lstate);
+    return cudaGetLastError();
 }
 
 void launch_superpose(cudaStream_t st, int blocks, const ChunkView &cv, const TemplateView &tv,
@@ -3067,8 +3438,41 @@ __global__ void k_compact_rows(const int32_t *flags, int32_t n_rows, int32_t *pa
 
 namespace {
 std::mutex g_noalloc_mutex;
-void *g_noalloc_ptr[64] = {};  // device address of g_noalloc_flags, per device
+void *g_noalloc_ptr[64] = {};                 // device address of g_noalloc_flags, per device
+unsigned long long g_noalloc_ctx[64] = {};    // id of the context that address belongs to
 thread_local char g_noalloc_err[256];
+
+// Unique id of the calling thread's current CUDA context (0 if unknown).
+// The driver never reuses an id, so a context destroyed and recreated on
+// the same device (cudaDeviceReset, then new work) gets a new one.  The two
+// driver calls are reached through the runtime's entry-point query, so the
+// library needs no link against the driver library.
+unsigned long long current_context_id() {
+    using GetCurrent = int (*)(void **);
+    using GetId = int (*)(void *, unsigned long long *);
+    static GetCurrent get_current = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        cudaGetLastError();
+        return (GetCurrent)f;
+    }();
+    static GetId get_id = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        cudaGetLastError();
+        return (GetId)f;
+    }();
+    void *ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
 }  // namespace
 
 extern "C" const char *pjg_noalloc_last_error(void) { return g_noalloc_err; }
@@ -3103,10 +3507,16 @@ extern "C" pjg_status pjg_superpose_noalloc(const double *mol_xyz, const double 
     }
     void *flags = nullptr;
     {
-        // once per device, with that device current: the device address of
-        // the static scratch (host code must not pass the symbol itself)
+        // once per device and context, with that device current: the device
+        // address of the static scratch (host code must not pass the symbol
+        // itself).  A context reset since the lookup (a new context id) gets
+        // the address looked up again, so a cached address is never used in
+        // a context it does not belong to.  (Before the process's first
+        // CUDA call there is no context yet: the lookup creates it, and the
+        // id is read after it.)
+        const unsigned long long ctx = current_context_id();
         std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-        if (!g_noalloc_ptr[dev]) {
+        if (!g_noalloc_ptr[dev] || ctx == 0 || ctx != g_noalloc_ctx[dev]) {
             void *p = nullptr;
             e = cudaGetSymbolAddress(&p, pjg::g_noalloc_flags);
             if (e != cudaSuccess || !p) {
@@ -3115,6 +3525,7 @@ extern "C" pjg_status pjg_superpose_noalloc(const double *mol_xyz, const double 
                 return PJG_ERR_CUDA;
             }
             g_noalloc_ptr[dev] = p;
+            g_noalloc_ctx[dev] = current_context_id();
         }
         flags = g_noalloc_ptr[dev];
     }

@@ -27,6 +27,12 @@ constexpr int SEARCH_WARPS = PJG_SEARCH_WARPS;  // warps per block of k_search
 #ifndef PJG_BLOCK_MIN
 #define PJG_BLOCK_MIN 64
 #endif
+// templates of more than 32 atoms: k_search_large, warps per block and
+// per-warp shared-memory bytes for templates of up to nmax atoms
+constexpr int LARGE_WARPS = 2;
+__host__ __device__ constexpr int large_warp_bytes(int nmax) { return ((52 * nmax) + 15) & ~15; }
+// longest template pjg_templates_create accepts
+constexpr int MAX_TEMPLATE_ATOMS = 1024;
 constexpr int LEAF_WARPS = 4;          // warps per block of k_leaf_order
 constexpr int LEAF_FAST_MAX = 192;     // capacity of the rank method's buffers
 constexpr int LEAF_RANK_MAX = 192;     // default: longest list ordered by the rank method
@@ -219,6 +225,14 @@ cudaError_t launch_search(cudaStream_t st, int grid, bool wide, bool fp32, const
                           const TemplateView &tv, const CandView &cd, const SearchArgs &sa, int32_t *pair_counter,
                           const int32_t *scanned, const CompleteRows &out, unsigned long long *counters,
                           const LeafDemand &dm);
+
+// k_search_large over the pairs (chunk structure x templates `large`) of
+// the templates with more than 32 atoms; item_counter zeroed by the caller;
+// lstate: per-list leaf-order state (nullptr: every list ordered)
+cudaError_t launch_search_large(cudaStream_t st, const ChunkView &cv, const TemplateView &tv, const CandView &cd,
+                                const SearchArgs &sa, const int32_t *large, int32_t n_large, int32_t *item_counter,
+                                const int32_t *scanned, const CompleteRows &out, unsigned long long *counters,
+                                const int32_t *lstate);
 
 void launch_superpose(cudaStream_t st, int blocks, const ChunkView &cv, const TemplateView &tv,
                       const CompleteRows &in, const RowResults &out);
