@@ -58,6 +58,10 @@ def parse():
                     help="structures run through the plain FP64 per-structure path (-1: all, 0: none)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--tune", action="store_true",
+                    help="run the autotuner when the tuning cache has no entry for this GPU and workload "
+                         "(else the cached entry, or the defaults, are used)")
+    ap.add_argument("--default-tuning", action="store_true", help="ignore the tuning cache")
     ap.add_argument("--search-profile", action="store_true",
                     help="run the search-profile build of the library and print k_search's event counts "
                          "and section cycles (not a bench line)")
@@ -252,6 +256,8 @@ def search_profile(args):
         "share_block": prof["cyc_block"] / max(1, prof["cyc_pair"]),
         "share_product": prof["cyc_prod"] / max(1, prof["cyc_pair"]),
         "share_emit": prof["cyc_emit"] / max(1, prof["cyc_pair"]),
+        "share_block_chain": prof["cyc_chain"] / max(1, prof["cyc_pair"]),
+        "share_block_batch": prof["cyc_batch"] / max(1, prof["cyc_pair"]),
         "blocks_hit_per_tested": prof["blocks_hit"] / max(1, prof["blocks_tested"]),
         "inbox_per_leaf_loaded": prof["leaves_inbox"] / max(1, 32 * prof["blocks_hit"]),
         "children_per_block_test": prof["child_block"] / max(1, prof["batch_lanes"]),
@@ -288,6 +294,18 @@ def main():
     wl = workload(args, rank, world)
     gen_s = time.time() - t0
     P = query_params(wl, _native.MODE_BATCHED_FP32)
+    # execution tuning: the cached entry for this GPU and workload shape
+    # (autotuned on a sample of the workload when --tune finds none)
+    from pyjess_gb300 import tune
+
+    if args.default_tuning:
+        entry, source = None, "default"
+    else:
+        entry, source = tune.ensure(wl.templates, wl.structures, wl.params, tune=args.tune)
+    tuning = {"values": tune.apply(entry), "source": source,
+              "key": tune.shape_key(wl.templates, wl.structures, wl.params)}
+    if entry is not None:
+        tuning.update({k: entry[k] for k in ("sample", "ms", "default_ms") if k in entry})
     tpl = _native.Templates(wl.templates)
     sts = _native.Structures(wl.structures)
 
@@ -428,6 +446,7 @@ def main():
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": launches,
+        "tuning": tuning,
         "clocks": clocks.summary(),
     }
     print(json.dumps(line))

@@ -231,6 +231,48 @@ pjg_status pjg_results_stats(const pjg_results *r, pjg_stats *stats);
 
 void pjg_results_destroy(pjg_results *r);
 
+/* Execution tuning -------------------------------------------------------
+ *
+ * No counterpart in the reference (its search is one thread).  The knobs of
+ * the GPU search that trade work between kernels; the autotuner
+ * (pyjess_gb300/tune.py) measures them on a sample of a workload and sets
+ * the fastest.  Process-wide: each pjg_query reads the values in force when
+ * it starts.  A field of 0 keeps the built-in default.
+ *   leaf_levels    levels (after level 0) whose candidate lists are put in
+ *                  kd leaf order before the search; deeper lists when a
+ *                  pair first reaches them (default 4; -1 every list up
+ *                  front; the plain FP64 mode always orders every list)
+ *   block_min      shortest list the search expands one parent at a time
+ *                  with block culling (shorter lists: lanes over (parent,
+ *                  candidate) pairs) (default 64, 1 .. 65535)
+ *   tile_cap       most entries of a frontier tile (default 4096, 32 ..
+ *                  16384)
+ *   pair_grain     (structure, template) pairs a search warp takes from the
+ *                  work queue at a time (default 1, 1 .. 64)
+ *   leaf_rank_max  longest tie-free list put in leaf order by the rank
+ *                  method (longer lists: sorted-axis splits) (default 192,
+ *                  1 .. 192)
+ *   leaf_reach     when a pair reaches a list with no leaf order it is
+ *                  suspended and requests that list and the next
+ *                  leaf_reach - 1 deeper ones of its levels (-1, the
+ *                  default: every deeper one; 1 .. 64)
+ * Out-of-range values return PJG_ERR_INVALID and change nothing. */
+typedef struct {
+    int32_t leaf_levels;
+    int32_t block_min;
+    int32_t tile_cap;
+    int32_t pair_grain;
+    int32_t leaf_rank_max;
+    int32_t leaf_reach;
+} pjg_tuning;
+
+/* Set the tuning (NULL restores every default). */
+pjg_status pjg_set_tuning(const pjg_tuning *tuning);
+/* The tuning in force, defaults filled in. */
+pjg_status pjg_get_tuning(pjg_tuning *tuning);
+/* Name of the current CUDA device (the autotuner's cache key). */
+pjg_status pjg_device_name(char *buf, int32_t len);
+
 /* Allocation-free superposition --------------------------------------------
  *
  * No counterpart in the reference.  For callers that cannot allocate device

@@ -51,6 +51,22 @@ class QueryParams(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    """pjg_tuning: execution knobs of pjg_query (0 keeps a default)."""
+
+    _fields_ = [
+        ("leaf_levels", C.c_int32),
+        ("block_min", C.c_int32),
+        ("tile_cap", C.c_int32),
+        ("pair_grain", C.c_int32),
+        ("leaf_rank_max", C.c_int32),
+        ("leaf_reach", C.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("pairs", C.c_int64),

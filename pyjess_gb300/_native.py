@@ -12,7 +12,7 @@ import threading
 
 import numpy as np
 
-from ._abi import QueryParams, Stats, StructureSet, TemplateSet
+from ._abi import QueryParams, Stats, StructureSet, TemplateSet, Tuning
 from ._build import build, lib_path
 
 MODE_PLAIN_FP64 = 0
@@ -28,8 +28,8 @@ EXPORTED = (
     "pjg_init", "pjg_last_error", "pjg_templates_create", "pjg_templates_destroy",
     "pjg_structures_create", "pjg_structures_destroy", "pjg_query", "pjg_results_count",
     "pjg_results_atom_count", "pjg_results_copy", "pjg_results_warning_count",
-    "pjg_results_warnings", "pjg_results_stats", "pjg_results_destroy", "pjg_superpose_noalloc",
-    "pjg_noalloc_last_error",
+    "pjg_results_warnings", "pjg_results_stats", "pjg_results_destroy", "pjg_set_tuning", "pjg_get_tuning",
+    "pjg_device_name", "pjg_superpose_noalloc", "pjg_noalloc_last_error",
 )
 
 _lib = None
@@ -75,6 +75,12 @@ def load(build_if_missing: bool = True):
         L.pjg_results_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
         L.pjg_results_stats.restype = C.c_int
         L.pjg_results_destroy.argtypes = [C.c_void_p]
+        L.pjg_set_tuning.argtypes = [C.POINTER(Tuning)]
+        L.pjg_set_tuning.restype = C.c_int
+        L.pjg_get_tuning.argtypes = [C.POINTER(Tuning)]
+        L.pjg_get_tuning.restype = C.c_int
+        L.pjg_device_name.argtypes = [C.c_char_p, C.c_int32]
+        L.pjg_device_name.restype = C.c_int
         _lib = L
         return L
 
@@ -202,3 +208,27 @@ def query(templates: Templates, structures: Structures, params: QueryParams) -> 
     h = C.c_void_p()
     _check(L.pjg_query(templates.handle, structures.handle, C.byref(params), C.byref(h)), "pjg_query")
     return Result(h)
+
+
+def set_tuning(tuning: dict | None):
+    """Set the process-wide execution tuning (``None``: the defaults)."""
+    L = _ready()
+    if tuning is None:
+        _check(L.pjg_set_tuning(None), "pjg_set_tuning")
+        return
+    t = Tuning(**{k: int(v) for k, v in tuning.items() if k in dict(Tuning._fields_)})
+    _check(L.pjg_set_tuning(C.byref(t)), "pjg_set_tuning")
+
+
+def get_tuning() -> dict:
+    L = _ready()
+    t = Tuning()
+    _check(L.pjg_get_tuning(C.byref(t)), "pjg_get_tuning")
+    return t.as_dict()
+
+
+def device_name() -> str:
+    L = _ready()
+    buf = C.create_string_buffer(256)
+    _check(L.pjg_device_name(buf, 256), "pjg_device_name")
+    return buf.value.decode(errors="replace")

@@ -817,7 +817,7 @@ void write_search_profile(const unsigned long long *d_prof, cudaStream_t st, con
         "pairs", "empty", "cyc_pair", "cyc_setup", "cyc_seed", "cyc_block", "cyc_prod", "cyc_emit",
         "loop_iters", "block_visits", "block_visits_l0", "chain_full", "chain_sibling", "g0_iters",
         "blocks_tested", "blocks_hit", "leaves_inbox", "batches", "batch_lanes", "child_block",
-        "prod_batches", "prod_batches_l0", "prod_lanes", "child_prod", "fp64", "rows"};
+        "prod_batches", "prod_batches_l0", "prod_lanes", "child_prod", "fp64", "rows", "cyc_chain", "cyc_batch"};
     unsigned long long h[SP_NUM] = {};
     if (cudaMemcpyAsync(h, d_prof, sizeof h, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
@@ -835,6 +835,63 @@ void write_search_profile(const unsigned long long *d_prof, cudaStream_t st, con
 #endif
 
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// Execution tuning (process-wide, read at the start of each query)
+
+namespace {
+std::mutex g_tuning_mutex;
+constexpr pjg_tuning TUNING_DEFAULTS = {4, 64, 4096, 1, LEAF_RANK_MAX, -1};
+pjg_tuning g_tuning = TUNING_DEFAULTS;
+
+pjg_tuning current_tuning() {
+    std::lock_guard<std::mutex> g(g_tuning_mutex);
+    return g_tuning;
+}
+}  // namespace
+
+extern "C" pjg_status pjg_set_tuning(const pjg_tuning *t) {
+    pjg_tuning d = TUNING_DEFAULTS;
+    if (t) {
+        if (t->leaf_levels < -1 || t->leaf_levels > 64) return fail(PJG_ERR_INVALID, "leaf_levels %d", t->leaf_levels);
+        if (t->block_min < 0 || t->block_min > 65535) return fail(PJG_ERR_INVALID, "block_min %d", t->block_min);
+        if (t->tile_cap != 0 && (t->tile_cap < 32 || t->tile_cap > 16384))
+            return fail(PJG_ERR_INVALID, "tile_cap %d", t->tile_cap);
+        if (t->pair_grain < 0 || t->pair_grain > 64) return fail(PJG_ERR_INVALID, "pair_grain %d", t->pair_grain);
+        if (t->leaf_rank_max < 0 || t->leaf_rank_max > LEAF_FAST_MAX)
+            return fail(PJG_ERR_INVALID, "leaf_rank_max %d", t->leaf_rank_max);
+        if (t->leaf_reach < -1 || t->leaf_reach > 64) return fail(PJG_ERR_INVALID, "leaf_reach %d", t->leaf_reach);
+        if (t->leaf_levels) d.leaf_levels = t->leaf_levels;
+        if (t->block_min) d.block_min = t->block_min;
+        if (t->tile_cap) d.tile_cap = t->tile_cap;
+        if (t->pair_grain) d.pair_grain = t->pair_grain;
+        if (t->leaf_rank_max) d.leaf_rank_max = t->leaf_rank_max;
+        if (t->leaf_reach) d.leaf_reach = t->leaf_reach;
+    }
+    std::lock_guard<std::mutex> g(g_tuning_mutex);
+    g_tuning = d;
+    return PJG_OK;
+}
+
+extern "C" pjg_status pjg_get_tuning(pjg_tuning *t) {
+    if (!t) return fail(PJG_ERR_INVALID, "null argument");
+    *t = current_tuning();
+    return PJG_OK;
+}
+
+extern "C" pjg_status pjg_device_name(char *buf, int32_t len) {
+    if (!buf || len <= 0) return fail(PJG_ERR_INVALID, "null or empty buffer");
+    int dev = 0;
+    cudaDeviceProp prop;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaGetDeviceProperties(&prop, dev);
+    if (e != cudaSuccess) {
+        buf[0] = 0;
+        return fail(PJG_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+    }
+    snprintf(buf, (size_t)len, "%s", prop.name);
+    return PJG_OK;
+}
 
 extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *sp, const pjg_query_params *P,
                                 pjg_results **out) {
@@ -890,15 +947,16 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     t_scan_launches = 0;
     int64_t suspensions = 0;
     // levels whose lists are put in kd leaf order before the search (deeper
-    // lists when a pair's frontier first reaches them); PJG_LEAF_LEVELS
-    // overrides it, a negative value orders every list up front.  The plain
-    // per-structure path orders every list up front: with one structure a
-    // chunk, the host round trip of each extra search round costs more
-    // than the ordering it saves.
-    int demand_levels = P->mode == PJG_MODE_PLAIN_FP64 ? -1 : 4;
+    // lists when a pair's frontier first reaches them): the tuning's
+    // leaf_levels, or PJG_LEAF_LEVELS when set; a negative value orders
+    // every list up front.  The plain per-structure path orders every list
+    // up front: with one structure a chunk, the host round trip of each
+    // extra search round costs more than the ordering it saves.
+    const pjg_tuning tune = current_tuning();
+    int demand_levels = P->mode == PJG_MODE_PLAIN_FP64 ? -1 : tune.leaf_levels;
     {
         const char *v = getenv("PJG_LEAF_LEVELS");
-        if (v && *v) demand_levels = atoi(v);
+        if (v && *v && P->mode != PJG_MODE_PLAIN_FP64) demand_levels = atoi(v);
     }
     std::vector<int64_t> totals(S);
 
@@ -1179,7 +1237,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 launch_leaf_order(st, leaf_blocks, cv, G, cnt_c, d_offset.p, d_boff.p, d_cand_atom.p, leaf_off,
                                   d_leaf_atom.p, d_leaf_xyz.p, d_blk_lo.p, d_blk_hi.p, d_sorted_list.p,
                                   d_sorted_count.p, Wc, d_exact_list.p, d_exact_count.p, d_counters.p, dm.work,
-                                  dm.n_work);
+                                  dm.n_work, tune.leaf_rank_max);
                 launches += 6;
                 if (dm.state) {
                     launch_mark_ordered(st, sm_count() * 4, dm);
@@ -1260,6 +1318,10 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             sa.cut_inline = cut_inline ? 1 : 0;
             sa.rmsd_threshold = P->rmsd_threshold;
             sa.prof = nullptr;
+            sa.block_min = tune.block_min;
+            sa.tile_cap = tune.tile_cap;
+            sa.pair_grain = tune.pair_grain;
+            sa.leaf_reach = tune.leaf_reach;
 #if PJG_SEARCH_PROF
             if (!d_prof.p) {
                 CUDA_TRY(dalloc(d_prof, SP_NUM, st));
@@ -1279,10 +1341,17 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             CUDA_TRY(cudaMemcpyAsync(snap, d_counters.p, sizeof snap, cudaMemcpyDeviceToHost, st));
             CUDA_TRY(cudaStreamSynchronize(st));
             CUDA_TRY(dalloc(d_pair_rows, (size_t)n_pairs, st));
-            if (c_cap < 2 * n_pairs) {
-                // room for two complete rows a pair before the first attempt
-                // (a rerun of the search costs a whole chunk)
-                c_cap = 2 * n_pairs;
+            // room before the first attempt (a rerun of the search costs a
+            // whole chunk): two complete rows a pair, or, with best_match
+            // and max_candidates, the most a pair can produce (max_candidates
+            // + 2) when the row budget takes that
+            int64_t want_rows = 2 * n_pairs;
+            if (P->best_match && P->max_candidates >= 0) {
+                const int64_t bound = n_pairs * ((int64_t)P->max_candidates + 2);
+                if (bound <= row_budget()) want_rows = std::max(want_rows, bound);
+            }
+            if (c_cap < want_rows) {
+                c_cap = want_rows;
                 CUDA_TRY(dalloc(d_c_pair, c_cap, st));
                 CUDA_TRY(dalloc(d_c_ord, c_cap, st));
                 CUDA_TRY(dalloc(d_c_atoms, (size_t)c_cap * stride, st));
@@ -1343,7 +1412,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                     }
                     search_rounds++;
                     if (ns == 0) break;
-                    if (round > 64) {
+                    if (round > 80) {
                         status = fail(PJG_ERR_CAPACITY, "leaf order on demand did not converge");
                         goto done;
                     }

@@ -1723,7 +1723,7 @@ __device__ double lane_rmsd(int n, const int32_t *atoms, const double *xyz, cons
 // first over tiles, breadth first inside a tile), which reproduces that
 // order.
 //
-// Two expansion modes per level.  Block mode (lists of PJG_BLOCK_MIN = 64
+// Two expansion modes per level.  Block mode (lists of sa.block_min (64)
 // or more): one parent at a time; its chain of atoms, key bits and FP32
 // annulus bounds sit in shared memory and are read by all lanes as
 // broadcasts; the parent's join box (intersection of its annulus boxes)
@@ -1755,6 +1755,9 @@ struct PairState {
     // block mode: leaves inside the parent's join box awaiting the full test
     float4 qxyz[64];
     int32_t qpos[64];
+    // statistics of this warp's pairs (C_PAIRS .. C_BYTES_EXP), added to the
+    // global counters once, when the warp exits
+    unsigned long long acc[C_BYTES_EXP + 1];
 };
 
 template <typename PosT>
@@ -1893,6 +1896,8 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
 #endif
     unsigned char *wbase = smem + (size_t)wib * sa.warp_smem;
     PairState &st = *reinterpret_cast<PairState *>(wbase);
+    if (lane <= C_BYTES_EXP) st.acc[lane] = 0;
+    __syncwarp();
     const size_t o2 = (sizeof(PairState) + 15) & ~size_t(15);
     E *tiles = reinterpret_cast<E *>(wbase + o2);
     const int64_t tile_units = (int64_t)(sa.warp_smem - o2) / (int64_t)sizeof(E);
@@ -1920,10 +1925,16 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
     // earlier round suspended (each with the rows it has already emitted)
     const bool fresh = dm.resume == nullptr;
     const int n_items = fresh ? sa.n_pairs : dm.n_resume;
+    // work queue: a warp takes sa.pair_grain consecutive items at a time
+    int g_next = 0, g_end = 0;
     for (;;) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(pair_counter, 1);
-        item = __shfl_sync(FULL_MASK, item, 0);
+        if (g_next >= g_end) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(pair_counter, sa.pair_grain);
+            g_next = __shfl_sync(FULL_MASK, base, 0);
+            g_end = g_next + sa.pair_grain;
+        }
+        const int item = g_next++;
         if (item >= n_items || timed_out) break;
         SPROF_T(t_pair);
         SPROF_ADD(SP_PAIRS, 1);
@@ -1957,9 +1968,9 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                 cc += __shfl_xor_sync(FULL_MASK, cc, o);
             }
             if (lane == 0 && fresh) {
-                atomicAdd(&counters[C_PAIRS], 1ull);
-                atomicAdd(&counters[C_BYTES_CAND], (unsigned long long)bc);
-                atomicAdd(&counters[C_CAND], (unsigned long long)cc);
+                st.acc[C_PAIRS] += 1ull;
+                st.acc[C_BYTES_CAND] += (unsigned long long)bc;
+                st.acc[C_CAND] += (unsigned long long)cc;
             }
         }
         if (zero) {
@@ -1981,7 +1992,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
         if (k < n) st.order[rank] = k;
         __syncwarp();
         // tile capacity: equal entry count for levels 0..n-2
-        int cap = n >= 2 ? (int)min((int64_t)4096, tile_units / (n - 1)) : 0;
+        int cap = n >= 2 ? (int)min((int64_t)sa.tile_cap, tile_units / (n - 1)) : 0;
         // levels whose list is in kd leaf order (level 0 reads the
         // candidate order)
         bool lvl_ready = true;
@@ -2236,10 +2247,12 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                             for (int i = lane; i < cj; i += 32) dst[pj + i] = src[i];
                         }
                     }
-                    // request the lists of this level and of every deeper
-                    // one (a resumed pair then never stops again: a chunk
-                    // takes at most two search rounds)
-                    if (lane >= child && lane < n && !((ready_mask >> lane) & 1u))
+                    // request the list of this level and of the next
+                    // sa.leaf_reach - 1 deeper ones, or of every deeper
+                    // one (leaf_reach < 0: a resumed pair then never stops
+                    // again, a chunk takes at most two search rounds)
+                    if (lane >= child && lane < n && (sa.leaf_reach < 0 || lane < child + sa.leaf_reach) &&
+                        !((ready_mask >> lane) & 1u))
                         request_list(dm, (int64_t)s * G + tv.sig[ab + st.order[lane]], st.lvl_cnt[lane]);
                     if (lane == 0) {
                         Suspended sp;
@@ -2263,7 +2276,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                 int my_parent = 0;      // product mode: this lane's parent entry
                 int32_t chainpos[32];   // product mode: this lane's parent chain
                 SPROF_T(t_exp);
-                if (mc >= PJG_BLOCK_MIN) {
+                if (mc >= sa.block_min) {
                     // ---------------- block mode ----------------
                     if (!last && cap - ccnt < 32) {
                         __syncwarp();
@@ -2298,13 +2311,15 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         bl = cd.blk_lo[boff + gfirst + lane];
                         bh = cd.blk_hi[boff + gfirst + lane];
                     }
+                    SPROF_T(t_chain);
                     if (chain_lev != lev || chain_par != ppar) {
                         const E pe = tiles[st.tile[lev] + ppar];
                         float olo[3] = {-INFINITY, -INFINITY, -INFINITY}, ohi[3] = {INFINITY, INFINITY, INFINITY};
-                        if (chain_lev == lev && lev > 0 && (int)pe.parent == st.chain_gp) {
-                            // a sibling of the previous parent: levels below
-                            // lev are unchanged, only this parent's point
-                            // and box are new
+                        if (chain_lev == lev && (int)pe.parent == st.chain_gp) {
+                            // a sibling of the previous parent (every seed is
+                            // one of the previous seed): levels below lev are
+                            // unchanged, only this parent's point and box are
+                            // new
                             SPROF_ADD(SP_CHAIN_SIBLING, 1);
                             if (lane == lev) {
                                 const float4 cj = level_xyz(lev, (int)pe.pos);
@@ -2376,12 +2391,17 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         chain_par = ppar;
                         __syncwarp();
                     }
+                    SPROF_CYC(SP_CYC_CHAIN, t_chain);
                     int ncnt = ccnt;
                     int resume = -1;
                     int queued = 0;
+                    // the parent's point and its annulus bounds to the child
+                    const float4 pxyz = st.cxyz[lev];
+                    const float4 pthr = st.cthr[lev];
                     // full test of queue entries 0..k-1 (lane i takes entry i),
                     // then the entries after them move to the queue's front
                     auto run_batch = [&](int k) {
+                        SPROF_T(t_batch);
                         SPROF_ADD(SP_BATCHES, 1);
                         SPROF_ADD(SP_BATCH_LANES, k);
                         cr = lane < k ? st.qpos[lane] : 0;
@@ -2450,6 +2470,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         }
                         __syncwarp();
                         queued = rest;
+                        SPROF_CYC(SP_CYC_BATCH, t_batch);
                     };
                     for (int g0 = gfirst; g0 < nblk && resume < 0 && !stop; g0 += 32) {
                         const int b = g0 + lane;
@@ -2487,9 +2508,18 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                                 if (nxt * 32 + lane < mc) xn = cd.leaf_xyz[coff + nxt * 32 + lane];
                             }
                             const int q = blk * 32 + lane;
-                            const bool inb = q < mc && q >= pstart &&
-                                             !(xc.x < box_lo[0] || xc.x > box_hi[0] || xc.y < box_lo[1] ||
-                                               xc.y > box_hi[1] || xc.z < box_lo[2] || xc.z > box_hi[2]);
+                            // inside the join box and not certainly outside
+                            // the parent's own annulus (the FP32 reject
+                            // bounds of the full test, so the full test
+                            // would reject the same leaves)
+                            bool inb = q < mc && q >= pstart &&
+                                       !(xc.x < box_lo[0] || xc.x > box_hi[0] || xc.y < box_lo[1] ||
+                                         xc.y > box_hi[1] || xc.z < box_lo[2] || xc.z > box_hi[2]);
+                            if (FP32 && inb) {
+                                const float dx = pxyz.x - xc.x, dy = pxyz.y - xc.y, dz = pxyz.z - xc.z;
+                                const float d2 = dx * dx + dy * dy + dz * dz;
+                                inb = !(d2 < pthr.x || d2 > pthr.w);
+                            }
                             const unsigned im = __ballot_sync(FULL_MASK, inb);
                             SPROF_ADD(SP_LEAVES_INBOX, __popc(im));
                             if (inb) {
@@ -2618,7 +2648,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                     my_parent = p;
                 }
                 // ---- children / complete rows
-                const bool block_mode = mc >= PJG_BLOCK_MIN;
+                const bool block_mode = mc >= sa.block_min;
                 unsigned m = __ballot_sync(FULL_MASK, pass);
                 SPROF_ADD(SP_CHILD_PROD, __popc(m));
                 if (last) {
@@ -2682,13 +2712,15 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
             for (int l = 0; l < n; l++) partials += st.F[l];
             for (int l = 1; l < n; l++)
                 bexp += 4LL * l * st.F[l - 1] + (4LL * (l + 1) + 16) * st.F[l];
-            atomicAdd(&counters[C_PARTIALS], (unsigned long long)partials);
-            atomicAdd(&counters[C_COMPLETE], (unsigned long long)st.F[n - 1]);
-            atomicAdd(&counters[C_BYTES_EXP], (unsigned long long)bexp);
-            atomicAdd(&counters[C_RECHECK], rechecks);
+            st.acc[C_PARTIALS] += (unsigned long long)partials;
+            st.acc[C_COMPLETE] += (unsigned long long)st.F[n - 1];
+            st.acc[C_BYTES_EXP] += (unsigned long long)bexp;
+            st.acc[C_RECHECK] += rechecks;
         }
         __syncwarp();
     }
+    __syncwarp();
+    if (lane <= C_BYTES_EXP && st.acc[lane]) atomicAdd(&counters[lane], st.acc[lane]);
 #if PJG_SEARCH_PROF
     for (int o = 16; o; o >>= 1) sp_fp64 += __shfl_xor_sync(FULL_MASK, sp_fp64, o);
     SPROF_ADD(SP_FP64, sp_fp64);
@@ -3185,16 +3217,12 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
                        const int64_t *leaf_offset, int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
                        int64_t *sorted_list, unsigned long long *sorted_count, int64_t list_cap,
                        int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters,
-                       const int64_t *work, const unsigned long long *n_work) {
+                       const int64_t *work, const unsigned long long *n_work, int rank_max) {
     cudaMemsetAsync(sorted_count, 0, 3 * sizeof(unsigned long long), st);
     cudaMemsetAsync(exact_count, 0, sizeof(unsigned long long), st);
     // lists longer than rank_max take the sorted-axis split (the rank
-    // method costs O(m^2) a level); PJG_LEAF_RANK_MAX overrides the crossover
-    static const int rank_max = [] {
-        const char *v = getenv("PJG_LEAF_RANK_MAX");
-        int r = v ? atoi(v) : LEAF_RANK_MAX;
-        return r < 1 ? 1 : r > LEAF_FAST_MAX ? LEAF_FAST_MAX : r;
-    }();
+    // method costs O(m^2) a level)
+    rank_max = rank_max < 1 ? 1 : rank_max > LEAF_FAST_MAX ? LEAF_FAST_MAX : rank_max;
     k_leaf_order<<<blocks, LEAF_WARPS * 32, 0, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset,
                                                     leaf_atom, leaf_xyz, blk_lo, blk_hi, sorted_list, sorted_count,
                                                     list_cap, exact_list, exact_count, counters, rank_max,

@@ -22,11 +22,6 @@ constexpr int SEARCH_WARPS = PJG_SEARCH_WARPS;  // warps per block of k_search
 #ifndef PJG_SEARCH_MIN_BLOCKS
 #define PJG_SEARCH_MIN_BLOCKS 2
 #endif
-// shortest child list k_search expands one parent at a time in block mode
-// (shorter lists: product mode, lanes over (parent, candidate) pairs)
-#ifndef PJG_BLOCK_MIN
-#define PJG_BLOCK_MIN 64
-#endif
 // templates of more than 32 atoms: k_search_large, warps per block and
 // per-warp shared-memory bytes for templates of up to nmax atoms
 constexpr int LARGE_WARPS = 2;
@@ -74,6 +69,8 @@ enum SearchProf : int {
     SP_CHILD_PROD,       // children / rows from product mode
     SP_FP64,             // candidates decided in FP64
     SP_ROWS,             // complete rows emitted
+    SP_CYC_CHAIN,        // cycles gathering a block-mode parent's chain and box
+    SP_CYC_BATCH,        // cycles in block-mode full-test batches
     SP_NUM
 };
 
@@ -90,6 +87,14 @@ struct SearchArgs {
     uint64_t budget_ns;                // per-warp wall-time budget (globaltimer)
     unsigned long long *prof;          // [SP_NUM] search profile (profile
                                        // builds only, else nullptr)
+    int32_t block_min;                 // shortest child list expanded one
+                                       // parent at a time in block mode
+                                       // (shorter: product mode)
+    int32_t tile_cap;                  // most entries of a frontier tile
+    int32_t pair_grain;                // work-queue items a warp takes at once
+    int32_t leaf_reach;                // lists a suspending pair requests: its
+                                       // level and the next leaf_reach - 1
+                                       // (< 0: every deeper level)
 };
 
 // A pair whose search stopped at a level whose candidate list had no kd
@@ -200,7 +205,7 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
                        const int64_t *leaf_offset, int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
                        int64_t *sorted_list, unsigned long long *sorted_count, int64_t list_cap,
                        int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters,
-                       const int64_t *work, const unsigned long long *n_work);
+                       const int64_t *work, const unsigned long long *n_work, int rank_max);
 
 // requests (LeafDemand) the lists of levels 1 .. max_level of every pair
 // of the chunk that has no empty candidate list
