@@ -62,6 +62,8 @@ def parse():
                     help="run the autotuner when the tuning cache has no entry for this GPU and workload "
                          "(else the cached entry, or the defaults, are used)")
     ap.add_argument("--default-tuning", action="store_true", help="ignore the tuning cache")
+    ap.add_argument("--ingest-files", type=int, default=200,
+                    help="PDB files read back for the ingestion measurement (0: skip)")
     ap.add_argument("--search-profile", action="store_true",
                     help="run the search-profile build of the library and print k_search's event counts "
                          "and section cycles (not a bench line)")
@@ -167,15 +169,26 @@ def cpu_structures(wl, stride):
 
 
 def cpu_sample(wl, idx, threads):
-    """Time the CPU oracle on structures `idx` x all templates."""
+    """Time the CPU oracle on structures `idx` x all templates; returns
+    (pairs/s, seconds, pairs, hits, boundary counts of the adversarial and
+    of the ordinary structures of the sample).  The two groups run as two
+    oracle calls, timed together."""
     from oracle import oracle
 
-    sub = wl.structures.subset(idx)
-    t0 = time.perf_counter()
-    r = oracle.query(wl.templates, sub, threads=threads, **wl.params)
-    dt = time.perf_counter() - t0
-    pairs = wl.templates.n_templates * sub.n_structures
-    return pairs / dt, dt, pairs, r["hits"]["count"]
+    groups = [[i for i in idx if i < wl.n_adversarial], [i for i in idx if i >= wl.n_adversarial]]
+    dt, hits, boundary = 0.0, 0, []
+    for g in groups:
+        if not g:
+            boundary.append({"tests": 0, "near": 0})
+            continue
+        sub = wl.structures.subset(g)
+        t0 = time.perf_counter()
+        r = oracle.query(wl.templates, sub, threads=threads, **wl.params)
+        dt += time.perf_counter() - t0
+        hits += r["hits"]["count"]
+        boundary.append(r["boundary"])
+    pairs = wl.templates.n_templates * len(idx)
+    return pairs / dt, dt, pairs, hits, boundary
 
 
 def sample_text(wl, idx, stride):
@@ -195,7 +208,7 @@ def run_reference(args):
     idx = cpu_structures(wl, args.cpu_stride)
     vals = []
     for i in range(args.warmup + args.steps):
-        v, dt, pairs, hits = cpu_sample(wl, idx, threads)
+        v, dt, pairs, hits, _ = cpu_sample(wl, idx, threads)
         if i >= args.warmup:
             vals.append(v)
     value = statistics.median(vals)
@@ -210,6 +223,66 @@ def run_reference(args):
         "notes": "the reference's C core cannot be built (empty vendor/jess submodule); the oracle port "
                  "restating its algorithm runs on all host cores",
     }))
+
+
+def pdb_text(ps, s: int) -> str:
+    """PDB ATOM records of packed structure `s` (the columns the reader takes)."""
+    a0, a1 = int(ps.atom_offset[s]), int(ps.atom_offset[s + 1])
+    dec = lambda b: bytes(b).replace(b"_", b" ").replace(b"\0", b" ").decode()
+    lines = []
+    for i in range(a0, a1):
+        x, y, z = ps.xyz[i]
+        ch = bytes(ps.chain[i]).decode()
+        lines.append(f"ATOM  {int(ps.serial[i]):5d} {dec(ps.name[i])} {dec(ps.resname[i])[:3]}{ch}"
+                     f"{int(ps.res_seq[i]):4d}    {x:8.3f}{y:8.3f}{z:8.3f}  1.00  0.00          "
+                     f"{dec(ps.name[i]).strip()[:1]:>2}  \n")
+    return "".join(lines) + "END\n"
+
+
+def ingestion(wl, tpl, P, n_files: int, threads: int):
+    """Structure ingestion in front of the query: `n_files` structures
+    written as PDB files, read back with Molecule.load (the native record
+    reader, on `threads` host threads), packed and uploaded
+    (pjg_structures_create), then queried.  The general Python reader is
+    timed on a few of the files for comparison."""
+    import concurrent.futures
+    import tempfile
+
+    from pyjess_gb300 import Molecule, _io, _native
+    from pyjess_gb300._pack import pack_molecules
+
+    idx = list(range(wl.n_adversarial, min(wl.structures.n_structures, wl.n_adversarial + n_files)))
+    with tempfile.TemporaryDirectory() as d:
+        paths = []
+        for s in idx:
+            path = os.path.join(d, f"s{s}.pdb")
+            with open(path, "w") as f:
+                f.write(pdb_text(wl.structures, s))
+            paths.append(path)
+        atoms = int(sum(wl.structures.atom_offset[s + 1] - wl.structures.atom_offset[s] for s in idx))
+        t0 = time.perf_counter()
+        with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as pool:
+            mols = list(pool.map(Molecule.load, paths))
+        t1 = time.perf_counter()
+        packed = pack_molecules(mols)
+        t2 = time.perf_counter()
+        sts = _native.Structures(packed)
+        t3 = time.perf_counter()
+        res = _native.query(tpl, sts, P)
+        q_ms = res.stats()["ms_total"]
+        k = min(10, len(paths))
+        t4 = time.perf_counter()
+        for path in paths[:k]:
+            with open(path) as f:
+                _io.parse_pdb(f)
+        py_ms = (time.perf_counter() - t4) / k * 1e3
+    n = len(paths)
+    return {"structures": n, "atoms": atoms, "threads": threads,
+            "load_ms_per_structure": (t1 - t0) / n * 1e3, "atoms_per_s": atoms / (t1 - t0),
+            "pack_ms": (t2 - t1) * 1e3, "structures_create_ms": (t3 - t2) * 1e3, "query_ms": q_ms,
+            "python_reader_ms_per_structure": py_ms,
+            "note": "Molecule.load of PDB files (native record reader) on host threads, then pack_molecules and "
+                    "pjg_structures_create, against the device query of the same structures x all templates"}
 
 
 def query_params(wl, mode, guard_band=1e-4):
@@ -234,10 +307,11 @@ def search_profile(args):
     search-profile build of the library (one query after one warm-up)."""
     import tempfile
 
-    os.environ["PJG_LIB_VARIANT"] = "prof"
+    variant = os.environ.get("PJG_PROF_VARIANT", "prof")
+    os.environ["PJG_LIB_VARIANT"] = variant
     from pyjess_gb300 import _build, _native
 
-    _build.build(variant="prof")
+    _build.build(variant=variant)
     _native.init(dist_env()[2])
     wl = workload(args)
     tpl = _native.Templates(wl.templates)
@@ -400,7 +474,7 @@ def main():
 
     # ---- CPU baseline (rank 0, N=1): the same strided sample as the
     # reference arm, median of three runs
-    cpu = None
+    cpu, boundary = None, None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         idx = cpu_structures(wl, args.cpu_stride)
@@ -409,6 +483,22 @@ def main():
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": sample_text(wl, idx, args.cpu_stride) + f" (median of 3 runs of "
                                                                   f"{statistics.median(r[1] for r in runs):.1f} s)"}
+        # adversarial structures: share of the candidate-pair distance tests
+        # (the kd range queries' annulus tests, counted by the oracle on the
+        # sample) within 1e-6 A of an annulus boundary, against the ordinary
+        # structures of the same sample
+        adv, ordn = runs[0][4]
+        if wl.n_adversarial:
+            boundary = {
+                "adversarial_structures": wl.n_adversarial,
+                "near_boundary_fraction_adversarial": adv["near"] / max(1, adv["tests"]),
+                "near_boundary_fraction_ordinary": ordn["near"] / max(1, ordn["tests"]),
+                "tests_adversarial": adv["tests"], "tests_ordinary": ordn["tests"],
+                "measured_on": "the CPU sample's structures (oracle counts of every annulus test)"}
+
+    ingest = None
+    if rank == 0 and args.ingest_files > 0:
+        ingest = ingestion(wl, tpl, P, args.ingest_files, os.cpu_count() or 1)
 
     if rank != 0:
         return
@@ -428,7 +518,8 @@ def main():
         "config": {"workload": wl.name, "pairs_per_gpu": pairs_step, "structures": wl.structures.n_structures,
                    "templates": wl.templates.n_templates, "atoms": wl.structures.n_atoms,
                    "params": wl.params, "l2": "inputs and candidate lists larger than L2 (no flush)",
-                   "adversarial": wl.notes, "generation_s": round(gen_s, 1)},
+                   "adversarial": wl.notes, "adversarial_boundary": boundary,
+                   "generation_s": round(gen_s, 1)},
         "hits_per_s": hits_per_s,
         "hits_per_step": s0["hits"],
         "plain_fp64": plain,
@@ -444,6 +535,7 @@ def main():
                                         "fp64_rechecks", "leaf_lists", "leaf_entries", "leaf_exact", "suspensions",
                                         "search_rounds", "chunks", "row_splits")},
         "cpu_baseline": cpu,
+        "ingestion": ingest,
         "e2e": e2e,
         "gpu_launches": launches,
         "tuning": tuning,

@@ -273,6 +273,26 @@ pjg_status pjg_get_tuning(pjg_tuning *tuning);
 /* Name of the current CUDA device (the autotuner's cache key). */
 pjg_status pjg_device_name(char *buf, int32_t len);
 
+/* Structure ingestion ---------------------------------------------------
+ *
+ * Replaces the per-record loop of the reference's PDB reader
+ * (src/pyjess/_io.py:52-103, PDBMoleculeParser, over the C Atom_parse):
+ * scans a whole PDB text and writes every ATOM (and HETATM, unless
+ * PJG_PDB_SKIP_HETATM) record up to the first ENDMDL (unless
+ * PJG_PDB_IGNORE_ENDMDL) into `records`, 59-byte packed rows of the atom
+ * table (x, y, z f64; occupancy, temperature factor f32; serial i32; name
+ * 4 B; altloc; residue name 4 B; chain 2 B; residue number i32; insertion
+ * code; segment 4 B; element 2 B; charge i8).  Host code; thread-safe.
+ * Returns PJG_OK with n_atoms rows and end_offset = where the scan ended
+ * (the ENDMDL line, or len).  A record in a form it does not take (blank
+ * or non-decimal fields, non-printable bytes, a short line, an mmCIF tag,
+ * more records than `capacity`) returns PJG_ERR_INVALID with stop_offset =
+ * that line's offset, and the caller reads the text with its general
+ * parser. */
+enum { PJG_PDB_IGNORE_ENDMDL = 1, PJG_PDB_SKIP_HETATM = 2 };
+pjg_status pjg_parse_pdb(const char *text, int64_t len, int32_t flags, void *records, int64_t capacity,
+                         int64_t *n_atoms, int64_t *end_offset, int64_t *stop_offset);
+
 /* Allocation-free superposition --------------------------------------------
  *
  * No counterpart in the reference.  For callers that cannot allocate device

@@ -246,12 +246,15 @@ void candidates(const Template &T, const Molecule &M, int k, std::vector<int> &o
 
 struct Annulus {
     double centre[3], minBox[3], maxBox[3], min, max;
+    double ra, rb;  // the radii themselves (boundary instrumentation only)
 };
 
 void annulus_set(Annulus &A, const double *u, double a, double b) {
     if (b < a) { double t = a; a = b; b = t; }
     if (a < 0.0) a = 0.0;
     if (b < 0.0) b = 0.0;
+    A.ra = a;
+    A.rb = b;
     for (int i = 0; i < 3; i++) A.centre[i] = u[i];
     A.min = a * a;
     A.max = b * b;
@@ -268,6 +271,28 @@ inline bool annulus_includes(const Annulus &A, const double *x) {
         sum += t * t;
     }
     return !(sum < A.min || sum > A.max);
+}
+
+// Instrumentation of the candidate-pair distance tests (not part of the
+// reference's algorithm): every annulus test a kd query makes, and those
+// whose distance lies within BOUNDARY_EPS of one of the annulus radii
+// (d -+ theta, the lower one raised to 0.5).
+constexpr double BOUNDARY_EPS = 1e-6;
+
+struct BoundaryCount {
+    int64_t tests = 0, near = 0;
+};
+
+inline void count_boundary(const Annulus &A, const double *x, BoundaryCount *bc) {
+    if (!bc) return;
+    double sum = 0.0;
+    for (int i = 0; i < 3; i++) {
+        double t = A.centre[i] - x[i];
+        sum += t * t;
+    }
+    const double d = std::sqrt(sum);
+    bc->tests++;
+    if (std::fabs(d - A.ra) <= BOUNDARY_EPS || std::fabs(d - A.rb) <= BOUNDARY_EPS) bc->near++;
 }
 
 struct Box { double min[3], max[3]; };
@@ -405,11 +430,13 @@ struct KdQuery {
     int count = 0;
     Box box;
     std::vector<int> stack;
+    BoundaryCount *bc = nullptr;
 
-    void reset(const KdTree *t, const Annulus *regions, int nregions) {
+    void reset(const KdTree *t, const Annulus *regions, int nregions, BoundaryCount *counts) {
         tree = t;
         R = regions;
         count = nregions;
+        bc = counts;
         join_box(regions, nregions, box);
         stack.clear();
         stack.push_back(t->root);
@@ -421,7 +448,10 @@ struct KdQuery {
             stack.pop_back();
             if (N.type < 0) {
                 bool in = true;
-                for (int j = 0; j < count && in; j++) in = annulus_includes(R[j], N.min);
+                for (int j = 0; j < count && in; j++) {
+                    count_boundary(R[j], N.min, bc);
+                    in = annulus_includes(R[j], N.min);
+                }
                 if (in) return N.index;
                 continue;
             }
@@ -445,6 +475,7 @@ struct PairStats {
     int64_t scanned = 0;     // sum |R_k|
     int64_t cand = 0;        // sum |C_k|
     std::vector<int64_t> frontier;  // |F_l| per level
+    BoundaryCount boundary;  // candidate-pair distance tests
 };
 
 // ---------------------------------------------------------------------------
@@ -596,7 +627,7 @@ struct Scanner {
                 annulus_set(regions[k][j], atom[oj]->x, mn, mx);
             }
             active[ok] = 1;
-            query[ok].reset(&tree[ok], regions[k].data(), k);
+            query[ok].reset(&tree[ok], regions[k].data(), k, stats ? &stats->boundary : nullptr);
         }
         return k >= 0;
     }
@@ -744,6 +775,7 @@ struct StructureResult {
     std::vector<StreamRow> stream;
     std::vector<Warning> warnings;
     pjg_stats stats{};
+    BoundaryCount boundary;
 };
 
 // ---------------------------------------------------------------------------
@@ -761,6 +793,7 @@ struct JessQuery {
     int64_t ordinal = 0;       // position in the current template's stream
     PairStats pst;
     pjg_stats *stats;
+    BoundaryCount *boundary;
     int n_templates() const { return (int)templates->size(); }
     const Template *tpl() const { return node < n_templates() ? &(*templates)[n_templates() - 1 - node] : nullptr; }
 
@@ -768,6 +801,8 @@ struct JessQuery {
         const Template *T = tpl();
         if (!T) return;
         stats->pairs++;
+        boundary->tests += pst.boundary.tests;
+        boundary->near += pst.boundary.near;
         stats->candidate_entries += pst.cand;
         stats->bytes_candidates += 8 * pst.scanned + 16 * pst.cand;
         int n = T->count();
@@ -818,6 +853,7 @@ void run_structure(const std::vector<Template> &templates, const Molecule &M, in
     Q.s = P.max_dynamic_distance;
     Q.reorder = P.reorder != 0;
     Q.stats = &out.stats;
+    Q.boundary = &out.boundary;
 
     bool partial = false;
     int candidates_seen = 0;
@@ -905,6 +941,7 @@ struct oracle_result {
     std::vector<StreamRow> stream;
     std::vector<Warning> warnings;
     pjg_stats stats{};
+    BoundaryCount boundary;
 };
 
 extern "C" {
@@ -1000,6 +1037,8 @@ oracle_result *oracle_query(const pjg_template_set *ts, const pjg_structure_set 
         a.bytes_candidates += b.bytes_candidates;
         a.bytes_expansion += b.bytes_expansion;
         a.bytes_superposition += b.bytes_superposition;
+        r->boundary.tests += per[s].boundary.tests;
+        r->boundary.near += per[s].boundary.near;
     }
     {
         int64_t H = (int64_t)r->hits.size();
@@ -1071,6 +1110,13 @@ void oracle_warnings(const oracle_result *r, int32_t *structure, int64_t *hits_b
 }
 
 void oracle_stats(const oracle_result *r, pjg_stats *out) { *out = r->stats; }
+
+// Candidate-pair distance tests of the query's kd range queries, and how
+// many of them lie within 1e-6 A of an annulus boundary.
+void oracle_boundary_stats(const oracle_result *r, int64_t *tests, int64_t *near) {
+    *tests = r->boundary.tests;
+    *near = r->boundary.near;
+}
 
 void oracle_free(oracle_result *r) { delete r; }
 

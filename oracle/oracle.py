@@ -48,6 +48,7 @@ def lib():
         L.oracle_warnings.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_stats.argtypes = [C.c_void_p, C.c_void_p]
         L.oracle_free.argtypes = [C.c_void_p]
+        L.oracle_boundary_stats.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_set_kd_right_first.argtypes = [C.c_int]
         L.oracle_set_kd_right_first(KD_RIGHT_FIRST)
         _lib = L
@@ -113,6 +114,9 @@ def query(ptemplates, pstructures, *, rmsd_threshold, distance_cutoff, max_dynam
         stats = Stats()
         L.oracle_stats(h, C.byref(stats))
         out["stats"] = stats.as_dict()
+        tests, near = C.c_int64(), C.c_int64()
+        L.oracle_boundary_stats(h, C.byref(tests), C.byref(near))
+        out["boundary"] = {"tests": tests.value, "near": near.value}
         return out
     finally:
         L.oracle_free(h)

@@ -27,11 +27,13 @@ NVCC_FLAGS = [
     "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
     "-I", str(INCLUDE),
 ]
-SOURCES = ["pjg_kernels.cu", "pjg_api.cu"]
+SOURCES = ["pjg_kernels.cu", "pjg_api.cu", "pjg_io.cpp"]
 # library variants: "" the product library; "prof" adds the search profile
 # (event counts and section cycles of k_search, written per query to the
-# file named by PJG_PROF_OUT) and is never the timed build
-VARIANTS = {"": [], "prof": ["-DPJG_SEARCH_PROF=1"]}
+# file named by PJG_PROF_OUT) and is never the timed build; "blk8"/"blk16"
+# cull by blocks of 8/16 leaves instead of 32 (measured against each other)
+VARIANTS = {"": [], "prof": ["-DPJG_SEARCH_PROF=1"], "blk8": ["-DPJG_CULL_BLK=8"], "blk16": ["-DPJG_CULL_BLK=16"],
+            "blk8prof": ["-DPJG_CULL_BLK=8", "-DPJG_SEARCH_PROF=1"]}
 
 
 def lib_path(variant: str = "") -> pathlib.Path:
@@ -52,7 +54,8 @@ def _stale(lib: pathlib.Path = LIB) -> bool:
     if not lib.exists():
         return True
     t = lib.stat().st_mtime
-    deps = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + [INCLUDE / "pjg.h", pathlib.Path(__file__)]
+    deps = (list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.cpp")) +
+            [INCLUDE / "pjg.h", pathlib.Path(__file__)])
     return any(p.stat().st_mtime > t for p in deps)
 
 

@@ -109,6 +109,55 @@ def parse_pdb(file, *, ignore_endmdl=False, skip_hetatm=False):
     return records, id_, date, name
 
 
+def _header_fields(lines):
+    """(id, date, name) from HEADER lines, as `parse_pdb` reads them."""
+    id_ = date = name = None
+    for line in lines:
+        if id_ is None:
+            id_ = line[62:66].strip() or None
+        if date is None:
+            text = line[50:59].strip()
+            if text:
+                date = datetime.datetime.strptime(text, "%d-%b-%y").date()
+        if name is None:
+            name = line[10:50].strip() or None
+    return id_, date, name
+
+
+def _header_lines(text: str, end: int):
+    """The lines of text[:end] that start with HEADER."""
+    starts = [0] if text.startswith("HEADER") and end > 0 else []
+    i = text.find("\nHEADER", 0, end)
+    while i >= 0:
+        starts.append(i + 1)
+        i = text.find("\nHEADER", i + 1, end)
+    out = []
+    for s in starts:
+        e = text.find("\n", s)
+        out.append(text[s:e if e >= 0 else len(text)])
+    return out
+
+
+def parse_pdb_text(text: str, *, ignore_endmdl=False, skip_hetatm=False):
+    """`parse_pdb` over a whole text, the atom records read by the native
+    reader of libpjg (one call, no per-atom Python work).  Texts it does not
+    take (non-ASCII, unusual field forms, mmCIF) and machines without the
+    library go through `parse_pdb`, which gives the same records."""
+    if text.isascii():
+        try:
+            from . import _native
+
+            flags = (_native.PDB_IGNORE_ENDMDL if ignore_endmdl else 0) | (_native.PDB_SKIP_HETATM if skip_hetatm
+                                                                             else 0)
+            fast = _native.parse_pdb_records(text.encode("ascii"), flags, ATOM_DTYPE)
+        except (OSError, RuntimeError):
+            fast = None
+        if fast is not None:
+            records, end = fast
+            return (records, *_header_fields(_header_lines(text, end)))
+    return parse_pdb(io.StringIO(text), ignore_endmdl=ignore_endmdl, skip_hetatm=skip_hetatm)
+
+
 class PDBMoleculeParser:
     """Parse a molecule from PDB text (``_io.py:52-103`` of the reference)."""
 
@@ -128,9 +177,12 @@ class PDBMoleculeParser:
         except TypeError:
             handle = nullcontext(file)
         with handle as f:
-            records, id_, date, name = parse_pdb(
-                f, ignore_endmdl=self.ignore_endmdl, skip_hetatm=self.skip_hetatm
-            )
+            text = f.read()
+        if not isinstance(text, str):
+            text = text.decode()
+        records, id_, date, name = parse_pdb_text(
+            text, ignore_endmdl=self.ignore_endmdl, skip_hetatm=self.skip_hetatm
+        )
         return molecule_type._from_records(
             records,
             id=self.id if self.id is not None else id_,

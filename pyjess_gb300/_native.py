@@ -29,7 +29,7 @@ EXPORTED = (
     "pjg_structures_create", "pjg_structures_destroy", "pjg_query", "pjg_results_count",
     "pjg_results_atom_count", "pjg_results_copy", "pjg_results_warning_count",
     "pjg_results_warnings", "pjg_results_stats", "pjg_results_destroy", "pjg_set_tuning", "pjg_get_tuning",
-    "pjg_device_name", "pjg_superpose_noalloc", "pjg_noalloc_last_error",
+    "pjg_device_name", "pjg_parse_pdb", "pjg_superpose_noalloc", "pjg_noalloc_last_error",
 )
 
 _lib = None
@@ -81,6 +81,9 @@ def load(build_if_missing: bool = True):
         L.pjg_get_tuning.restype = C.c_int
         L.pjg_device_name.argtypes = [C.c_char_p, C.c_int32]
         L.pjg_device_name.restype = C.c_int
+        L.pjg_parse_pdb.argtypes = [C.c_char_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64,
+                                    C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.pjg_parse_pdb.restype = C.c_int
         _lib = L
         return L
 
@@ -232,3 +235,22 @@ def device_name() -> str:
     buf = C.create_string_buffer(256)
     _check(L.pjg_device_name(buf, 256), "pjg_device_name")
     return buf.value.decode(errors="replace")
+
+
+PDB_IGNORE_ENDMDL = 1
+PDB_SKIP_HETATM = 2
+
+
+def parse_pdb_records(data: bytes, flags: int, dtype):
+    """Atom records of a PDB text by the library's native reader: (records,
+    end offset), or None when the text needs the general reader (a record in
+    a form the native reader does not take).  Host code: no device needed."""
+    L = load()
+    cap = data.count(b"\n") + 1
+    records = np.empty(cap, dtype=dtype)
+    n, end, stop = C.c_int64(), C.c_int64(), C.c_int64()
+    st = L.pjg_parse_pdb(data, len(data), int(flags), records.ctypes.data, cap, C.byref(n), C.byref(end),
+                         C.byref(stop))
+    if st != PJG_OK:
+        return None
+    return records[: n.value], end.value

@@ -34,6 +34,32 @@ class PackedTemplates:
     def n_templates(self) -> int:
         return len(self.atom_offset) - 1
 
+    def subset(self, indices) -> "PackedTemplates":
+        """The templates at `indices`, repacked contiguously (in that order)."""
+        indices = np.asarray(indices, dtype=np.int64)
+        a_lo, a_hi = self.atom_offset[indices], self.atom_offset[indices + 1]
+        atoms = (np.concatenate([np.arange(a, b) for a, b in zip(a_lo, a_hi)]).astype(np.int64)
+                 if len(indices) else np.zeros(0, np.int64))
+
+        def ragged(offsets, values):
+            lo, hi = offsets[atoms], offsets[atoms + 1]
+            off = np.zeros(len(atoms) + 1, np.int32)
+            np.cumsum(hi - lo, out=off[1:])
+            rows = (np.concatenate([np.arange(a, b) for a, b in zip(lo, hi)]).astype(np.int64)
+                    if len(atoms) else np.zeros(0, np.int64))
+            return off, np.ascontiguousarray(values[rows])
+
+        name_off, names = ragged(self.name_offset, self.names)
+        res_off, resnames = ragged(self.resname_offset, self.resnames)
+        aoff = np.zeros(len(indices) + 1, np.int32)
+        np.cumsum(a_hi - a_lo, out=aoff[1:])
+        return PackedTemplates(
+            atom_offset=aoff, code=np.ascontiguousarray(self.code[atoms]),
+            res_seq=np.ascontiguousarray(self.res_seq[atoms]), chain=np.ascontiguousarray(self.chain[atoms]),
+            xyz=np.ascontiguousarray(self.xyz[atoms]), dist_weight=np.ascontiguousarray(self.dist_weight[atoms]),
+            name_offset=name_off, names=names, resname_offset=res_off, resnames=resnames,
+            dim=np.ascontiguousarray(self.dim[indices]))
+
     def abi(self) -> TemplateSet:
         s = TemplateSet()
         s.n_templates = self.n_templates

@@ -6,7 +6,7 @@
 //   k_candidate_counts            |C| and |R| of every (structure, signature)
 //   k_struct_totals               candidate entries per structure
 //   per structure chunk (bounded entry budget):
-//     k_scan_*, k_block_counts    list offsets, blocks of 32 leaves
+//     k_scan_*, k_block_counts    list offsets, culling blocks of CULL_BLK leaves
 //     k_candidates                lists in candidate order
 //     k_demand_levels             requests the lists of the first levels
 //     k_leaf_order, k_leaf_sorted, k_leaf_exact, k_mark_ordered
@@ -1042,14 +1042,17 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
 
     {
         // chunks of structures under an entry budget.  A candidate entry
-        // costs at most ~26 B: its atom in candidate order (4), block boxes
-        // (~1), per-list arrays (~1) and, once its list is put in leaf order,
-        // its atom and FP32 point in leaf order (20; allocated as lists are
-        // requested).  The budget takes 60% of the free device memory
-        // (counting memory the stream-ordered pool holds unused) at that
-        // worst case, at least 48M entries, which leaves room for growing
-        // the leaf arrays (old and new copies live at once while they grow).  Fewer, larger chunks leave fewer
-        // kernel tails and search rounds.  PJG_ENTRY_BUDGET overrides it.
+        // costs at most ENTRY_BYTES: its atom in candidate order (4), block
+        // boxes (32 B a block of CULL_BLK leaves), per-list arrays (~1) and,
+        // once its list is put in leaf order, its atom and FP32 point in
+        // leaf order (20; allocated as lists are requested).  The budget
+        // takes 60% of the free device memory (counting memory the
+        // stream-ordered pool holds unused) at that worst case, at least 48M
+        // entries, which leaves room for growing the leaf arrays (old and new
+        // copies live at once while they grow).  Fewer, larger chunks leave
+        // fewer kernel tails and search rounds.  PJG_ENTRY_BUDGET overrides
+        // it.
+        constexpr double ENTRY_BYTES = 25.0 + 32.0 / CULL_BLK;
         int64_t ENTRY_BUDGET = 48ll << 20;
         {
             size_t free_b = 0, total_b = 0;
@@ -1063,7 +1066,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                         free_b += (size_t)(reserved - used);
                 }
                 cudaGetLastError();
-                ENTRY_BUDGET = std::max<int64_t>(ENTRY_BUDGET, (int64_t)((double)free_b * 0.6 / 26.0));
+                ENTRY_BUDGET = std::max<int64_t>(ENTRY_BUDGET, (int64_t)((double)free_b * 0.6 / ENTRY_BYTES));
             }
             const char *v = getenv("PJG_ENTRY_BUDGET");
             if (v && atoll(v) > 0) ENTRY_BUDGET = atoll(v);
@@ -1153,7 +1156,8 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             CUDA_TRY(dalloc(d_offset, (size_t)Wc, st));
             CUDA_TRY(cudaEventRecord(ev[1], st));
             CUDA_TRY(scan_exclusive(cnt_c, Wc, d_offset.p, scan_tmp, st));
-            // blocks of 32 leaves: counts, offsets, total (one small sync)
+            // culling blocks of CULL_BLK leaves: counts, offsets, total (one
+            // small sync)
             int64_t nblocks = 0;
             CUDA_TRY(dalloc(d_nblk, (size_t)Wc, st));
             CUDA_TRY(dalloc(d_boff, (size_t)Wc, st));

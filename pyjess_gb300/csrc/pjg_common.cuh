@@ -114,7 +114,7 @@ struct CandView {
     const int32_t *leaf_atom;       // structure-local atom, kd leaf order
     const float4 *leaf_xyz;         // its FP32 point (xyz32)
     const int64_t *blk_offset;      // first block of the list
-    const float4 *blk_lo;           // bounding box of each block of 32
+    const float4 *blk_lo;           // bounding box of each block of CULL_BLK
     const float4 *blk_hi;           //   consecutive leaves (FP32)
 };
 

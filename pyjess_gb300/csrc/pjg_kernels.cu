@@ -399,7 +399,7 @@ __global__ void k_scan_add(int64_t *out, int64_t n, const int64_t *tile_offsets)
 // centroid-relative keys are a monotone rounding of the FP64 coordinates, so
 // a tie there only sends the list to the exact path.  Exact path: the
 // literal qselect replay on the FP64 coordinates (k_leaf_exact).  Each list
-// also gets the bounding boxes of its blocks of 32 consecutive leaves (the
+// also gets the bounding boxes of its blocks of CULL_BLK consecutive leaves (the
 // search culls whole blocks against a parent's join box).
 
 __device__ __forceinline__ int axis_cmp(double c, double d) { return c < d ? -1 : c > d ? 1 : 0; }
@@ -490,14 +490,16 @@ struct LeafWarp {
     uint16_t seg_n[LEAF_FAST_MAX];
 };
 
-// Bounding boxes of the blocks of 32 consecutive leaves of a list.
+// Bounding boxes of the blocks of CULL_BLK consecutive leaves of a list
+// (one warp; each 32-leaf step reduces CULL_BLK-lane segments).
 __device__ void write_boxes(int m, int64_t o, const float4 *leaf_xyz, int64_t bo, float4 *blk_lo, float4 *blk_hi) {
     const int lane = lane_id();
     for (int b = 0; b * 32 < m; b++) {
-        int r = b * 32 + lane;
-        float4 p = leaf_xyz[o + (r < m ? r : b * 32)];
+        const int r = b * 32 + lane;
+        const int first = r & ~(CULL_BLK - 1);  // first leaf of this lane's block
+        float4 p = leaf_xyz[o + (r < m ? r : first < m ? first : b * 32)];
         float mnx = p.x, mny = p.y, mnz = p.z, mxx = p.x, mxy = p.y, mxz = p.z;
-        for (int off = 16; off; off >>= 1) {
+        for (int off = CULL_BLK / 2; off; off >>= 1) {
             mnx = fminf(mnx, __shfl_xor_sync(FULL_MASK, mnx, off));
             mny = fminf(mny, __shfl_xor_sync(FULL_MASK, mny, off));
             mnz = fminf(mnz, __shfl_xor_sync(FULL_MASK, mnz, off));
@@ -505,16 +507,14 @@ __device__ void write_boxes(int m, int64_t o, const float4 *leaf_xyz, int64_t bo
             mxy = fmaxf(mxy, __shfl_xor_sync(FULL_MASK, mxy, off));
             mxz = fmaxf(mxz, __shfl_xor_sync(FULL_MASK, mxz, off));
         }
-        if (lane == 0) {
-            blk_lo[bo + b] = make_float4(mnx, mny, mnz, 0.f);
-            blk_hi[bo + b] = make_float4(mxx, mxy, mxz, 0.f);
+        if ((lane & (CULL_BLK - 1)) == 0 && first < m) {
+            blk_lo[bo + r / CULL_BLK] = make_float4(mnx, mny, mnz, 0.f);
+            blk_hi[bo + r / CULL_BLK] = make_float4(mxx, mxy, mxz, 0.f);
         }
     }
     __syncwarp();
 }
 
-// Leaf order of a list from its partitioned candidate array `order`
-// (read backwards: the right subtree is visited first), plus its block boxes.
 __device__ void write_leaves(const uint16_t *order, int m, int64_t lo, const int32_t *ca, const float4 *pts,
                              int32_t *leaf_atom, float4 *leaf_xyz, int64_t bo, float4 *blk_lo, float4 *blk_hi) {
     const int lane = lane_id();
@@ -1464,7 +1464,7 @@ __global__ void k_mark_ordered(LeafDemand dm) {
 
 __global__ void k_block_counts(int64_t n, const int32_t *count, int32_t *nblk) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) nblk[i] = (count[i] + 31) / 32;
+    if (i < n) nblk[i] = (count[i] + CULL_BLK - 1) / CULL_BLK;
 }
 
 // ---------------------------------------------------------------------------
@@ -1727,7 +1727,7 @@ __device__ double lane_rmsd(int n, const int32_t *atoms, const double *xyz, cons
 // or more): one parent at a time; its chain of atoms, key bits and FP32
 // annulus bounds sit in shared memory and are read by all lanes as
 // broadcasts; the parent's join box (intersection of its annulus boxes)
-// culls whole blocks of 32 consecutive leaves by their bounding boxes, the
+// culls whole blocks of CULL_BLK consecutive leaves by their bounding boxes, the
 // leaves of the surviving blocks inside the join box are queued, and the
 // full tests run on batches of 32 queued leaves.  Product mode (shorter
 // lists): lanes take consecutive (parent, candidate) positions of the
@@ -2302,9 +2302,9 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                     // issued before the chain is gathered.
                     SPROF_ADD(SP_BLOCK_VISITS, 1);
                     SPROF_ADD(SP_BLOCK_VISITS_L0, lev == 0);
-                    const int nblk = (mc + 31) >> 5;
+                    const int nblk = (mc + CULL_BLK - 1) / CULL_BLK;
                     const int pstart = st.cnd[lev];
-                    const int gfirst = pstart >> 5;
+                    const int gfirst = pstart / CULL_BLK;
                     const int64_t boff = st.blk_off[child];
                     float4 bl = make_float4(0.f, 0.f, 0.f, 0.f), bh = bl;
                     if (gfirst + lane < nblk) {
@@ -2489,30 +2489,42 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         SPROF_ADD(SP_G0_ITERS, 1);
                         SPROF_ADD(SP_BLOCKS_TESTED, min(32, nblk - g0));
                         SPROF_ADD(SP_BLOCKS_HIT, __popc(hm));
-                        // hit blocks in order; the leaves of the next hit
-                        // block are loaded while the current one is queued
-                        int nxt = -1;
+                        // hit blocks in order, 32 / CULL_BLK of them a step:
+                        // lane l takes leaf l % CULL_BLK of the step's
+                        // (l / CULL_BLK)-th hit block; the leaves of the next
+                        // step are loaded while the current one is queued
+                        constexpr int GRP = 32 / CULL_BLK;
+                        const int slot = lane / CULL_BLK;
+                        auto step_leaf = [&](unsigned &h) -> int {
+                            // this lane's leaf position in the next step (-1:
+                            // its slot has no block), the step's blocks
+                            // removed from h
+                            unsigned hh = h;
+                            for (int i = 0; i < slot; i++) hh &= hh - 1;
+                            const int q = hh ? (g0 + __ffs(hh) - 1) * CULL_BLK + (lane & (CULL_BLK - 1)) : -1;
+                            for (int i = 0; i < GRP; i++) h &= h - 1;
+                            return q;
+                        };
+                        bool have = hm != 0;
+                        int qnext = -1;
                         float4 xn = make_float4(0.f, 0.f, 0.f, 0.f);
-                        if (hm) {
-                            nxt = g0 + __ffs(hm) - 1;
-                            hm &= hm - 1;
-                            if (nxt * 32 + lane < mc) xn = cd.leaf_xyz[coff + nxt * 32 + lane];
+                        if (have) {
+                            qnext = step_leaf(hm);
+                            if (qnext >= 0 && qnext < mc) xn = cd.leaf_xyz[coff + qnext];
                         }
-                        while (nxt >= 0) {
-                            const int blk = nxt;
+                        while (have) {
+                            const int q = qnext;
                             const float4 xc = xn;
-                            nxt = -1;
-                            if (hm) {
-                                nxt = g0 + __ffs(hm) - 1;
-                                hm &= hm - 1;
-                                if (nxt * 32 + lane < mc) xn = cd.leaf_xyz[coff + nxt * 32 + lane];
+                            have = hm != 0;
+                            if (have) {
+                                qnext = step_leaf(hm);
+                                if (qnext >= 0 && qnext < mc) xn = cd.leaf_xyz[coff + qnext];
                             }
-                            const int q = blk * 32 + lane;
                             // inside the join box and not certainly outside
                             // the parent's own annulus (the FP32 reject
                             // bounds of the full test, so the full test
                             // would reject the same leaves)
-                            bool inb = q < mc && q >= pstart &&
+                            bool inb = q >= 0 && q < mc && q >= pstart &&
                                        !(xc.x < box_lo[0] || xc.x > box_hi[0] || xc.y < box_lo[1] ||
                                          xc.y > box_hi[1] || xc.z < box_lo[2] || xc.z > box_hi[2]);
                             if (FP32 && inb) {

@@ -22,6 +22,14 @@ constexpr int SEARCH_WARPS = PJG_SEARCH_WARPS;  // warps per block of k_search
 #ifndef PJG_SEARCH_MIN_BLOCKS
 #define PJG_SEARCH_MIN_BLOCKS 2
 #endif
+// leaves per culling block: k_search tests a parent's join box against the
+// bounding box of each block of CULL_BLK consecutive leaves of a list in kd
+// leaf order, and loads the leaves of the blocks it meets (8, 16 or 32)
+#ifndef PJG_CULL_BLK
+#define PJG_CULL_BLK 32
+#endif
+constexpr int CULL_BLK = PJG_CULL_BLK;
+static_assert(CULL_BLK == 8 || CULL_BLK == 16 || CULL_BLK == 32, "culling block of 8, 16 or 32 leaves");
 // templates of more than 32 atoms: k_search_large, warps per block and
 // per-warp shared-memory bytes for templates of up to nmax atoms
 constexpr int LARGE_WARPS = 2;
@@ -221,7 +229,7 @@ void launch_axis_ranks(cudaStream_t st, int32_t n_structures, const int64_t *ato
                        const double *xyz64, int64_t n_atoms, unsigned long long *tile_key, uint16_t *tile_idx,
                        uint32_t *lrank, uint32_t *urank);
 
-// blocks of 32 leaves per list: ceil(count / 32)
+// culling blocks per list: ceil(count / CULL_BLK)
 void launch_block_counts(cudaStream_t st, int64_t n, const int32_t *count, int32_t *nblk);
 
 // k_search variant: wide = 32-bit frontier entries (structures above 65535
