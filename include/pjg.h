@@ -113,6 +113,12 @@ typedef struct {
     int32_t reorder;                 /* 0/1                                */
     int32_t mode;                    /* PJG_MODE_*                         */
     double guard_band;               /* Angstrom, FP32 mode (0: 1e-4)      */
+    int32_t count_only;              /* 1: count the hits and warnings
+                                        (pjg_results_count, _atom_count,
+                                        _warning_count, stats) without
+                                        keeping them; copying them out
+                                        then returns PJG_ERR_INVALID.  For
+                                        queries whose hits outgrow memory */
 } pjg_query_params;
 
 /* Per-query counters and device timings (milliseconds, CUDA events). */
@@ -225,6 +231,15 @@ pjg_status pjg_results_copy(const pjg_results *r, int32_t *structure,
 int64_t pjg_results_warning_count(const pjg_results *r);
 pjg_status pjg_results_warnings(const pjg_results *r, int32_t *structure,
                                 int64_t *hits_before);
+
+/* Replaces, for every hit at once, Hit.atoms(transform=True) /
+ * Molecule.transform(hit.transformation) of the reference
+ * (src/pyjess/_jess.pyx:878-907, 2343-2377): each hit's matched molecule
+ * atoms mapped into its template's frame, T(v) R T(-c) x, computed on the
+ * device from the structures `s` the query searched (any other set returns
+ * PJG_ERR_INVALID).  xyz[3k + d] for hit atom k, in the order of
+ * pjg_results_copy's atoms (pjg_results_atom_count x 3 doubles). */
+pjg_status pjg_results_superposed(const pjg_results *r, const pjg_structures *s, double *xyz);
 
 /* Counters and device timings of the query that produced `r`. */
 pjg_status pjg_results_stats(const pjg_results *r, pjg_stats *stats);

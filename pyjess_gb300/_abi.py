@@ -48,6 +48,7 @@ class QueryParams(C.Structure):
         ("reorder", C.c_int32),
         ("mode", C.c_int32),
         ("guard_band", C.c_double),
+        ("count_only", C.c_int32),
     ]
 
 

@@ -1075,9 +1075,9 @@ class HitArrays:
     """
 
     __slots__ = ("molecule", "template", "ordinal", "rmsd", "rotation", "centres", "atom_offset", "atoms",
-                 "_jess", "_molecules")
+                 "_jess", "_molecules", "_device")
 
-    def __init__(self, data, jess, molecules):
+    def __init__(self, data, jess, molecules, device=None):
         n = data["count"]
         self.molecule = data["structure"]
         self.template = data["template"]
@@ -1089,6 +1089,16 @@ class HitArrays:
         self.atoms = data["atoms"]
         self._jess = jess
         self._molecules = molecules
+        self._device = device  # (device result, device structures) of the query
+
+    def superposed_atoms(self):
+        """The matched atoms of every hit in its template's frame: an
+        (atoms, 3) array aligned with `atoms` -- what ``Hit.atoms()`` gives
+        hit by hit -- computed on the GPU from the query's device results."""
+        if self._device is None:
+            raise RuntimeError("the device results of this query are no longer held")
+        result, structures = self._device
+        return result.superposed(structures)
 
     def __len__(self):
         return len(self.rmsd)
@@ -1233,9 +1243,9 @@ class Jess:
                   max_candidates, ignore_chain, best_match, reorder)
         mode = {"fp32": _native.MODE_BATCHED_FP32, "fp64": _native.MODE_BATCHED_FP64,
                 "plain": _native.MODE_PLAIN_FP64}[precision]
-        result = _native.query(self._device_templates(), _native.structures_for(molecules),
-                               q._params(mode))
+        structures = _native.structures_for(molecules)
+        result = _native.query(self._device_templates(), structures, q._params(mode))
         for s, ws in enumerate(result.warnings_by_structure(len(molecules))):
             for _ in ws:
                 warnings.warn("Jess returned a superposition matrix with NaN values", UserWarning, 2)
-        return HitArrays(result.arrays(), self, molecules)
+        return HitArrays(result.arrays(), self, molecules, device=(result, structures))

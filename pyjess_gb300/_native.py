@@ -28,7 +28,8 @@ EXPORTED = (
     "pjg_init", "pjg_last_error", "pjg_templates_create", "pjg_templates_destroy",
     "pjg_structures_create", "pjg_structures_destroy", "pjg_query", "pjg_results_count",
     "pjg_results_atom_count", "pjg_results_copy", "pjg_results_warning_count",
-    "pjg_results_warnings", "pjg_results_stats", "pjg_results_destroy", "pjg_set_tuning", "pjg_get_tuning",
+    "pjg_results_warnings", "pjg_results_superposed", "pjg_results_stats", "pjg_results_destroy",
+    "pjg_set_tuning", "pjg_get_tuning",
     "pjg_device_name", "pjg_parse_pdb", "pjg_superpose_noalloc", "pjg_noalloc_last_error",
 )
 
@@ -75,6 +76,8 @@ def load(build_if_missing: bool = True):
         L.pjg_results_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
         L.pjg_results_stats.restype = C.c_int
         L.pjg_results_destroy.argtypes = [C.c_void_p]
+        L.pjg_results_superposed.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.pjg_results_superposed.restype = C.c_int
         L.pjg_set_tuning.argtypes = [C.POINTER(Tuning)]
         L.pjg_set_tuning.restype = C.c_int
         L.pjg_get_tuning.argtypes = [C.POINTER(Tuning)]
@@ -184,6 +187,15 @@ class Result:
                 "pjg_results_copy")
             self._arrays = a
         return self._arrays
+
+    def superposed(self, structures: "Structures") -> np.ndarray:
+        """Every hit's matched atoms in its template's frame, (atoms, 3),
+        computed on the device (pjg_results_superposed)."""
+        L = _lib
+        na = L.pjg_results_atom_count(self.handle)
+        out = np.zeros((na, 3), np.float64)
+        _check(L.pjg_results_superposed(self.handle, structures.handle, out.ctypes.data), "pjg_results_superposed")
+        return out
 
     def warnings(self):
         L = _lib

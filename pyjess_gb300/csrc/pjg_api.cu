@@ -254,6 +254,9 @@ struct pjg_results {
     HitStore store;
     pjg_stats stats{};
     int device = 0;
+    // count-only query: store.hits/atoms/warns are counts, nothing is kept
+    bool count_only = false;
+    const pjg_structures *structures = nullptr;  // the set the query searched
 };
 
 namespace {
@@ -900,11 +903,14 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     if (P->ignore_chain < 0 || P->ignore_chain > 2) return fail(PJG_ERR_INVALID, "invalid ignore_chain %d", P->ignore_chain);
     if (P->max_candidates < -1) return fail(PJG_ERR_INVALID, "invalid max_candidates %d", P->max_candidates);
     if (P->mode < 0 || P->mode > 2) return fail(PJG_ERR_INVALID, "invalid mode %d", P->mode);
+    if (P->count_only < 0 || P->count_only > 1) return fail(PJG_ERR_INVALID, "invalid count_only %d", P->count_only);
     if (!std::isfinite(P->distance_cutoff) || !std::isfinite(P->max_dynamic_distance))
         return fail(PJG_ERR_INVALID, "non-finite distance parameters");
 
     pjg_results *res = new pjg_results;
     cudaGetDevice(&res->device);
+    res->count_only = P->count_only != 0;
+    res->structures = sp;
     const int T = tp->T, S = sp->S, G = tp->G;
     const bool fp32 = P->mode == PJG_MODE_BATCHED_FP32;
     cudaStream_t st = nullptr;
@@ -1522,7 +1528,12 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                     CUDA_TRY(cudaMemcpyAsync(tot, d_rtotals.p, sizeof tot, cudaMemcpyDeviceToHost, st));
                     CUDA_TRY(cudaStreamSynchronize(st));
                     passing += (int64_t)tot[3];
-                    if (tot[0] + tot[1] > 0) {
+                    if (P->count_only) {
+                        // counts only: the hits and warnings are not kept
+                        res->store.hits += (int64_t)tot[0];
+                        res->store.atoms += (int64_t)tot[2];
+                        res->store.warns += (int64_t)tot[1];
+                    } else if (tot[0] + tot[1] > 0) {
                         HitStore &hs = res->store;
                         CUDA_TRY(hs.reserve((int64_t)tot[0], (int64_t)tot[2], (int64_t)tot[1], st));
                         launch_gather_hits(st, rows, T, s0, hs.atoms, tp->d_atom_begin, cr, rr, d_r_hit.p,
@@ -1646,6 +1657,7 @@ int64_t pjg_results_atom_count(const pjg_results *r) { return r ? r->store.atoms
 pjg_status pjg_results_copy(const pjg_results *r, int32_t *structure, int32_t *template_index, int64_t *ordinal,
                             double *rmsd, double *rotation, double *centres, int64_t *atom_offset, int32_t *atoms) {
     if (!r) return fail(PJG_ERR_INVALID, "null results");
+    if (r->count_only) return fail(PJG_ERR_INVALID, "the results of a count-only query hold no hits");
     const HitStore &hs = r->store;
     const size_t n = (size_t)hs.hits;
     if (atom_offset) atom_offset[n] = hs.atoms;
@@ -1668,8 +1680,41 @@ pjg_status pjg_results_copy(const pjg_results *r, int32_t *structure, int32_t *t
 
 int64_t pjg_results_warning_count(const pjg_results *r) { return r ? r->store.warns : 0; }
 
+pjg_status pjg_results_superposed(const pjg_results *r, const pjg_structures *s, double *xyz) {
+    if (!r || !s) return fail(PJG_ERR_INVALID, "null argument");
+    if (r->count_only) return fail(PJG_ERR_INVALID, "the results of a count-only query hold no hits");
+    if (s != r->structures) return fail(PJG_ERR_INVALID, "structures differ from the ones the query searched");
+    const HitStore &hs = r->store;
+    if (hs.atoms == 0) return PJG_OK;
+    if (!xyz) return fail(PJG_ERR_INVALID, "null output");
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (prev != r->device) cudaSetDevice(r->device);
+    cudaStream_t st = nullptr;
+    double *d_out = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&d_out, (size_t)hs.atoms * 3 * sizeof(double), st);
+    if (e == cudaSuccess) {
+        launch_superposed_atoms(st, hs.hits, hs.structure, hs.atom_offset, hs.atoms_, hs.rot, hs.centres,
+                                s->d_atom_base, s->d_xyz64, d_out);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(xyz, d_out, (size_t)hs.atoms * 3 * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (d_out) cudaFreeAsync(d_out, st);
+    if (st) {
+        cudaError_t e2 = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) e = e2;
+        cudaStreamDestroy(st);
+    }
+    if (prev != r->device) cudaSetDevice(prev);
+    if (e != cudaSuccess) return fail(PJG_ERR_CUDA, "superposed atoms: %s", cudaGetErrorString(e));
+    return PJG_OK;
+}
+
 pjg_status pjg_results_warnings(const pjg_results *r, int32_t *structure, int64_t *hits_before) {
     if (!r) return fail(PJG_ERR_INVALID, "null results");
+    if (r->count_only) return fail(PJG_ERR_INVALID, "the results of a count-only query hold no warnings");
     const HitStore &hs = r->store;
     if (hs.warns == 0) return PJG_OK;
     int prev = 0;

@@ -36,3 +36,28 @@ def test_query_arrays_empty():
 
     arr = Jess().query_arrays([Molecule()], 2, 2, 2)
     assert len(arr) == 0 and list(arr.molecule_offsets()) == [0, 0]
+
+
+def test_superposed_atoms_match_host_transform(t133, t412, amy, ayx):
+    """HitArrays.superposed_atoms (the device transform of every hit's
+    matched atoms) against Hit.atoms(transform=True) on the host."""
+    from pyjess_gb300 import Jess
+
+    jess = Jess([t133, t412])
+    mols = [amy, ayx]
+    arr = jess.query_arrays(mols, 2, 4, 4)
+    xyz = arr.superposed_atoms()
+    assert xyz.shape == (len(arr.atoms), 3) and len(arr) > 0
+    worst = 0.0
+    for i in range(len(arr)):
+        hit = arr.hit(i)
+        host = np.array([[a.x, a.y, a.z] for a in hit.atoms(transform=True)])
+        a0, a1 = arr.atom_offset[i], arr.atom_offset[i + 1]
+        worst = max(worst, float(np.abs(xyz[a0:a1] - host).max()))
+    assert worst < 1e-12, worst
+    # the transformed atoms reproduce each hit's rmsd against its template
+    for i in range(0, len(arr), 7):
+        tpl = np.array([[a.x, a.y, a.z] for a in jess[int(arr.template[i])]])
+        a0, a1 = arr.atom_offset[i], arr.atom_offset[i + 1]
+        rmsd = np.sqrt(((xyz[a0:a1] - tpl) ** 2).sum() / len(tpl))
+        assert abs(rmsd - arr.rmsd[i]) < 1e-9
