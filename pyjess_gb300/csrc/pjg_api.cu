@@ -1358,7 +1358,20 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             int64_t want_rows = 2 * n_pairs;
             if (P->best_match && P->max_candidates >= 0) {
                 const int64_t bound = n_pairs * ((int64_t)P->max_candidates + 2);
-                if (bound <= row_budget()) want_rows = std::max(want_rows, bound);
+                const int64_t budget = row_budget();
+                if (bound <= budget) {
+                    want_rows = std::max(want_rows, bound);
+                } else if (Sc > 1) {
+                    // with the chunk's own lists in memory its bound no
+                    // longer fits: take fewer structures before searching
+                    chunk_cap = std::max(1, (int)((double)Sc * (double)budget / (double)bound));
+                    bound_cap = std::min(bound_cap, chunk_cap);
+                    chunks--;
+                    row_splits++;
+                    CUDA_TRY(cudaMemcpyAsync(d_counters.p, chunk_snap, sizeof chunk_snap, cudaMemcpyHostToDevice,
+                                             st));
+                    continue;
+                }
             }
             if (c_cap < want_rows) {
                 c_cap = want_rows;

@@ -211,6 +211,9 @@ def autotune(ptemplates, pstructures, params: dict, *, sample_pairs: int = 1_000
         "ms": best_ms,
         "default_ms": default_ms,
         "trials": len(trials),
+        # every configuration timed: the knobs that differ from the
+        # defaults, and its device milliseconds
+        "timed": [[{k: v for k, v in c.items() if v != DEFAULTS[k]}, round(t, 3)] for c, t in trials],
         "sample": f"{len(idx)} of {pstructures.n_structures} structures x {ptemplates.n_templates} templates",
         "tune_s": round(time.perf_counter() - t0, 1),
         "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime()),
