@@ -933,6 +933,10 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     DBuf<int32_t> d_lstate;
     DBuf<int64_t> d_work;
     DBuf<unsigned long long> d_nwork, d_nsusp;
+    // lists filled on demand
+    DBuf<int32_t> d_fill_state;
+    DBuf<int64_t> d_fill_work;
+    DBuf<unsigned long long> d_nfill;
     DBuf<Suspended> d_susp_a, d_susp_b;
     DBuf<unsigned char> d_pool_a, d_pool_b;
     DBuf<unsigned long long> d_pool_used;
@@ -1195,14 +1199,22 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             }
             CUDA_TRY(dalloc(d_leaf_xyz, d_leaf_atom.n, st));
             int64_t leaf_filled = 0;  // leaf entries of the lists ordered so far
+            const int fill_blocks = std::max(1, (int)std::min<int64_t>((Wc + 7) / 8, (int64_t)sm_count() * 32));
             {
-                int blocks = (int)std::min<int64_t>((Wc + 7) / 8, (int64_t)sm_count() * 32);
-                launch_candidates(st, std::max(blocks, 1), true, cv, sv, nullptr, nullptr, d_offset.p, d_cand_atom.p);
+                // every list is filled here when every list is put in leaf
+                // order up front; otherwise only the lists a search reads:
+                // the level-0 list of each pair that can run (queued by
+                // k_demand_levels) and each list put in leaf order (filled
+                // just before it is ordered)
+                if (demand_levels < 0) {
+                    launch_candidates(st, fill_blocks, true, cv, sv, nullptr, nullptr, d_offset.p, d_cand_atom.p);
+                    launches++;
+                }
                 CUDA_TRY(dalloc(d_exact_list, (size_t)Wc, st));
                 CUDA_TRY(dalloc(d_exact_count, 1, st));
                 CUDA_TRY(dalloc(d_sorted_list, 3 * (size_t)Wc, st));
                 CUDA_TRY(dalloc(d_sorted_count, 3, st));
-                launches += 2;  // block counts, candidate fill
+                launches++;  // block counts
                 CUDA_TRY(cudaGetLastError());
             }
             TemplateView tv{T, tp->nmax, tp->d_atom_begin, tp->d_sig, tp->d_pos, tp->d_key, tp->d_param_begin,
@@ -1244,6 +1256,12 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 return cudaSuccess;
             };
             auto order_requested = [&]() -> cudaError_t {
+                if (dm.fill_state) {
+                    // the requested lists not filled yet
+                    launch_candidates(st, fill_blocks, true, cv, sv, nullptr, nullptr, d_offset.p, d_cand_atom.p,
+                                      dm.work, dm.n_work, dm.fill_state, true);
+                    launches++;
+                }
                 launch_leaf_order(st, leaf_blocks, cv, G, cnt_c, d_offset.p, d_boff.p, d_cand_atom.p, leaf_off,
                                   d_leaf_atom.p, d_leaf_xyz.p, d_blk_lo.p, d_blk_hi.p, d_sorted_list.p,
                                   d_sorted_count.p, Wc, d_exact_list.p, d_exact_count.p, d_counters.p, dm.work,
@@ -1292,12 +1310,23 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 CUDA_TRY(cudaMemsetAsync(d_leaf_used.p, 0, sizeof(unsigned long long), st));
                 dm.leaf_offset = d_leaf_off.p;
                 dm.leaf_used = d_leaf_used.p;
+                CUDA_TRY(dalloc(d_fill_state, (size_t)Wc, st));
+                CUDA_TRY(dalloc(d_fill_work, (size_t)Wc, st));
+                CUDA_TRY(dalloc(d_nfill, 1, st));
+                CUDA_TRY(cudaMemsetAsync(d_fill_state.p, 0, (size_t)Wc * sizeof(int32_t), st));
+                CUDA_TRY(cudaMemsetAsync(d_nfill.p, 0, sizeof(unsigned long long), st));
+                dm.fill_state = d_fill_state.p;
+                dm.fill_work = d_fill_work.p;
+                dm.n_fill = d_nfill.p;
                 if (n_pairs > INT32_MAX) {
                     status = fail(PJG_ERR_CAPACITY, "too many pairs in one chunk");
                     goto done;
                 }
                 launch_demand_levels(st, sm_count() * 16, tv, cd, (int32_t)n_pairs, demand_levels, P->reorder, dm);
-                launches++;
+                // the level-0 lists the pairs read in candidate order
+                launch_candidates(st, fill_blocks, true, cv, sv, nullptr, nullptr, d_offset.p, d_cand_atom.p,
+                                  dm.fill_work, dm.n_fill, nullptr, false);
+                launches += 2;
                 unsigned long long used = 0;
                 CUDA_TRY(cudaMemcpyAsync(&used, d_leaf_used.p, sizeof used, cudaMemcpyDeviceToHost, st));
                 CUDA_TRY(cudaStreamSynchronize(st));
@@ -1322,8 +1351,8 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 // templates of up to 32 atoms)
                 int levels = std::max(1, std::min(tp->nmax, 32) - 1);
                 size_t entry = sp->max_atoms > 65535 ? 8 : 4;
-                size_t need = 4096 + entry * 64 * (size_t)levels;
-                sa.warp_smem = (int)((std::max<size_t>(need, 9472) + 15) & ~size_t(15));
+                size_t need = search_state_bytes() + entry * 64 * (size_t)levels;
+                sa.warp_smem = (int)((std::max<size_t>(need, search_state_bytes() + 5376) + 15) & ~size_t(15));
             }
             sa.cut_inline = cut_inline ? 1 : 0;
             sa.rmsd_threshold = P->rmsd_threshold;
@@ -1647,6 +1676,7 @@ done:
         dfree(d_r_aidx, st); dfree(d_lstate, st); dfree(d_work, st); dfree(d_nwork, st); dfree(d_nsusp, st);
         dfree(d_susp_a, st); dfree(d_susp_b, st); dfree(d_pool_a, st); dfree(d_pool_b, st); dfree(d_pool_used, st);
         dfree(d_prof, st);
+        dfree(d_fill_state, st); dfree(d_fill_work, st); dfree(d_nfill, st);
         for (auto &b : scan_tmp) dfree(b, st);
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);

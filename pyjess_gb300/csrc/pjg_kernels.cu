@@ -190,12 +190,23 @@ __device__ __forceinline__ bool sig_match_regs(const SigView &sv, const SigRegs 
 
 // One warp per (structure, signature): the list's atoms in candidate order
 // at offset[w] (its length comes from k_candidate_counts).
-__global__ void k_candidates(ChunkView cv, SigView sv, const int64_t *offset, int32_t *cand_atom) {
+// Lists filled: every list of the chunk (work == nullptr), or the n_work
+// lists of `work`; with `claim`, a list is filled only by the warp that
+// moves its fill state from 0 to 1 (lists already filled are skipped).
+__global__ void k_candidates(ChunkView cv, SigView sv, const int64_t *offset, int32_t *cand_atom,
+                             const int64_t *work, const unsigned long long *n_work, int32_t *fill_state,
+                             int32_t claim) {
     int lane = lane_id();
     int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    int64_t total = (int64_t)cv.n_structures * sv.n_sigs;
-    for (int64_t w = warp; w < total; w += nwarps) {
+    int64_t total = work ? (int64_t)*n_work : (int64_t)cv.n_structures * sv.n_sigs;
+    for (int64_t item = warp; item < total; item += nwarps) {
+        const int64_t w = work ? work[item] : item;
+        if (claim) {
+            int taken = 0;
+            if (lane == 0) taken = atomicCAS(&fill_state[w], 0, 1) != 0;
+            if (__shfl_sync(FULL_MASK, taken, 0)) continue;
+        }
         int s = (int)(w / sv.n_sigs);
         int g = (int)(w % sv.n_sigs);
         int code = sv.code[g];
@@ -1385,6 +1396,13 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
 
 // Request list w (m entries) for kd leaf order: the first request moves it
 // from state 0 to 1, reserves its place in the leaf arrays and queues it.
+// List w is read in candidate order by some pair (its level 0): queue it
+// for the fill (once).
+__device__ __forceinline__ void request_fill(const LeafDemand &dm, int64_t w) {
+    if (dm.fill_state && dm.fill_state[w] == 0 && atomicCAS(&dm.fill_state[w], 0, 1) == 0)
+        dm.fill_work[atomicAdd(dm.n_fill, 1ull)] = w;
+}
+
 __device__ __forceinline__ void request_list(const LeafDemand &dm, int64_t w, int m) {
     if (dm.state[w] == 0 && atomicCAS(&dm.state[w], 0, 1) == 0) {
         dm.leaf_offset[w] = (int64_t)atomicAdd(dm.leaf_used, (unsigned long long)m);
@@ -1407,7 +1425,13 @@ __global__ void k_demand_levels(TemplateView tv, CandView cd, int32_t n_pairs, i
         const int s = (int)(pair / T), t = (int)(pair % T);
         const int ab = tv.atom_begin[t];
         const int n = tv.atom_begin[t + 1] - ab;
-        if (n < 2) continue;
+        if (n < 1) continue;
+        if (n == 1) {
+            // a one-atom template reads its only list, in candidate order
+            const int64_t w = (int64_t)s * G + tv.sig[ab];
+            if (lane == 0 && cd.count[w] > 0) request_fill(dm, w);
+            continue;
+        }
         if (n > 32) {
             // k_search_large: every list but the level-0 one, before the
             // search (those pairs never suspend)
@@ -1430,11 +1454,11 @@ __global__ void k_demand_levels(TemplateView tv, CandView cd, int32_t n_pairs, i
                 }
             }
             const int k0 = reorder ? best_k : 0;
-            for (int k = lane; k < n; k += 32)
-                if (k != k0) {
-                    const int64_t w = (int64_t)s * G + tv.sig[ab + k];
-                    request_list(dm, w, cd.count[w]);
-                }
+            for (int k = lane; k < n; k += 32) {
+                const int64_t w = (int64_t)s * G + tv.sig[ab + k];
+                if (k != k0) request_list(dm, w, cd.count[w]);
+                else request_fill(dm, w);
+            }
             continue;
         }
         int c = INT_MAX;
@@ -1453,6 +1477,7 @@ __global__ void k_demand_levels(TemplateView tv, CandView cd, int32_t n_pairs, i
             }
         }
         if (lane < n && rank >= 1 && rank <= max_level) request_list(dm, w, c);
+        if (lane < n && rank == 0) request_fill(dm, w);
     }
 }
 
@@ -1755,10 +1780,15 @@ struct PairState {
     // block mode: leaves inside the parent's join box awaiting the full test
     float4 qxyz[64];
     int32_t qpos[64];
+    // product mode: annulus bounds of (level j, child level) for j <= the
+    // level pthr_lev they were loaded for
+    float4 pthr[32];
     // statistics of this warp's pairs (C_PAIRS .. C_BYTES_EXP), added to the
     // global counters once, when the warp exits
     unsigned long long acc[C_BYTES_EXP + 1];
 };
+
+size_t search_state_bytes() { return (sizeof(PairState) + 15) & ~size_t(15); }
 
 template <typename PosT>
 struct __align__(4) Entry {
@@ -2120,6 +2150,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
             int root = 0;
             int lev = -1;
             int chain_lev = -1, chain_par = -1;
+            int pthr_lev = -1;  // level whose product-mode bounds st.pthr holds
             float box_lo[3], box_hi[3];
             if (saved >= 0) {
                 // resume a suspended pair from its saved state
@@ -2590,9 +2621,32 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                     }
                     const int pcnd = st.cnd[lev];
                     const int tt = pcnd + lane;
-                    const int p = ppar + tt / mc;
-                    cr = tt % mc;
+                    // (parent, candidate) of product position tt: divmod by
+                    // mc through a float reciprocal, corrected to exact
+                    const float rmc = __frcp_rn((float)mc);
+                    auto divmod = [&](int x, int &q, int &r) {
+                        q = __float2int_rz(__int2float_rn(x) * rmc);
+                        r = x - q * mc;
+                        if (r < 0) {
+                            q--;
+                            r += mc;
+                        } else if (r >= mc) {
+                            q++;
+                            r -= mc;
+                        }
+                    };
+                    int pq;
+                    divmod(tt, pq, cr);
+                    const int p = ppar + pq;
                     const bool valid = lane < batch && p < pcnt;
+                    if (pthr_lev != lev) {
+                        // annulus bounds of this level pair, for every
+                        // batch of the level
+                        __syncwarp();
+                        if (lane <= lev) st.pthr[lane] = prm[st.order[lane] * n + qn].thr;
+                        __syncwarp();
+                        pthr_lev = lev;
+                    }
                     SPROF_ADD(SP_PROD_BATCHES, 1);
                     SPROF_ADD(SP_PROD_BATCHES_L0, lev == 0);
 #if PJG_SEARCH_PROF
@@ -2622,7 +2676,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                             if (FP32) {
                                 float dx = xj.x - xc.x, dy = xj.y - xc.y, dz = xj.z - xc.z;
                                 float d2 = dx * dx + dy * dy + dz * dz;
-                                float4 th = prm[st.order[j] * n + qn].thr;
+                                float4 th = st.pthr[j];
                                 if (d2 < th.x || d2 > th.w) {
                                     pass = false;
                                     break;
@@ -2644,9 +2698,9 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         }
                     }
                     // advance the parent cursor by `batch` product positions
-                    int nt = pcnd + batch;
-                    int np2 = ppar + nt / mc;
-                    int nc2 = nt % mc;
+                    int np2, nc2;
+                    divmod(pcnd + batch, np2, nc2);
+                    np2 += ppar;
                     if (np2 >= pcnt) {
                         np2 = pcnt;
                         nc2 = 0;
@@ -3205,8 +3259,10 @@ void launch_params(cudaStream_t st, int n_templates, const int32_t *atom_begin, 
 }
 
 void launch_candidates(cudaStream_t st, int blocks, bool fill, const ChunkView &cv, const SigView &sv,
-                       int32_t *count, int32_t *scanned, const int64_t *offset, int32_t *cand_atom) {
-    if (fill) k_candidates<<<blocks, 256, 0, st>>>(cv, sv, offset, cand_atom);
+                       int32_t *count, int32_t *scanned, const int64_t *offset, int32_t *cand_atom,
+                       const int64_t *work, const unsigned long long *n_work, int32_t *fill_state, bool claim) {
+    if (fill)
+        k_candidates<<<blocks, 256, 0, st>>>(cv, sv, offset, cand_atom, work, n_work, fill_state, claim ? 1 : 0);
     else k_candidate_counts<<<blocks, 256, 0, st>>>(cv, sv, count, scanned);
 }
 

@@ -149,6 +149,11 @@ struct LeafDemand {
     unsigned long long *pool_used;     //   (bytes taken; may pass pool_cap)
     int64_t pool_cap;
     const unsigned char *pool_in;      // states of the pairs of this round
+    // lists filled on demand (nullptr: every list of the chunk is filled
+    // before the search): per list 0 not yet, 1 filled or queued
+    int32_t *fill_state;
+    int64_t *fill_work;                // level-0 lists queued for the fill
+    unsigned long long *n_fill;
 };
 
 // Complete assignments written by k_search.
@@ -191,13 +196,21 @@ struct HitSegment {
     int64_t *warn_before;              // hits of the structure before the warning
 };
 
+// bytes of k_search's per-warp pair state (shared memory, before the tiles)
+size_t search_state_bytes();
+
 // Host-side launchers (the kernels themselves live in pjg_kernels.cu).
 
 void launch_params(cudaStream_t st, int n_templates, const int32_t *atom_begin, const int32_t *param_begin,
                    const double *dist, const double *weight, double r, double s, double g, AnnulusParam *out);
 
+// fill == false: list lengths of every list of the chunk; fill == true: the
+// lists themselves, of every list (work == nullptr) or of the lists in
+// `work` (claim: only those whose fill state this launch moves from 0 to 1)
 void launch_candidates(cudaStream_t st, int blocks, bool fill, const ChunkView &cv, const SigView &sv,
-                       int32_t *count, int32_t *scanned, const int64_t *offset, int32_t *cand_atom);
+                       int32_t *count, int32_t *scanned, const int64_t *offset, int32_t *cand_atom,
+                       const int64_t *work = nullptr, const unsigned long long *n_work = nullptr,
+                       int32_t *fill_state = nullptr, bool claim = false);
 
 // exclusive scan of one tile (SCAN_TILE entries) per block
 constexpr int SCAN_TILE_THREADS = 512;
