@@ -1773,6 +1773,7 @@ struct PairState {
     float4 cxyz[32];
     float4 cthr[32];
     int32_t cpos[32];
+    int32_t cidx[32];   // index of each chain entry in its level's tile
     // join box of the chain below the parent's level, and the parent index
     // (one level up) that chain belongs to
     float pbox[6];
@@ -2356,6 +2357,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                                 const float4 cj = level_xyz(lev, (int)pe.pos);
                                 st.cxyz[lev] = cj;
                                 st.cpos[lev] = (int)pe.pos;
+                                st.cidx[lev] = ppar;
                                 const float rb = sqrtf(fmaxf(st.cthr[lev].w, 0.f)) * 1.000001f + 1e-3f;
                                 olo[0] = cj.x - rb;
                                 olo[1] = cj.y - rb;
@@ -2365,25 +2367,48 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                                 ohi[2] = cj.z + rb;
                             }
                         } else {
-                            // positions of the parent's chain, by walking the tiles
+                            // positions of the parent's chain, by walking the
+                            // tiles up from the parent.  With the same child
+                            // level as the chain held (chain_lev == lev: no
+                            // tile below lev was refilled since), the walk
+                            // stops at the first level whose entry is the held
+                            // chain's, and only the levels above it get new
+                            // points; the annulus bounds stay.
                             SPROF_ADD(SP_CHAIN_FULL, 1);
+                            const bool same_child = chain_lev == lev;
+                            int jmin = 0;
                             __syncwarp();
                             if (lane == 0) {
                                 int idx = ppar;
                                 for (int j = lev; j >= 0; j--) {
+                                    if (same_child && j < lev && idx == st.cidx[j]) {
+                                        jmin = j + 1;
+                                        break;
+                                    }
                                     E e = tiles[st.tile[j] + idx];
                                     st.cpos[j] = (int)e.pos;
+                                    st.cidx[j] = idx;
                                     idx = e.parent;
                                 }
                                 st.chain_gp = (int)pe.parent;
                             }
+                            jmin = __shfl_sync(FULL_MASK, jmin, 0);
                             __syncwarp();
                             float lo[3] = {-INFINITY, -INFINITY, -INFINITY}, hi[3] = {INFINITY, INFINITY, INFINITY};
                             if (lane <= lev) {
-                                float4 cj = level_xyz(lane, st.cpos[lane]);
-                                float4 th = prm[st.order[lane] * n + qn].thr;
-                                st.cxyz[lane] = cj;
-                                st.cthr[lane] = th;
+                                float4 cj, th;
+                                if (lane >= jmin) {
+                                    cj = level_xyz(lane, st.cpos[lane]);
+                                    st.cxyz[lane] = cj;
+                                } else {
+                                    cj = st.cxyz[lane];
+                                }
+                                if (!same_child) {
+                                    th = prm[st.order[lane] * n + qn].thr;
+                                    st.cthr[lane] = th;
+                                } else {
+                                    th = st.cthr[lane];
+                                }
                                 float rb = sqrtf(fmaxf(th.w, 0.f)) * 1.000001f + 1e-3f;
                                 lo[0] = cj.x - rb;
                                 lo[1] = cj.y - rb;
