@@ -332,6 +332,8 @@ def search_profile(args):
         "share_emit": prof["cyc_emit"] / max(1, prof["cyc_pair"]),
         "share_block_chain": prof["cyc_chain"] / max(1, prof["cyc_pair"]),
         "share_block_batch": prof["cyc_batch"] / max(1, prof["cyc_pair"]),
+        "share_control": prof["cyc_ctrl"] / max(1, prof["cyc_pair"]),
+        "share_suspend": prof["cyc_susp"] / max(1, prof["cyc_pair"]),
         "blocks_hit_per_tested": prof["blocks_hit"] / max(1, prof["blocks_tested"]),
         "inbox_per_leaf_loaded": prof["leaves_inbox"] / max(1, 32 * prof["blocks_hit"]),
         "children_per_block_test": prof["child_block"] / max(1, prof["batch_lanes"]),

@@ -2188,6 +2188,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
             while (!stop) {
                 if (over_budget()) break;
                 SPROF_ADD(SP_LOOP_ITERS, 1);
+                SPROF_T(t_it);
                 if (lev < 0) {
                     if (root >= m0) break;
                     SPROF_T(t_seed);
@@ -2227,11 +2228,13 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         }
                         __syncwarp();
                         lev = child;
+                        SPROF_CYC(SP_CYC_CTRL, t_it);
                         continue;
                     }
                     if (lane == 0) st.cnt[lev] = 0;
                     __syncwarp();
                     lev--;
+                    SPROF_CYC(SP_CYC_CTRL, t_it);
                     continue;
                 }
                 if (!((ready_mask >> child) & 1u)) {
@@ -2295,6 +2298,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         dm.suspended[atomicAdd(dm.n_suspended, 1ull)] = sp;
                     }
                     suspended = true;
+                    SPROF_CYC(SP_CYC_SUSP, t_it);
                     break;
                 }
                 const int mc = st.lvl_cnt[child];
@@ -2307,6 +2311,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                 int cr = 0;
                 int my_parent = 0;      // product mode: this lane's parent entry
                 int32_t chainpos[32];   // product mode: this lane's parent chain
+                SPROF_CYC(SP_CYC_CTRL, t_it);
                 SPROF_T(t_exp);
                 if (mc >= sa.block_min) {
                     // ---------------- block mode ----------------

@@ -79,6 +79,9 @@ enum SearchProf : int {
     SP_ROWS,             // complete rows emitted
     SP_CYC_CHAIN,        // cycles gathering a block-mode parent's chain and box
     SP_CYC_BATCH,        // cycles in block-mode full-test batches
+    SP_CYC_CTRL,         // cycles of the loop's level bookkeeping (moving up
+                         // or down a level, choosing the expansion mode)
+    SP_CYC_SUSP,         // cycles suspending pairs (state saved, lists requested)
     SP_NUM
 };
 
