@@ -107,3 +107,24 @@ def test_config3_full_size_identical_to_oracle():
           f"({summary['max_rmsd_err_outside_svd_rows']:.3g} A outside the {summary['svd_rmsd_rows']} "
           f"ill-conditioned rows checked against an SVD); {summary['svd_rotation_rows']} rotations checked "
           f"against SVD-Kabsch; {gs['fp64_rechecks']} FP64 rechecks; {len(gw[0])} warnings")
+
+
+def test_config4_full_size_structures_best_match_strided():
+    """Config 4 at its full structure sizes (2,000-5,000 residues), all 500
+    permissive templates, max_candidates 10,000, best_match=True: every
+    50th structure, searched together on the GPU and by the oracle."""
+    from oracle import oracle
+    from pyjess_gb300 import workloads
+
+    wl = workloads.config(4)
+    sub = wl.structures.subset(list(range(0, wl.structures.n_structures, 50)))
+    p = dict(wl.params)
+    assert p["max_candidates"] == 10000
+    res = gpu_query(wl.templates, sub, mode="fp32", best_match=True, **p)
+    g = res.arrays()
+    ref = oracle.query(wl.templates, sub, threads=os.cpu_count() or 1, best_match=True, **p)
+    summary = compare_full(g, ref["hits"], wl.templates, sub)
+    gw = res.warnings()
+    assert np.array_equal(gw[0], ref["warnings"][0]) and np.array_equal(gw[1], ref["warnings"][1])
+    print(f"\nconfig 4 full-size structures, best_match=True ({sub.n_structures} x {wl.templates.n_templates}): "
+          f"{summary['hits']} hits identical to the oracle; max |rmsd - oracle| = {summary['max_rmsd_err']:.3g} A")
