@@ -1738,7 +1738,7 @@ pjg_status pjg_results_superposed(const pjg_results *r, const pjg_structures *s,
     cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMallocAsync((void **)&d_out, (size_t)hs.atoms * 3 * sizeof(double), st);
     if (e == cudaSuccess) {
-        launch_superposed_atoms(st, hs.hits, hs.structure, hs.atom_offset, hs.atoms_, hs.rot, hs.centres,
+        launch_superposed_atoms(st, hs.hits, hs.atoms, hs.structure, hs.atom_offset, hs.atoms_, hs.rot, hs.centres,
                                 s->d_atom_base, s->d_xyz64, d_out);
         e = cudaGetLastError();
     }

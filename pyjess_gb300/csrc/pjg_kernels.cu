@@ -3440,9 +3440,10 @@ cudaError_t launch_search_large(cudaStream_t st, const ChunkView &cv, const Temp
 // molecule atoms x mapped by the hit's transformation T(v) R T(-c)
 // (Hit.transformation, src/pyjess/_jess.pyx:2343-2377): R x + t with
 // t = R (-c) + v.
-__global__ void k_superposed_atoms(int64_t n_hits, const int32_t *structure, const int64_t *atom_offset,
-                                   const int32_t *atoms, const double *rot, const double *centres,
-                                   const int64_t *atom_base, const double *xyz64, double *out) {
+__global__ void k_superposed_atoms(int64_t n_hits, int64_t n_atoms, const int32_t *structure,
+                                   const int64_t *atom_offset, const int32_t *atoms, const double *rot,
+                                   const double *centres, const int64_t *atom_base, const double *xyz64,
+                                   double *out) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < n_hits; h += stride) {
         const double *R = rot + 9 * h;
@@ -3455,7 +3456,10 @@ __global__ void k_superposed_atoms(int64_t n_hits, const int32_t *structure, con
             t[i] = __dadd_rn(acc, c[3 + i]);
         }
         const double *xs = xyz64 + 3 * atom_base[structure[h]];
-        for (int64_t k = atom_offset[h]; k < atom_offset[h + 1]; k++) {
+        // the hit store holds the first atom of each hit; the last hit ends
+        // at the store's atom count
+        const int64_t k1 = h + 1 < n_hits ? atom_offset[h + 1] : n_atoms;
+        for (int64_t k = atom_offset[h]; k < k1; k++) {
             const double *x = xs + 3 * (int64_t)atoms[k];
             for (int i = 0; i < 3; i++) {
                 double acc = __dmul_rn(R[3 * i], x[0]);
@@ -3467,13 +3471,13 @@ __global__ void k_superposed_atoms(int64_t n_hits, const int32_t *structure, con
     }
 }
 
-void launch_superposed_atoms(cudaStream_t st, int64_t n_hits, const int32_t *structure, const int64_t *atom_offset,
-                             const int32_t *atoms, const double *rot, const double *centres, const int64_t *atom_base,
-                             const double *xyz64, double *out) {
+void launch_superposed_atoms(cudaStream_t st, int64_t n_hits, int64_t n_atoms, const int32_t *structure,
+                             const int64_t *atom_offset, const int32_t *atoms, const double *rot,
+                             const double *centres, const int64_t *atom_base, const double *xyz64, double *out) {
     if (n_hits <= 0) return;
     const int blocks = (int)std::min<int64_t>((n_hits + 255) / 256, 152 * 32);
-    k_superposed_atoms<<<blocks, 256, 0, st>>>(n_hits, structure, atom_offset, atoms, rot, centres, atom_base, xyz64,
-                                               out);
+    k_superposed_atoms<<<blocks, 256, 0, st>>>(n_hits, n_atoms, structure, atom_offset, atoms, rot, centres,
+                                               atom_base, xyz64, out);
 }
 
 void launch_superpose(cudaStream_t st, int blocks, const ChunkView &cv, const TemplateView &tv,

@@ -264,9 +264,9 @@ cudaError_t launch_search_large(cudaStream_t st, const ChunkView &cv, const Temp
                                 const int32_t *lstate);
 
 // every hit atom in its template's frame (out[3 * k + d] for hit atom k)
-void launch_superposed_atoms(cudaStream_t st, int64_t n_hits, const int32_t *structure, const int64_t *atom_offset,
-                             const int32_t *atoms, const double *rot, const double *centres, const int64_t *atom_base,
-                             const double *xyz64, double *out);
+void launch_superposed_atoms(cudaStream_t st, int64_t n_hits, int64_t n_atoms, const int32_t *structure,
+                             const int64_t *atom_offset, const int32_t *atoms, const double *rot,
+                             const double *centres, const int64_t *atom_base, const double *xyz64, double *out);
 
 void launch_superpose(cudaStream_t st, int blocks, const ChunkView &cv, const TemplateView &tv,
                       const CompleteRows &in, const RowResults &out);
