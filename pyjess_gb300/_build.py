@@ -31,9 +31,10 @@ SOURCES = ["pjg_kernels.cu", "pjg_api.cu", "pjg_io.cpp"]
 # library variants: "" the product library; "prof" adds the search profile
 # (event counts and section cycles of k_search, written per query to the
 # file named by PJG_PROF_OUT) and is never the timed build; "blk8"/"blk16"
-# cull by blocks of 8/16 leaves instead of 32 (measured against each other)
+# cull by blocks of 8/16 leaves instead of 32, "w10" runs the search with
+# 10 warps a block (measured against each other)
 VARIANTS = {"": [], "prof": ["-DPJG_SEARCH_PROF=1"], "blk8": ["-DPJG_CULL_BLK=8"], "blk16": ["-DPJG_CULL_BLK=16"],
-            "blk8prof": ["-DPJG_CULL_BLK=8", "-DPJG_SEARCH_PROF=1"]}
+            "blk8prof": ["-DPJG_CULL_BLK=8", "-DPJG_SEARCH_PROF=1"], "w10": ["-DPJG_SEARCH_WARPS=10"]}
 
 
 def lib_path(variant: str = "") -> pathlib.Path:

@@ -1911,7 +1911,10 @@ __device__ __noinline__ bool decide_fp64(unsigned exact_mask, int lev, const int
     } while (0)
 #endif
 
-template <typename PosT, bool FP32>
+// CUT: the max_candidates cut applied inline (non-best mode with
+// max_candidates); the other queries get a kernel without that code (its
+// FP64 superposition in the loop costs registers everywhere).
+template <typename PosT, bool FP32, bool CUT>
 __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
     k_search(ChunkView cv, TemplateView tv, CandView cd, SearchArgs sa, int32_t *pair_counter,
              const int32_t *scanned, CompleteRows out, unsigned long long *counters, LeafDemand dm) {
@@ -2084,7 +2087,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                 for (int j = 0; j < n - 1; j++) at[st.order[j]] = level_atom(j, pos[j]);
                 at[st.order[n - 1]] = level_atom(n - 1, lastpos);
             }
-            if (sa.cut_inline) {
+            if (CUT) {
                 // Query.__next__'s max_candidates cut, applied while
                 // searching: the candidate whose distance from the last hit
                 // (or the template start) reaches M+1 ends the template's
@@ -3385,24 +3388,33 @@ void launch_block_counts(cudaStream_t st, int64_t n, const int32_t *count, int32
     if (n > 0) k_block_counts<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, count, nblk);
 }
 
-template <typename RowT, bool FP32>
+template <typename RowT, bool FP32, bool CUT>
 static cudaError_t search_variant(cudaStream_t st, int grid, const ChunkView &cv, const TemplateView &tv,
                                   const CandView &cd, const SearchArgs &sa, int32_t *pair_counter,
                                   const int32_t *scanned, const CompleteRows &out, unsigned long long *counters,
                                   const LeafDemand &dm) {
     size_t smem = (size_t)sa.warp_smem * SEARCH_WARPS;
-    cudaError_t e = cudaFuncSetAttribute(k_search<RowT, FP32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto kern = k_search<RowT, FP32, CUT>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     // persistent grid: as many blocks as can be resident at once
     int per_sm = 0, dev = 0, sms = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<RowT, FP32>, SEARCH_WARPS * 32, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, SEARCH_WARPS * 32, smem);
     if (e != cudaSuccess) return e;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (per_sm > 0 && sms > 0) grid = per_sm * sms;
-    k_search<RowT, FP32><<<grid, SEARCH_WARPS * 32, smem, st>>>(cv, tv, cd, sa, pair_counter, scanned, out, counters,
-                                                                 dm);
+    kern<<<grid, SEARCH_WARPS * 32, smem, st>>>(cv, tv, cd, sa, pair_counter, scanned, out, counters, dm);
     return cudaGetLastError();
+}
+
+template <typename RowT, bool FP32>
+static cudaError_t search_cut(cudaStream_t st, int grid, const ChunkView &cv, const TemplateView &tv,
+                              const CandView &cd, const SearchArgs &sa, int32_t *pair_counter, const int32_t *scanned,
+                              const CompleteRows &out, unsigned long long *counters, const LeafDemand &dm) {
+    return sa.cut_inline
+               ? search_variant<RowT, FP32, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm)
+               : search_variant<RowT, FP32, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm);
 }
 
 cudaError_t launch_search(cudaStream_t st, int grid, bool wide, bool fp32, const ChunkView &cv,
@@ -3410,11 +3422,10 @@ cudaError_t launch_search(cudaStream_t st, int grid, bool wide, bool fp32, const
                           const int32_t *scanned, const CompleteRows &out, unsigned long long *counters,
                           const LeafDemand &dm) {
     if (wide)
-        return fp32 ? search_variant<uint32_t, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm)
-                    : search_variant<uint32_t, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters,
-                                                      dm);
-    return fp32 ? search_variant<uint16_t, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm)
-                : search_variant<uint16_t, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm);
+        return fp32 ? search_cut<uint32_t, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm)
+                    : search_cut<uint32_t, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm);
+    return fp32 ? search_cut<uint16_t, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm)
+                : search_cut<uint16_t, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm);
 }
 
 cudaError_t launch_search_large(cudaStream_t st, const ChunkView &cv, const TemplateView &tv, const CandView &cd,
