@@ -2752,9 +2752,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                 SPROF_ADD(SP_CHILD_PROD, __popc(m));
                 if (last) {
                     if (block_mode) {
-                        int32_t pos[32];
-                        for (int j = 0; j <= lev; j++) pos[j] = st.cpos[j];
-                        emit(pass, pos, cr);
+                        emit(pass, st.cpos, cr);
                     } else {
                         emit(pass, chainpos, cr);
                     }
