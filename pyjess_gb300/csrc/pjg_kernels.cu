@@ -499,6 +499,10 @@ struct LeafWarp {
     uint16_t ord[2][LEAF_FAST_MAX];  // candidate index at each position
     uint16_t seg_lo[LEAF_FAST_MAX];  // node (segment) of each position
     uint16_t seg_n[LEAF_FAST_MAX];
+    // level 0 by a bitmap over the structure's unique x ranks (a window of
+    // 32 * LEAF_SORT_WORDS ranks at a time)
+    uint32_t bits[LEAF_SORT_WORDS];
+    uint16_t wpre[LEAF_SORT_WORDS];  // elements placed before each word
 };
 
 // Bounding boxes of the blocks of CULL_BLK consecutive leaves of a list
@@ -589,18 +593,66 @@ __global__ void __launch_bounds__(LEAF_WARPS * 32)
             for (int d = 0; d < levels; d++) {
                 const uint16_t *A = L.ord[src];
                 uint16_t *B = L.ord[src ^ 1];
-                for (int p = lane; p < m; p += 32) {
-                    const int lo = L.seg_lo[p], n = L.seg_n[p];
-                    const int e = A[p];
-                    if (n <= 1) {
-                        B[p] = (uint16_t)e;
-                        continue;
+                // level 0 of a longer list: the whole list in x order is the
+                // structure's x order restricted to the list, read from a
+                // bitmap over the unique x ranks (what the counting below
+                // computes, in O(atoms / 32 + m / 32) instead of O(m^2 / 32))
+                bool sorted0 = false;
+                if (d == 0 && m >= LEAF_SORT_FROM) {
+                    const int natoms = cv.atom_count[w / n_sigs];
+                    constexpr int WB = 32 * LEAF_SORT_WORDS;
+                    int placed = 0;
+                    for (int wb = 0; wb < natoms; wb += WB) {
+                        const int nwords = min(LEAF_SORT_WORDS, (natoms - wb + 31) >> 5);
+                        for (int q = lane; q < nwords; q += 32) L.bits[q] = 0u;
+                        __syncwarp();
+                        for (int e = lane; e < m; e += 32) {
+                            const uint32_t u = L.ur[0][e] - (uint32_t)wb;
+                            if (u < (uint32_t)WB) atomicOr(&L.bits[u >> 5], 1u << (u & 31));
+                        }
+                        __syncwarp();
+                        int carry = placed;
+                        for (int w0 = 0; w0 < nwords; w0 += 32) {
+                            const int wd = w0 + lane;
+                            const int c = wd < nwords ? __popc(L.bits[wd]) : 0;
+                            int incl = c;
+                            for (int off = 1; off < 32; off <<= 1) {
+                                const int y = __shfl_up_sync(FULL_MASK, incl, off);
+                                if (lane >= off) incl += y;
+                            }
+                            if (wd < nwords) L.wpre[wd] = (uint16_t)(carry + incl - c);
+                            carry += __shfl_sync(FULL_MASK, incl, 31);
+                        }
+                        __syncwarp();
+                        for (int e = lane; e < m; e += 32) {
+                            const uint32_t u = L.ur[0][e] - (uint32_t)wb;
+                            if (u < (uint32_t)WB) {
+                                const uint32_t word = L.bits[u >> 5];
+                                const int pos = L.wpre[u >> 5] + __popc(word & ((1u << (u & 31)) - 1u));
+                                if (pos < m) B[pos] = (uint16_t)e;
+                            }
+                        }
+                        __syncwarp();
+                        placed = carry;
                     }
-                    const uint32_t x = L.cur[p];
-                    int before = 0;
+                    // every element placed once (a repeated atom would not
+                    // be: count then)
+                    sorted0 = placed == m;
+                }
+                if (!sorted0) {
+                    for (int p = lane; p < m; p += 32) {
+                        const int lo = L.seg_lo[p], n = L.seg_n[p];
+                        const int e = A[p];
+                        if (n <= 1) {
+                            B[p] = (uint16_t)e;
+                            continue;
+                        }
+                        const uint32_t x = L.cur[p];
+                        int before = 0;
 #pragma unroll 8
-                    for (int q = lo; q < lo + n; q++) before += L.cur[q] < x;
-                    B[lo + before] = (uint16_t)e;
+                        for (int q = lo; q < lo + n; q++) before += L.cur[q] < x;
+                        B[lo + before] = (uint16_t)e;
+                    }
                 }
                 __syncwarp();
                 // median-boundary ties, next axis keys, child nodes
