@@ -1527,8 +1527,12 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 // complete row: when the chunk's rows need more than 70% of
                 // the memory they may use, or the row buffers could not hold
                 // them, the chunk is redone on half its structures
-                if (Sc > 1 && (split || rows > row_budget())) {
-                    chunk_cap = std::max(1, Sc / 2);
+                const int64_t budget_now = row_budget();
+                if (Sc > 1 && (split || rows > budget_now)) {
+                    // at most half the structures, fewer when the rows seen
+                    // say so (rows scale with the structures of a chunk)
+                    const double fit = 0.8 * (double)Sc * (double)budget_now / (double)std::max<int64_t>(rows, 1);
+                    chunk_cap = std::max(1, std::min(Sc / 2, (int)fit));
                     chunks--;
                     row_splits++;
                     search_rounds = search_rounds0;

@@ -1833,9 +1833,11 @@ struct PairState {
     // block mode: leaves inside the parent's join box awaiting the full test
     float4 qxyz[64];
     int32_t qpos[64];
+#if PJG_PTHR_CACHE
     // product mode: annulus bounds of (level j, child level) for j <= the
     // level pthr_lev they were loaded for
     float4 pthr[32];
+#endif
     // statistics of this warp's pairs (C_PAIRS .. C_BYTES_EXP), added to the
     // global counters once, when the warp exits
     unsigned long long acc[C_BYTES_EXP + 1];
@@ -2206,7 +2208,9 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
             int root = 0;
             int lev = -1;
             int chain_lev = -1, chain_par = -1;
+#if PJG_PTHR_CACHE
             int pthr_lev = -1;  // level whose product-mode bounds st.pthr holds
+#endif
             float box_lo[3], box_hi[3];
             if (saved >= 0) {
                 // resume a suspended pair from its saved state
@@ -2441,7 +2445,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                             if (lane == 0) {
                                 int idx = ppar;
                                 for (int j = lev; j >= 0; j--) {
-                                    if (same_child && j < lev && idx == st.cidx[j]) {
+                                    if (PJG_CHAIN_INCR && same_child && j < lev && idx == st.cidx[j]) {
                                         jmin = j + 1;
                                         break;
                                     }
@@ -2463,7 +2467,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                                 } else {
                                     cj = st.cxyz[lane];
                                 }
-                                if (!same_child) {
+                                if (!PJG_CHAIN_INCR || !same_child) {
                                     th = prm[st.order[lane] * n + qn].thr;
                                     st.cthr[lane] = th;
                                 } else {
@@ -2708,6 +2712,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                     const int tt = pcnd + lane;
                     // (parent, candidate) of product position tt: divmod by
                     // mc through a float reciprocal, corrected to exact
+#if PJG_PROD_DIVMOD
                     const float rmc = __frcp_rn((float)mc);
                     auto divmod = [&](int x, int &q, int &r) {
                         q = __float2int_rz(__int2float_rn(x) * rmc);
@@ -2720,10 +2725,17 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                             r -= mc;
                         }
                     };
+#else
+                    auto divmod = [&](int x, int &q, int &r) {
+                        q = x / mc;
+                        r = x % mc;
+                    };
+#endif
                     int pq;
                     divmod(tt, pq, cr);
                     const int p = ppar + pq;
                     const bool valid = lane < batch && p < pcnt;
+#if PJG_PTHR_CACHE
                     if (pthr_lev != lev) {
                         // annulus bounds of this level pair, for every
                         // batch of the level
@@ -2732,6 +2744,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         __syncwarp();
                         pthr_lev = lev;
                     }
+#endif
                     SPROF_ADD(SP_PROD_BATCHES, 1);
                     SPROF_ADD(SP_PROD_BATCHES_L0, lev == 0);
 #if PJG_SEARCH_PROF
@@ -2761,7 +2774,11 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                             if (FP32) {
                                 float dx = xj.x - xc.x, dy = xj.y - xc.y, dz = xj.z - xc.z;
                                 float d2 = dx * dx + dy * dy + dz * dz;
+#if PJG_PTHR_CACHE
                                 float4 th = st.pthr[j];
+#else
+                                float4 th = prm[st.order[j] * n + qn].thr;
+#endif
                                 if (d2 < th.x || d2 > th.w) {
                                     pass = false;
                                     break;
