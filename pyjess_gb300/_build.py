@@ -34,8 +34,7 @@ SOURCES = ["pjg_kernels.cu", "pjg_api.cu", "pjg_io.cpp"]
 # cull by blocks of 8/16 leaves instead of 32, "w10" runs the search with
 # 10 warps a block (measured against each other)
 VARIANTS = {"": [], "prof": ["-DPJG_SEARCH_PROF=1"], "blk8": ["-DPJG_CULL_BLK=8"], "blk16": ["-DPJG_CULL_BLK=16"],
-            "blk8prof": ["-DPJG_CULL_BLK=8", "-DPJG_SEARCH_PROF=1"], "w10": ["-DPJG_SEARCH_WARPS=10"],
-            "divmod": ["-DPJG_PROD_DIVMOD=1"], "pthr": ["-DPJG_PTHR_CACHE=1"], "incr": ["-DPJG_CHAIN_INCR=1"]}
+            "blk8prof": ["-DPJG_CULL_BLK=8", "-DPJG_SEARCH_PROF=1"], "w10": ["-DPJG_SEARCH_WARPS=10"]}
 
 
 def lib_path(variant: str = "") -> pathlib.Path:

@@ -1825,7 +1825,6 @@ struct PairState {
     float4 cxyz[32];
     float4 cthr[32];
     int32_t cpos[32];
-    int32_t cidx[32];   // index of each chain entry in its level's tile
     // join box of the chain below the parent's level, and the parent index
     // (one level up) that chain belongs to
     float pbox[6];
@@ -1833,11 +1832,6 @@ struct PairState {
     // block mode: leaves inside the parent's join box awaiting the full test
     float4 qxyz[64];
     int32_t qpos[64];
-#if PJG_PTHR_CACHE
-    // product mode: annulus bounds of (level j, child level) for j <= the
-    // level pthr_lev they were loaded for
-    float4 pthr[32];
-#endif
     // statistics of this warp's pairs (C_PAIRS .. C_BYTES_EXP), added to the
     // global counters once, when the warp exits
     unsigned long long acc[C_BYTES_EXP + 1];
@@ -2208,9 +2202,6 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
             int root = 0;
             int lev = -1;
             int chain_lev = -1, chain_par = -1;
-#if PJG_PTHR_CACHE
-            int pthr_lev = -1;  // level whose product-mode bounds st.pthr holds
-#endif
             float box_lo[3], box_hi[3];
             if (saved >= 0) {
                 // resume a suspended pair from its saved state
@@ -2421,7 +2412,6 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                                 const float4 cj = level_xyz(lev, (int)pe.pos);
                                 st.cxyz[lev] = cj;
                                 st.cpos[lev] = (int)pe.pos;
-                                st.cidx[lev] = ppar;
                                 const float rb = sqrtf(fmaxf(st.cthr[lev].w, 0.f)) * 1.000001f + 1e-3f;
                                 olo[0] = cj.x - rb;
                                 olo[1] = cj.y - rb;
@@ -2431,48 +2421,25 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                                 ohi[2] = cj.z + rb;
                             }
                         } else {
-                            // positions of the parent's chain, by walking the
-                            // tiles up from the parent.  With the same child
-                            // level as the chain held (chain_lev == lev: no
-                            // tile below lev was refilled since), the walk
-                            // stops at the first level whose entry is the held
-                            // chain's, and only the levels above it get new
-                            // points; the annulus bounds stay.
+                            // positions of the parent's chain, by walking the tiles
                             SPROF_ADD(SP_CHAIN_FULL, 1);
-                            const bool same_child = chain_lev == lev;
-                            int jmin = 0;
                             __syncwarp();
                             if (lane == 0) {
                                 int idx = ppar;
                                 for (int j = lev; j >= 0; j--) {
-                                    if (PJG_CHAIN_INCR && same_child && j < lev && idx == st.cidx[j]) {
-                                        jmin = j + 1;
-                                        break;
-                                    }
                                     E e = tiles[st.tile[j] + idx];
                                     st.cpos[j] = (int)e.pos;
-                                    st.cidx[j] = idx;
                                     idx = e.parent;
                                 }
                                 st.chain_gp = (int)pe.parent;
                             }
-                            jmin = __shfl_sync(FULL_MASK, jmin, 0);
                             __syncwarp();
                             float lo[3] = {-INFINITY, -INFINITY, -INFINITY}, hi[3] = {INFINITY, INFINITY, INFINITY};
                             if (lane <= lev) {
-                                float4 cj, th;
-                                if (lane >= jmin) {
-                                    cj = level_xyz(lane, st.cpos[lane]);
-                                    st.cxyz[lane] = cj;
-                                } else {
-                                    cj = st.cxyz[lane];
-                                }
-                                if (!PJG_CHAIN_INCR || !same_child) {
-                                    th = prm[st.order[lane] * n + qn].thr;
-                                    st.cthr[lane] = th;
-                                } else {
-                                    th = st.cthr[lane];
-                                }
+                                float4 cj = level_xyz(lane, st.cpos[lane]);
+                                float4 th = prm[st.order[lane] * n + qn].thr;
+                                st.cxyz[lane] = cj;
+                                st.cthr[lane] = th;
                                 float rb = sqrtf(fmaxf(th.w, 0.f)) * 1.000001f + 1e-3f;
                                 lo[0] = cj.x - rb;
                                 lo[1] = cj.y - rb;
@@ -2712,7 +2679,6 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                     const int tt = pcnd + lane;
                     // (parent, candidate) of product position tt: divmod by
                     // mc through a float reciprocal, corrected to exact
-#if PJG_PROD_DIVMOD
                     const float rmc = __frcp_rn((float)mc);
                     auto divmod = [&](int x, int &q, int &r) {
                         q = __float2int_rz(__int2float_rn(x) * rmc);
@@ -2725,26 +2691,10 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                             r -= mc;
                         }
                     };
-#else
-                    auto divmod = [&](int x, int &q, int &r) {
-                        q = x / mc;
-                        r = x % mc;
-                    };
-#endif
                     int pq;
                     divmod(tt, pq, cr);
                     const int p = ppar + pq;
                     const bool valid = lane < batch && p < pcnt;
-#if PJG_PTHR_CACHE
-                    if (pthr_lev != lev) {
-                        // annulus bounds of this level pair, for every
-                        // batch of the level
-                        __syncwarp();
-                        if (lane <= lev) st.pthr[lane] = prm[st.order[lane] * n + qn].thr;
-                        __syncwarp();
-                        pthr_lev = lev;
-                    }
-#endif
                     SPROF_ADD(SP_PROD_BATCHES, 1);
                     SPROF_ADD(SP_PROD_BATCHES_L0, lev == 0);
 #if PJG_SEARCH_PROF
@@ -2774,11 +2724,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                             if (FP32) {
                                 float dx = xj.x - xc.x, dy = xj.y - xc.y, dz = xj.z - xc.z;
                                 float d2 = dx * dx + dy * dy + dz * dz;
-#if PJG_PTHR_CACHE
-                                float4 th = st.pthr[j];
-#else
                                 float4 th = prm[st.order[j] * n + qn].thr;
-#endif
                                 if (d2 < th.x || d2 > th.w) {
                                     pass = false;
                                     break;

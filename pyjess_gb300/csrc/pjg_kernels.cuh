@@ -30,19 +30,6 @@ constexpr int SEARCH_WARPS = PJG_SEARCH_WARPS;  // warps per block of k_search
 #endif
 constexpr int CULL_BLK = PJG_CULL_BLK;
 static_assert(CULL_BLK == 8 || CULL_BLK == 16 || CULL_BLK == 32, "culling block of 8, 16 or 32 leaves");
-// k_search variants measured against each other (0 = off): the product
-// mode's (parent, candidate) divmod by a float reciprocal; its annulus bounds
-// cached in shared memory per level; the block mode's chain walk stopping at
-// the held chain
-#ifndef PJG_PROD_DIVMOD
-#define PJG_PROD_DIVMOD 0
-#endif
-#ifndef PJG_PTHR_CACHE
-#define PJG_PTHR_CACHE 0
-#endif
-#ifndef PJG_CHAIN_INCR
-#define PJG_CHAIN_INCR 0
-#endif
 // templates of more than 32 atoms: k_search_large, warps per block and
 // per-warp shared-memory bytes for templates of up to nmax atoms
 constexpr int LARGE_WARPS = 2;
