@@ -542,6 +542,50 @@ __device__ void write_leaves(const uint16_t *order, int m, int64_t lo, const int
     write_boxes(m, lo, leaf_xyz, bo, blk_lo, blk_hi);
 }
 
+// The elements A[lo .. lo + n) in the order of their unique ranks on axis
+// `ax`, into B[lo .. lo + n): a bitmap over the structure's ranks (windows of
+// 32 * LEAF_SORT_WORDS), each element's place the set bits before it.
+// False when an element was not placed once (a repeated atom).
+__device__ bool sort_segment(LeafWarp &L, const uint16_t *A, uint16_t *B, int lo, int n, int ax, int natoms) {
+    const int lane = lane_id();
+    constexpr int WB = 32 * LEAF_SORT_WORDS;
+    int placed = 0;
+    for (int wb = 0; wb < natoms; wb += WB) {
+        const int nwords = min(LEAF_SORT_WORDS, (natoms - wb + 31) >> 5);
+        for (int q = lane; q < nwords; q += 32) L.bits[q] = 0u;
+        __syncwarp();
+        for (int p = lo + lane; p < lo + n; p += 32) {
+            const uint32_t u = L.ur[ax][A[p]] - (uint32_t)wb;
+            if (u < (uint32_t)WB) atomicOr(&L.bits[u >> 5], 1u << (u & 31));
+        }
+        __syncwarp();
+        int carry = placed;
+        for (int w0 = 0; w0 < nwords; w0 += 32) {
+            const int wd = w0 + lane;
+            const int c = wd < nwords ? __popc(L.bits[wd]) : 0;
+            int incl = c;
+            for (int off = 1; off < 32; off <<= 1) {
+                const int y = __shfl_up_sync(FULL_MASK, incl, off);
+                if (lane >= off) incl += y;
+            }
+            if (wd < nwords) L.wpre[wd] = (uint16_t)(carry + incl - c);
+            carry += __shfl_sync(FULL_MASK, incl, 31);
+        }
+        __syncwarp();
+        for (int p = lo + lane; p < lo + n; p += 32) {
+            const uint32_t u = L.ur[ax][A[p]] - (uint32_t)wb;
+            if (u < (uint32_t)WB) {
+                const uint32_t word = L.bits[u >> 5];
+                const int pos = L.wpre[u >> 5] + __popc(word & ((1u << (u & 31)) - 1u));
+                if (pos < n) B[lo + pos] = A[p];
+            }
+        }
+        __syncwarp();
+        placed = carry;
+    }
+    return placed == n;
+}
+
 // Short lists (at most rank_max entries) without a tie: rank method (each
 // entry's rank in its node by counting smaller keys), one warp per list.  Longer or tied lists go to k_leaf_sorted's worklists (up
 // to LEAF_SORTED_MAX entries), the rest to k_leaf_exact's.
@@ -593,51 +637,25 @@ __global__ void __launch_bounds__(LEAF_WARPS * 32)
             for (int d = 0; d < levels; d++) {
                 const uint16_t *A = L.ord[src];
                 uint16_t *B = L.ord[src ^ 1];
-                // level 0 of a longer list: the whole list in x order is the
-                // structure's x order restricted to the list, read from a
-                // bitmap over the unique x ranks (what the counting below
-                // computes, in O(atoms / 32 + m / 32) instead of O(m^2 / 32))
+                // the first levels of a longer list: each node in axis
+                // order is the structure's axis order restricted to the node,
+                // read from a bitmap over the unique axis ranks (what the
+                // counting below computes, in O(atoms / 32 + m / 32) a node
+                // instead of O(m n / 32))
                 bool sorted0 = false;
-                if (d == 0 && m >= LEAF_SORT_FROM) {
+                if ((d == 0 && m >= LEAF_SORT_FROM) || (d == 1 && m >= LEAF_SORT1_FROM)) {
                     const int natoms = cv.atom_count[w / n_sigs];
-                    constexpr int WB = 32 * LEAF_SORT_WORDS;
-                    int placed = 0;
-                    for (int wb = 0; wb < natoms; wb += WB) {
-                        const int nwords = min(LEAF_SORT_WORDS, (natoms - wb + 31) >> 5);
-                        for (int q = lane; q < nwords; q += 32) L.bits[q] = 0u;
-                        __syncwarp();
-                        for (int e = lane; e < m; e += 32) {
-                            const uint32_t u = L.ur[0][e] - (uint32_t)wb;
-                            if (u < (uint32_t)WB) atomicOr(&L.bits[u >> 5], 1u << (u & 31));
+                    sorted0 = true;
+                    for (int lo = 0; lo < m;) {
+                        const int n = L.seg_n[lo];
+                        if (n <= 1) {
+                            if (lane == 0) B[lo] = A[lo];
+                        } else {
+                            sorted0 = sort_segment(L, A, B, lo, n, d % 3, natoms) && sorted0;
                         }
-                        __syncwarp();
-                        int carry = placed;
-                        for (int w0 = 0; w0 < nwords; w0 += 32) {
-                            const int wd = w0 + lane;
-                            const int c = wd < nwords ? __popc(L.bits[wd]) : 0;
-                            int incl = c;
-                            for (int off = 1; off < 32; off <<= 1) {
-                                const int y = __shfl_up_sync(FULL_MASK, incl, off);
-                                if (lane >= off) incl += y;
-                            }
-                            if (wd < nwords) L.wpre[wd] = (uint16_t)(carry + incl - c);
-                            carry += __shfl_sync(FULL_MASK, incl, 31);
-                        }
-                        __syncwarp();
-                        for (int e = lane; e < m; e += 32) {
-                            const uint32_t u = L.ur[0][e] - (uint32_t)wb;
-                            if (u < (uint32_t)WB) {
-                                const uint32_t word = L.bits[u >> 5];
-                                const int pos = L.wpre[u >> 5] + __popc(word & ((1u << (u & 31)) - 1u));
-                                if (pos < m) B[pos] = (uint16_t)e;
-                            }
-                        }
-                        __syncwarp();
-                        placed = carry;
+                        lo += n < 1 ? 1 : n;
                     }
-                    // every element placed once (a repeated atom would not
-                    // be: count then)
-                    sorted0 = placed == m;
+                    __syncwarp();
                 }
                 if (!sorted0) {
                     for (int p = lane; p < m; p += 32) {
