@@ -1212,8 +1212,8 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 }
                 CUDA_TRY(dalloc(d_exact_list, (size_t)Wc, st));
                 CUDA_TRY(dalloc(d_exact_count, 1, st));
-                CUDA_TRY(dalloc(d_sorted_list, 3 * (size_t)Wc, st));
-                CUDA_TRY(dalloc(d_sorted_count, 3, st));
+                CUDA_TRY(dalloc(d_sorted_list, 4 * (size_t)Wc, st));
+                CUDA_TRY(dalloc(d_sorted_count, 4, st));
                 launches++;  // block counts
                 CUDA_TRY(cudaGetLastError());
             }
@@ -1266,7 +1266,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                                   d_leaf_atom.p, d_leaf_xyz.p, d_blk_lo.p, d_blk_hi.p, d_sorted_list.p,
                                   d_sorted_count.p, Wc, d_exact_list.p, d_exact_count.p, d_counters.p, dm.work,
                                   dm.n_work, tune.leaf_rank_max);
-                launches += 6;
+                launches += 7;
                 if (dm.state) {
                     launch_mark_ordered(st, sm_count() * 4, dm);
                     launches++;

@@ -490,15 +490,16 @@ __device__ __noinline__ void kd_exact(int32_t *perm, int m, const int32_t *ca, c
     }
 }
 
+template <int CAP>
 struct LeafWarp {
-    uint32_t ur[3][LEAF_FAST_MAX];   // unique axis ranks by candidate index
-    uint16_t lr[3][LEAF_FAST_MAX];   // strict-lower axis ranks (low 16 bits: equal
+    uint32_t ur[3][CAP];   // unique axis ranks by candidate index
+    uint16_t lr[3][CAP];   // strict-lower axis ranks (low 16 bits: equal
                                      // ranks stay equal, a rare false tie only
                                      // sends the list to k_leaf_sorted)
-    uint32_t cur[LEAF_FAST_MAX];     // current axis unique rank in position order
-    uint16_t ord[2][LEAF_FAST_MAX];  // candidate index at each position
-    uint16_t seg_lo[LEAF_FAST_MAX];  // node (segment) of each position
-    uint16_t seg_n[LEAF_FAST_MAX];
+    uint32_t cur[CAP];     // current axis unique rank in position order
+    uint16_t ord[2][CAP];  // candidate index at each position
+    uint16_t seg_lo[CAP];  // node (segment) of each position
+    uint16_t seg_n[CAP];
     // level 0 by a bitmap over the structure's unique x ranks (a window of
     // 32 * LEAF_SORT_WORDS ranks at a time)
     uint32_t bits[LEAF_SORT_WORDS];
@@ -546,7 +547,8 @@ __device__ void write_leaves(const uint16_t *order, int m, int64_t lo, const int
 // `ax`, into B[lo .. lo + n): a bitmap over the structure's ranks (windows of
 // 32 * LEAF_SORT_WORDS), each element's place the set bits before it.
 // False when an element was not placed once (a repeated atom).
-__device__ bool sort_segment(LeafWarp &L, const uint16_t *A, uint16_t *B, int lo, int n, int ax, int natoms) {
+template <int CAP>
+__device__ bool sort_segment(LeafWarp<CAP> &L, const uint16_t *A, uint16_t *B, int lo, int n, int ax, int natoms) {
     const int lane = lane_id();
     constexpr int WB = 32 * LEAF_SORT_WORDS;
     int placed = 0;
@@ -586,19 +588,25 @@ __device__ bool sort_segment(LeafWarp &L, const uint16_t *A, uint16_t *B, int lo
     return placed == n;
 }
 
-// Short lists (at most rank_max entries) without a tie: rank method (each
-// entry's rank in its node by counting smaller keys), one warp per list.  Longer or tied lists go to k_leaf_sorted's worklists (up
-// to LEAF_SORTED_MAX entries), the rest to k_leaf_exact's.
-__global__ void __launch_bounds__(LEAF_WARPS * 32)
+// Lists (at most rank_max <= CAP entries) without a tie: rank method, one
+// warp per list -- the first levels by bitmap sorts of the nodes, the rest by
+// counting each entry's smaller keys in its node.  Longer lists up to
+// mid_max go to `mid_list` (the instance with larger buffers), longer or
+// tied ones to k_leaf_sorted's worklists (up to LEAF_SORTED_MAX entries),
+// the rest to k_leaf_exact's.  count_lists: this instance counts the lists it
+// takes (the first one; the second sees lists the first already counted).
+template <int CAP, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
     k_leaf_order(ChunkView cv, int32_t n_sigs, const int32_t *count, const int64_t *offset,
                  const int64_t *blk_offset, const int32_t *cand_atom, const int64_t *leaf_offset,
                  int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi, int64_t *sorted_list,
                  unsigned long long *sorted_count, int64_t list_cap, int64_t *exact_list,
                  unsigned long long *exact_count, unsigned long long *counters, int rank_max,
-                 const int64_t *work, const unsigned long long *n_work) {
-    __shared__ LeafWarp sh[LEAF_WARPS];
+                 const int64_t *work, const unsigned long long *n_work, int64_t *mid_list,
+                 unsigned long long *mid_count, int mid_max, int count_lists) {
+    __shared__ LeafWarp<CAP> sh[WARPS];
     const int lane = lane_id();
-    LeafWarp &L = sh[threadIdx.x >> 5];
+    LeafWarp<CAP> &L = sh[threadIdx.x >> 5];
     int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     // the requested lists, or every list of the chunk
@@ -608,10 +616,17 @@ __global__ void __launch_bounds__(LEAF_WARPS * 32)
         const int64_t w = work ? work[item] : item;
         const int m = count[w];
         if (m <= 0) continue;
-        n_lists++;
-        n_entries += (unsigned long long)m;
+        if (count_lists) {
+            n_lists++;
+            n_entries += (unsigned long long)m;
+        }
         const int64_t o = offset[w];
         bool tie = m > rank_max;
+        if (tie && mid_list && m <= mid_max) {
+            if (lane == 0) mid_list[atomicAdd(mid_count, 1ull)] = w;
+            __syncwarp();
+            continue;
+        }
         int src = 0;
         if (!tie) {
             // keys: the atoms' unique axis ranks (an exact order of the FP64
@@ -643,7 +658,7 @@ __global__ void __launch_bounds__(LEAF_WARPS * 32)
                 // counting below computes, in O(atoms / 32 + m / 32) a node
                 // instead of O(m n / 32))
                 bool sorted0 = false;
-                if ((d == 0 && m >= LEAF_SORT_FROM) || (d == 1 && m >= LEAF_SORT1_FROM)) {
+                if ((m >> d) >= LEAF_SORT_FROM) {
                     const int natoms = cv.atom_count[w / n_sigs];
                     sorted0 = true;
                     for (int lo = 0; lo < m;) {
@@ -3350,18 +3365,24 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
                        int64_t *sorted_list, unsigned long long *sorted_count, int64_t list_cap,
                        int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters,
                        const int64_t *work, const unsigned long long *n_work, int rank_max) {
-    cudaMemsetAsync(sorted_count, 0, 3 * sizeof(unsigned long long), st);
+    cudaMemsetAsync(sorted_count, 0, 4 * sizeof(unsigned long long), st);
     cudaMemsetAsync(exact_count, 0, sizeof(unsigned long long), st);
-    // lists longer than rank_max take the sorted-axis split (the rank
-    // method costs O(m^2) a level)
+    // lists longer than rank_max go to the instance with larger buffers (up
+    // to LEAF_MID_MAX entries), longer ones to the sorted-axis split
     rank_max = rank_max < 1 ? 1 : rank_max > LEAF_FAST_MAX ? LEAF_FAST_MAX : rank_max;
-    k_leaf_order<<<blocks, LEAF_WARPS * 32, 0, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset,
-                                                    leaf_atom, leaf_xyz, blk_lo, blk_hi, sorted_list, sorted_count,
-                                                    list_cap, exact_list, exact_count, counters, rank_max,
-                                                    work, n_work);
+    int64_t *mid_list = sorted_list + 3 * list_cap;
+    unsigned long long *mid_count = sorted_count + 3;
+    k_leaf_order<LEAF_FAST_MAX, LEAF_WARPS><<<blocks, LEAF_WARPS * 32, 0, st>>>(
+        cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset, leaf_atom, leaf_xyz, blk_lo, blk_hi,
+        sorted_list, sorted_count, list_cap, exact_list, exact_count, counters, rank_max, work, n_work, mid_list,
+        mid_count, LEAF_MID_MAX, 1);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    k_leaf_order<LEAF_MID_MAX, 2><<<sms * 8, 64, 0, st>>>(
+        cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset, leaf_atom, leaf_xyz, blk_lo, blk_hi,
+        sorted_list, sorted_count, list_cap, exact_list, exact_count, counters, LEAF_MID_MAX, mid_list, mid_count,
+        nullptr, nullptr, 0, 0);
     // sorted-axis split, one worklist per size class: up to 512 entries
     // 13 KB a warp (4 warps a block), up to 1024 25 KB (2 a block), up to
     // LEAF_SORTED_MAX 50 KB (1 a block)

@@ -39,8 +39,9 @@ constexpr int MAX_TEMPLATE_ATOMS = 1024;
 constexpr int LEAF_WARPS = 4;          // warps per block of k_leaf_order
 constexpr int LEAF_FAST_MAX = 192;     // capacity of the rank method's buffers
 constexpr int LEAF_RANK_MAX = 192;     // default: longest list ordered by the rank method
-constexpr int LEAF_SORT_FROM = 64;     // rank method: level 0 by a bitmap sort from this length,
-constexpr int LEAF_SORT1_FROM = 128;   //   level 1 from this one
+constexpr int LEAF_MID_MAX = 384;      // longest list of the rank method's larger instance
+constexpr int LEAF_SORT_FROM = 64;     // rank method: a level's nodes of this many entries or
+                                       //   more are ordered by a bitmap sort
 constexpr int LEAF_SORT_WORDS = 128;   // its window (32-bit words)
 constexpr int LEAF_SORTED_MAX = 2048;  // longest list ordered by sorted axes
 constexpr int LEAF_SORT_MAX = 1024;    // longest list ordered by presorted axes
