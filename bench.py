@@ -342,6 +342,17 @@ def search_profile(args):
         "lanes_per_product_batch": prof["prod_lanes"] / max(1, prof["prod_batches"]),
         "block_visits_per_partial": prof["block_visits"] / max(1, st["partials"]),
     }
+    lo = prof.get("leaf_order")
+    if lo:
+        cyc = max(1, lo["cyc_list"])
+        derived["leaf_order"] = {
+            "warp_cycles_per_entry": lo["cyc_list"] / max(1, lo["entries"]),
+            **{f"share_{k}": lo[f"cyc_{k}"] / cyc for k in ("load", "sort", "count", "seg", "write")},
+            "sort_words_per_node": lo["sort_words"] / max(1, lo["sort_nodes"]),
+            "count_pairs_per_entry": lo["count_pairs"] / max(1, lo["entries"]),
+            "class_cycles_per_entry": [c / max(1, e) for c, e in zip(lo["class_cycles"], lo["class_entries"])],
+            "class_entry_share": [e / max(1, lo["entries"]) for e in lo["class_entries"]],
+        }
     print(json.dumps({"search_profile": prof, "derived": derived, "workload": wl.name,
                       "partials": st["partials"], "complete": st["complete"],
                       "ms_expansion_profile_build": st["ms_expansion"]}))

@@ -832,7 +832,21 @@ void write_search_profile(const unsigned long long *d_prof, cudaStream_t st, con
     fprintf(f, "{\"ms_expansion\": %.3f, \"partials\": %lld, \"search_rounds\": %d", stats.ms_expansion,
             (long long)stats.partials, stats.search_rounds);
     for (int i = 0; i < SP_NUM; i++) fprintf(f, ", \"%s\": %llu", names[i], h[i]);
-    fprintf(f, "}\n");
+    static const char *lnames[LP_CLASS] = {"lists", "entries", "handed", "cyc_list", "cyc_load", "cyc_sort",
+                                           "cyc_count", "cyc_seg", "cyc_write", "sort_nodes", "sort_words",
+                                           "count_pairs"};
+    unsigned long long lh[LP_NUM] = {};
+    leaf_profile_read(lh, st);
+    cudaStreamSynchronize(st);
+    fprintf(f, ", \"leaf_order\": {");
+    for (int i = 0; i < LP_CLASS; i++) fprintf(f, "%s\"%s\": %llu", i ? ", " : "", lnames[i], lh[i]);
+    const char *cls[3] = {"class_lists", "class_entries", "class_cycles"};
+    for (int k = 0; k < 3; k++) {
+        fprintf(f, ", \"%s\": [", cls[k]);
+        for (int c = 0; c < 7; c++) fprintf(f, "%s%llu", c ? ", " : "", lh[LP_CLASS + 7 * k + c]);
+        fprintf(f, "]");
+    }
+    fprintf(f, "}}\n");
     fclose(f);
 }
 #endif
@@ -1001,6 +1015,9 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
         }
     }
     CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+#if PJG_SEARCH_PROF
+    leaf_profile_reset(st);
+#endif
     for (auto &e : ev) CUDA_TRY(cudaEventCreate(&e));
     CUDA_TRY(cudaEventRecord(ev[0], st));
 

@@ -588,6 +588,24 @@ __device__ bool sort_segment(LeafWarp<CAP> &L, const uint16_t *A, uint16_t *B, i
     return placed == n;
 }
 
+// Leaf-order profile probes (PJG_SEARCH_PROF builds): every lane keeps the
+// same per-warp sums (the probes sit on warp-uniform paths); lane 0 adds them
+// to g_leaf_prof when the warp exits.
+#if PJG_SEARCH_PROF
+__device__ unsigned long long g_leaf_prof[LP_NUM];
+#define LPROF_T(name) const long long name = clock64()
+#define LPROF_ADD(i, v) (lp[i] += (unsigned long long)(v))
+#else
+#define LPROF_T(name)
+#define LPROF_ADD(i, v) \
+    do {                \
+    } while (0)
+#endif
+
+__device__ __forceinline__ int leaf_class(int m) {
+    return m <= 16 ? 0 : m <= 32 ? 1 : m <= 64 ? 2 : m <= 96 ? 3 : m <= 128 ? 4 : m <= 192 ? 5 : 6;
+}
+
 // Lists (at most rank_max <= CAP entries) without a tie: rank method, one
 // warp per list -- the first levels by bitmap sorts of the nodes, the rest by
 // counting each entry's smaller keys in its node.  Longer lists up to
@@ -612,6 +630,9 @@ __global__ void __launch_bounds__(WARPS * 32)
     // the requested lists, or every list of the chunk
     int64_t total = work ? (int64_t)*n_work : (int64_t)cv.n_structures * n_sigs;
     unsigned long long n_exact = 0, n_sorted = 0, n_lists = 0, n_entries = 0;
+#if PJG_SEARCH_PROF
+    unsigned long long lp[LP_NUM] = {};
+#endif
     for (int64_t item = warp; item < total; item += nwarps) {
         const int64_t w = work ? work[item] : item;
         const int m = count[w];
@@ -625,8 +646,10 @@ __global__ void __launch_bounds__(WARPS * 32)
         if (tie && mid_list && m <= mid_max) {
             if (lane == 0) mid_list[atomicAdd(mid_count, 1ull)] = w;
             __syncwarp();
+            LPROF_ADD(LP_HANDED, 1);
             continue;
         }
+        LPROF_T(t_list);
         int src = 0;
         if (!tie) {
             // keys: the atoms' unique axis ranks (an exact order of the FP64
@@ -647,6 +670,8 @@ __global__ void __launch_bounds__(WARPS * 32)
             __syncwarp();
             for (int i = lane; i < m; i += 32) L.cur[i] = L.ur[0][i];
             __syncwarp();
+            LPROF_T(t_load);
+            LPROF_ADD(LP_CYC_LOAD, t_load - t_list);
             int levels = 0;
             while ((1 << levels) < m) levels++;
             for (int d = 0; d < levels; d++) {
@@ -658,6 +683,7 @@ __global__ void __launch_bounds__(WARPS * 32)
                 // counting below computes, in O(atoms / 32 + m / 32) a node
                 // instead of O(m n / 32))
                 bool sorted0 = false;
+                LPROF_T(t_a);
                 if ((m >> d) >= LEAF_SORT_FROM) {
                     const int natoms = cv.atom_count[w / n_sigs];
                     sorted0 = true;
@@ -667,11 +693,15 @@ __global__ void __launch_bounds__(WARPS * 32)
                             if (lane == 0) B[lo] = A[lo];
                         } else {
                             sorted0 = sort_segment(L, A, B, lo, n, d % 3, natoms) && sorted0;
+                            LPROF_ADD(LP_SORT_NODES, 1);
+                            LPROF_ADD(LP_SORT_WORDS, (natoms + 31) >> 5);
                         }
                         lo += n < 1 ? 1 : n;
                     }
                     __syncwarp();
                 }
+                LPROF_T(t_b);
+                LPROF_ADD(LP_CYC_SORT, t_b - t_a);
                 if (!sorted0) {
                     for (int p = lane; p < m; p += 32) {
                         const int lo = L.seg_lo[p], n = L.seg_n[p];
@@ -685,9 +715,12 @@ __global__ void __launch_bounds__(WARPS * 32)
 #pragma unroll 8
                         for (int q = lo; q < lo + n; q++) before += L.cur[q] < x;
                         B[lo + before] = (uint16_t)e;
+                        LPROF_ADD(LP_COUNT_PAIRS, n);
                     }
                 }
                 __syncwarp();
+                LPROF_T(t_c);
+                LPROF_ADD(LP_CYC_COUNT, t_c - t_b);
                 // median-boundary ties, next axis keys, child nodes
                 const int ax = d % 3, nax = (d + 1) % 3;
                 bool t = false;
@@ -707,6 +740,8 @@ __global__ void __launch_bounds__(WARPS * 32)
                 }
                 src ^= 1;
                 __syncwarp();
+                LPROF_T(t_d);
+                LPROF_ADD(LP_CYC_SEG, t_d - t_c);
                 if (__any_sync(FULL_MASK, t)) {
                     tie = true;
                     break;
@@ -714,6 +749,9 @@ __global__ void __launch_bounds__(WARPS * 32)
             }
         }
         if (tie) {
+            LPROF_T(t_tie);
+            LPROF_ADD(LP_CYC_LIST, t_tie - t_list);
+            LPROF_ADD(LP_HANDED, 1);
             if (m <= LEAF_SORTED_MAX) {
                 // size classes of k_leaf_sorted: up to 512, 1024, 2048 entries
                 const int c = m <= 512 ? 0 : m <= 1024 ? 1 : 2;
@@ -726,9 +764,30 @@ __global__ void __launch_bounds__(WARPS * 32)
             __syncwarp();
             continue;
         }
+        LPROF_T(t_w0);
         write_leaves(L.ord[src], m, leaf_offset[w], cand_atom + o, cv.xyz32 + cv.atom_base[w / n_sigs], leaf_atom,
                      leaf_xyz, blk_offset[w], blk_lo, blk_hi);
+#if PJG_SEARCH_PROF
+        {
+            LPROF_T(t_w1);
+            const int c = leaf_class(m);
+            LPROF_ADD(LP_CYC_WRITE, t_w1 - t_w0);
+            LPROF_ADD(LP_CYC_LIST, t_w1 - t_list);
+            LPROF_ADD(LP_LISTS, 1);
+            LPROF_ADD(LP_ENTRIES, m);
+            LPROF_ADD(LP_CLASS + c, 1);
+            LPROF_ADD(LP_CLASS_ENT + c, m);
+            LPROF_ADD(LP_CLASS_CYC + c, t_w1 - t_list);
+        }
+#endif
     }
+#if PJG_SEARCH_PROF
+    // the comparison counts differ by lane; every other sum is warp-uniform
+    for (int off = 16; off; off >>= 1) lp[LP_COUNT_PAIRS] += __shfl_xor_sync(FULL_MASK, lp[LP_COUNT_PAIRS], off);
+    if (lane == 0)
+        for (int i = 0; i < LP_NUM; i++)
+            if (lp[i]) atomicAdd(&g_leaf_prof[i], lp[i]);
+#endif
     if (lane == 0 && n_exact) atomicAdd(&counters[C_LEAF_EXACT], n_exact);
     if (lane == 0 && n_sorted) atomicAdd(&counters[C_LEAF_SORTED], n_sorted);
     if (lane == 0 && n_lists) atomicAdd(&counters[C_LEAF_LISTS], n_lists);
@@ -3358,6 +3417,18 @@ void launch_scan_tiles_i64(cudaStream_t st, const int64_t *in, int64_t n, int64_
 void launch_scan_add(cudaStream_t st, int64_t *out, int64_t n, const int64_t *tile_offsets) {
     k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, n, tile_offsets);
 }
+
+#if PJG_SEARCH_PROF
+void leaf_profile_reset(cudaStream_t st) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_leaf_prof) == cudaSuccess)
+        cudaMemsetAsync(p, 0, LP_NUM * sizeof(unsigned long long), st);
+}
+
+void leaf_profile_read(unsigned long long *h, cudaStream_t st) {
+    cudaMemcpyFromSymbolAsync(h, g_leaf_prof, LP_NUM * sizeof(unsigned long long), 0, cudaMemcpyDeviceToHost, st);
+}
+#endif
 
 void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t n_sigs, const int32_t *count,
                        const int64_t *offset, const int64_t *blk_offset, const int32_t *cand_atom,

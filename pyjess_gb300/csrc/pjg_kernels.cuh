@@ -89,6 +89,28 @@ enum SearchProf : int {
     SP_NUM
 };
 
+// Leaf-order profile (same build flag): k_leaf_order's section cycles and
+// the lists it takes by length class, summed over warps of both instances.
+enum LeafProf : int {
+    LP_LISTS = 0,        // lists ordered by the rank method
+    LP_ENTRIES,          //   their entries
+    LP_HANDED,           // lists handed on (longer, or a median tie)
+    LP_CYC_LIST,         // cycles of every list begun, load to write-out or hand-on
+    LP_CYC_LOAD,         //   loading ranks
+    LP_CYC_SORT,         //   bitmap-sorted levels
+    LP_CYC_COUNT,        //   counted levels
+    LP_CYC_SEG,          //   tie checks, next keys, child nodes
+    LP_CYC_WRITE,        //   leaves and block boxes written
+    LP_SORT_NODES,       // nodes bitmap-sorted
+    LP_SORT_WORDS,       //   bitmap words they cleared and scanned
+    LP_COUNT_PAIRS,      // key comparisons of the counted levels
+    LP_CLASS,            // lists by length: <=16, <=32, <=64, <=96, <=128,
+                         //   <=192, <=384 (7 counters)
+    LP_CLASS_ENT = LP_CLASS + 7,  // entries by the same classes (7)
+    LP_CLASS_CYC = LP_CLASS_ENT + 7,  // cycles by the same classes (7)
+    LP_NUM = LP_CLASS_CYC + 7
+};
+
 struct SearchArgs {
     int32_t n_pairs;                   // chunk structures x templates
     int32_t ignore_chain;
@@ -228,6 +250,11 @@ void launch_scan_add(cudaStream_t st, int64_t *out, int64_t n, const int64_t *ti
 
 // kd leaf order of the lists in `work` (n_work entries, read on the device),
 // or of every list of the chunk when work == nullptr
+#if PJG_SEARCH_PROF
+// leaf-order profile: zero it / copy its LP_NUM sums to the host
+void leaf_profile_reset(cudaStream_t st);
+void leaf_profile_read(unsigned long long *h, cudaStream_t st);
+#endif
 void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t n_sigs, const int32_t *count,
                        const int64_t *offset, const int64_t *blk_offset, const int32_t *cand_atom,
                        const int64_t *leaf_offset, int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
