@@ -264,9 +264,10 @@ void pjg_results_destroy(pjg_results *r);
  *                  16384)
  *   pair_grain     (structure, template) pairs a search warp takes from the
  *                  work queue at a time (default 1, 1 .. 64)
- *   leaf_rank_max  longest tie-free list put in leaf order by the rank
- *                  method (longer lists: sorted-axis splits) (default 192,
- *                  1 .. 192)
+ *   leaf_rank_max  longest tie-free list put in leaf order by the
+ *                  leaf-order kernel's instance with the smallest buffers
+ *                  (longer lists: the instances for up to 512 and 1024
+ *                  entries) (default 256, 1 .. 256)
  *   leaf_reach     when a pair reaches a list with no leaf order it is
  *                  suspended and requests that list and the next
  *                  leaf_reach - 1 deeper ones of its levels (-1, the

@@ -1229,8 +1229,8 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 }
                 CUDA_TRY(dalloc(d_exact_list, (size_t)Wc, st));
                 CUDA_TRY(dalloc(d_exact_count, 1, st));
-                CUDA_TRY(dalloc(d_sorted_list, 4 * (size_t)Wc, st));
-                CUDA_TRY(dalloc(d_sorted_count, 4, st));
+                CUDA_TRY(dalloc(d_sorted_list, (size_t)LEAF_LISTS * (size_t)Wc, st));
+                CUDA_TRY(dalloc(d_sorted_count, LEAF_LISTS, st));
                 launches++;  // block counts
                 CUDA_TRY(cudaGetLastError());
             }

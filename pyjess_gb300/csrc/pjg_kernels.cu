@@ -794,6 +794,316 @@ __global__ void __launch_bounds__(WARPS * 32)
     if (lane == 0 && n_entries) atomicAdd(&counters[C_LEAF_ENTRIES], n_entries);
 }
 
+// ---------------------------------------------------------------------------
+// k_leaf_part: tie-free lists by axis partitions, one warp per list.
+//
+// The three axis orders of the list are sorted once (bitmap over the
+// structure's unique axis ranks, sort_segment); then every level takes, in
+// each node, the first n/2 entries of the split axis's order as the left
+// child (the n/2 smallest: the same sets k_leaf_order's ranks give), marks
+// them in one ballot pass over that order, and moves the other two orders
+// to their children by a stable partition (one ballot prefix a 32-entry
+// chunk).  O(m / 32) warp steps a level instead of the rank method's
+// O(m n / 32).  A tie at a median boundary (equal strict-lower ranks on both
+// sides of position n/2) hands the list on to k_leaf_sorted, which replays
+// qselect there.  Leaves and block boxes are written from the cached atom
+// indices, each 32-leaf chunk's boxes reduced in registers.
+
+template <int CAP>
+struct PartWarp {
+    uint16_t S[4][CAP];   // the three axis orders and a spare (candidate indices)
+    uint16_t lr[3][CAP];  // strict-lower axis ranks by candidate index (low 16
+                          // bits: a false tie only hands the list on)
+    int32_t atom[CAP];    // structure atom of each candidate index
+    union {
+        uint32_t ur[CAP];  // unique ranks of the axis being sorted
+        struct {
+            uint32_t seg[CAP];   // node of each position: lo | n << 16
+            uint16_t base[CAP];  // at a node's first position: left members
+                                 // of the nodes before it
+            uint8_t flag[CAP];   // candidate goes to the left child
+        } lv;
+    } u;
+    uint32_t bits[LEAF_SORT_WORDS];
+    uint16_t wpre[LEAF_SORT_WORDS];
+};
+
+// sort_segment's bitmap sort on a PartWarp: S_out[0..m) = candidate indices
+// 0..m-1 (keys L.u.ur) in key order; false when a key repeats
+template <int CAP>
+__device__ bool part_sort(PartWarp<CAP> &L, uint16_t *S_out, int m, int natoms) {
+    const int lane = lane_id();
+    constexpr int WB = 32 * LEAF_SORT_WORDS;
+    int placed = 0;
+    for (int wb = 0; wb < natoms; wb += WB) {
+        const int nwords = min(LEAF_SORT_WORDS, (natoms - wb + 31) >> 5);
+        for (int q = lane; q < nwords; q += 32) L.bits[q] = 0u;
+        __syncwarp();
+        for (int i = lane; i < m; i += 32) {
+            const uint32_t u = L.u.ur[i] - (uint32_t)wb;
+            if (u < (uint32_t)WB) atomicOr(&L.bits[u >> 5], 1u << (u & 31));
+        }
+        __syncwarp();
+        int carry = placed;
+        for (int w0 = 0; w0 < nwords; w0 += 32) {
+            const int wd = w0 + lane;
+            const int c = wd < nwords ? __popc(L.bits[wd]) : 0;
+            int incl = c;
+            for (int off = 1; off < 32; off <<= 1) {
+                const int y = __shfl_up_sync(FULL_MASK, incl, off);
+                if (lane >= off) incl += y;
+            }
+            if (wd < nwords) L.wpre[wd] = (uint16_t)(carry + incl - c);
+            carry += __shfl_sync(FULL_MASK, incl, 31);
+        }
+        __syncwarp();
+        for (int i = lane; i < m; i += 32) {
+            const uint32_t u = L.u.ur[i] - (uint32_t)wb;
+            if (u < (uint32_t)WB) {
+                const int pos = L.wpre[u >> 5] + __popc(L.bits[u >> 5] & ((1u << (u & 31)) - 1u));
+                if (pos < m) S_out[pos] = (uint16_t)i;
+            }
+        }
+        __syncwarp();
+        placed = carry;
+    }
+    return placed == m;
+}
+
+// Lists of at most take_max <= CAP entries without a median tie.  Longer
+// lists go to fwd_list[0] (up to fwd_max[0] entries) or fwd_list[1] (up to
+// fwd_max[1]) when given, else to k_leaf_sorted's worklists by size class
+// (up to LEAF_SORTED_MAX) or k_leaf_exact's; tied lists likewise to the
+// sorted or exact worklists.  count_lists: this instance counts the lists
+// it is given (the first instance; the others see lists already counted).
+template <int CAP, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+    k_leaf_part(ChunkView cv, int32_t n_sigs, const int32_t *count, const int64_t *offset,
+                const int64_t *blk_offset, const int32_t *cand_atom, const int64_t *leaf_offset,
+                int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi, int64_t *sorted_list,
+                unsigned long long *sorted_count, int64_t list_cap, int64_t *exact_list,
+                unsigned long long *exact_count, unsigned long long *counters, int take_max, const int64_t *work,
+                const unsigned long long *n_work, int64_t *fwd_list0, unsigned long long *fwd_count0,
+                int fwd_max0, int64_t *fwd_list1, unsigned long long *fwd_count1, int fwd_max1,
+                int count_lists) {
+    extern __shared__ __align__(16) unsigned char part_smem[];
+    PartWarp<CAP> &L = reinterpret_cast<PartWarp<CAP> *>(part_smem)[threadIdx.x >> 5];
+    const int lane = lane_id();
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t total = work ? (int64_t)*n_work : (int64_t)cv.n_structures * n_sigs;
+    unsigned long long n_exact = 0, n_sorted = 0, n_lists = 0, n_entries = 0;
+#if PJG_SEARCH_PROF
+    unsigned long long lp[LP_NUM] = {};
+#endif
+    for (int64_t item = warp; item < total; item += nwarps) {
+        const int64_t w = work ? work[item] : item;
+        const int m = count[w];
+        if (m <= 0) continue;
+        if (count_lists) {
+            n_lists++;
+            n_entries += (unsigned long long)m;
+        }
+        bool handoff = m > take_max;
+        LPROF_T(t_list);
+        if (handoff && fwd_list0 && m <= fwd_max0) {
+            if (lane == 0) fwd_list0[atomicAdd(fwd_count0, 1ull)] = w;
+            __syncwarp();
+            continue;
+        }
+        if (handoff && fwd_list1 && m <= fwd_max1) {
+            if (lane == 0) fwd_list1[atomicAdd(fwd_count1, 1ull)] = w;
+            __syncwarp();
+            continue;
+        }
+        const int s = (int)(w / n_sigs);
+        const int64_t gbase = cv.atom_base[s];
+        const int natoms = cv.atom_count[s];
+        const int32_t *ca = cand_atom + offset[w];
+        bool exact = false;
+        if (!handoff) {
+            // atoms, strict-lower ranks, x ranks; then the three axis orders
+            LPROF_T(t_l0);
+#pragma unroll 4
+            for (int i = lane; i < m; i += 32) {
+                const int a = ca[i];
+                const int64_t g = gbase + a;
+                L.atom[i] = a;
+                L.lr[0][i] = (uint16_t)cv.lrank[g];
+                L.lr[1][i] = (uint16_t)cv.lrank[cv.n_atoms + g];
+                L.lr[2][i] = (uint16_t)cv.lrank[2 * cv.n_atoms + g];
+                L.u.ur[i] = cv.urank[g];
+            }
+            __syncwarp();
+            {
+                LPROF_T(t_l1);
+                LPROF_ADD(LP_CYC_LOAD, t_l1 - t_l0);
+            }
+            for (int a = 0; a < 3 && !exact; a++) {
+                if (a > 0) {
+                    LPROF_T(t_g0);
+#pragma unroll 4
+                    for (int i = lane; i < m; i += 32) L.u.ur[i] = cv.urank[a * cv.n_atoms + gbase + L.atom[i]];
+                    __syncwarp();
+                    LPROF_T(t_g1);
+                    LPROF_ADD(LP_CYC_LOAD, t_g1 - t_g0);
+                }
+                LPROF_T(t_s0);
+                // a repeated atom (never in a candidate list) goes to the
+                // exact replay
+                exact = !part_sort(L, L.S[a], m, natoms);
+                LPROF_T(t_s1);
+                LPROF_ADD(LP_CYC_SORT, t_s1 - t_s0);
+                LPROF_ADD(LP_SORT_NODES, 1);
+                LPROF_ADD(LP_SORT_WORDS, (natoms + 31) >> 5);
+            }
+        }
+        LPROF_T(t_lv);
+        if (!handoff && !exact) {
+            for (int p = lane; p < m; p += 32) L.u.lv.seg[p] = (uint32_t)m << 16;
+            __syncwarp();
+            int cur0 = 0, cur1 = 1, cur2 = 2, spare = 3;
+            int levels = 0;
+            while ((1 << levels) < m) levels++;
+            for (int d = 0; d < levels; d++) {
+                const int a = d % 3;
+                const uint16_t *Sa = L.S[a == 0 ? cur0 : a == 1 ? cur1 : cur2];
+                const uint16_t *La = L.lr[a];
+                // left members of every node from the split axis's order,
+                // and the median-boundary tie check
+                bool tie = false;
+                int carry = 0;
+#pragma unroll 2
+                for (int p0 = 0; p0 < m; p0 += 32) {
+                    const int p = p0 + lane;
+                    const bool valid = p < m;
+                    const uint32_t sg = valid ? L.u.lv.seg[p] : 0u;
+                    const int lo = (int)(sg & 0xFFFFu), n = (int)(sg >> 16), k = n >> 1;
+                    const int e = valid ? Sa[p] : 0;
+                    const bool left = n >= 2 && p < lo + k;
+                    if (valid) L.u.lv.flag[e] = (uint8_t)left;
+                    if (n >= 2 && p == lo + k) tie |= La[Sa[p - 1]] == La[e];
+                    const unsigned bal = __ballot_sync(FULL_MASK, left);
+                    if (valid && p == lo) L.u.lv.base[p] = (uint16_t)(carry + __popc(bal & lt));
+                    carry += __popc(bal);
+                }
+                if (__any_sync(FULL_MASK, tie)) {
+                    handoff = true;
+                    break;
+                }
+                __syncwarp();
+                // the other two orders, stably partitioned within each node;
+                // the second pass also moves every position to its child node
+                for (int t = 1; t <= 2; t++) {
+                    const int b = (a + t) % 3;
+                    const int cb = b == 0 ? cur0 : b == 1 ? cur1 : cur2;
+                    const uint16_t *src = L.S[cb];
+                    uint16_t *dst = L.S[spare];
+                    int fc = 0;
+#pragma unroll 2
+                    for (int p0 = 0; p0 < m; p0 += 32) {
+                        const int p = p0 + lane;
+                        const bool valid = p < m;
+                        const int e = valid ? src[p] : 0;
+                        const bool f = valid && L.u.lv.flag[e];
+                        const unsigned bal = __ballot_sync(FULL_MASK, f);
+                        const int Fp = fc + __popc(bal & lt);
+                        fc += __popc(bal);
+                        if (valid) {
+                            uint32_t sg = L.u.lv.seg[p];
+                            const int lo = (int)(sg & 0xFFFFu), n = (int)(sg >> 16), k = n >> 1;
+                            int to = p;
+                            if (n >= 2) {
+                                const int lb = Fp - (int)L.u.lv.base[lo];  // left members before p in its node
+                                to = f ? lo + lb : p + k - lb;
+                                if (t == 2) sg = p < lo + k ? ((uint32_t)lo | ((uint32_t)k << 16))
+                                                            : ((uint32_t)(lo + k) | ((uint32_t)(n - k) << 16));
+                            }
+                            dst[to] = (uint16_t)e;
+                            if (t == 2) L.u.lv.seg[p] = sg;
+                        }
+                    }
+                    __syncwarp();
+                    if (b == 0) cur0 = spare;
+                    else if (b == 1) cur1 = spare;
+                    else cur2 = spare;
+                    spare = cb;
+                }
+            }
+            LPROF_T(t_lv1);
+            LPROF_ADD(LP_CYC_COUNT, t_lv1 - t_lv);
+            if (!handoff) {
+                // leaves in reverse partition order (the query pops the right
+                // subtree first) and the boxes of their CULL_BLK-leaf blocks
+                const uint16_t *fin = L.S[cur0];
+                const float4 *pts = cv.xyz32 + gbase;
+                const int64_t lo_out = leaf_offset[w], bo = blk_offset[w];
+                for (int r0 = 0; r0 < m; r0 += 32) {
+                    const int r = r0 + lane;
+                    const bool valid = r < m;
+                    const int a = valid ? L.atom[fin[m - 1 - r]] : 0;
+                    const float4 x = valid ? pts[a] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (valid) {
+                        leaf_atom[lo_out + r] = a;
+                        leaf_xyz[lo_out + r] = x;
+                    }
+                    float mnx = valid ? x.x : INFINITY, mny = valid ? x.y : INFINITY, mnz = valid ? x.z : INFINITY;
+                    float mxx = valid ? x.x : -INFINITY, mxy = valid ? x.y : -INFINITY,
+                          mxz = valid ? x.z : -INFINITY;
+                    for (int off = CULL_BLK / 2; off; off >>= 1) {
+                        mnx = fminf(mnx, __shfl_xor_sync(FULL_MASK, mnx, off));
+                        mny = fminf(mny, __shfl_xor_sync(FULL_MASK, mny, off));
+                        mnz = fminf(mnz, __shfl_xor_sync(FULL_MASK, mnz, off));
+                        mxx = fmaxf(mxx, __shfl_xor_sync(FULL_MASK, mxx, off));
+                        mxy = fmaxf(mxy, __shfl_xor_sync(FULL_MASK, mxy, off));
+                        mxz = fmaxf(mxz, __shfl_xor_sync(FULL_MASK, mxz, off));
+                    }
+                    if ((lane & (CULL_BLK - 1)) == 0 && valid) {
+                        blk_lo[bo + r / CULL_BLK] = make_float4(mnx, mny, mnz, 0.f);
+                        blk_hi[bo + r / CULL_BLK] = make_float4(mxx, mxy, mxz, 0.f);
+                    }
+                }
+                __syncwarp();
+#if PJG_SEARCH_PROF
+                {
+                    LPROF_T(t_w1);
+                    const int c = leaf_class(m);
+                    LPROF_ADD(LP_CYC_WRITE, t_w1 - t_lv1);
+                    LPROF_ADD(LP_CYC_LIST, t_w1 - t_list);
+                    LPROF_ADD(LP_LISTS, 1);
+                    LPROF_ADD(LP_ENTRIES, m);
+                    LPROF_ADD(LP_CLASS + c, 1);
+                    LPROF_ADD(LP_CLASS_ENT + c, m);
+                    LPROF_ADD(LP_CLASS_CYC + c, t_w1 - t_list);
+                }
+#endif
+                continue;
+            }
+        }
+        LPROF_ADD(LP_HANDED, 1);
+        if (!exact && m <= LEAF_SORTED_MAX) {
+            // size classes of k_leaf_sorted: up to 512, 1024, 2048 entries
+            const int c = m <= 512 ? 0 : m <= 1024 ? 1 : 2;
+            n_sorted++;
+            if (lane == 0) sorted_list[c * list_cap + (int64_t)atomicAdd(&sorted_count[c], 1ull)] = w;
+        } else {
+            n_exact++;
+            if (lane == 0) exact_list[atomicAdd(exact_count, 1ull)] = w;
+        }
+        __syncwarp();
+    }
+#if PJG_SEARCH_PROF
+    if (lane == 0)
+        for (int i = 0; i < LP_NUM; i++)
+            if (lp[i]) atomicAdd(&g_leaf_prof[i], lp[i]);
+#endif
+    if (lane == 0 && n_exact) atomicAdd(&counters[C_LEAF_EXACT], n_exact);
+    if (lane == 0 && n_sorted) atomicAdd(&counters[C_LEAF_SORTED], n_sorted);
+    if (lane == 0 && n_lists) atomicAdd(&counters[C_LEAF_LISTS], n_lists);
+    if (lane == 0 && n_entries) atomicAdd(&counters[C_LEAF_ENTRIES], n_entries);
+}
+
 // Exact replay for the lists k_leaf_order could not order by ranks (a tie
 // at some median boundary, or a list too long for its shared buffer).
 //
@@ -3436,24 +3746,64 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
                        int64_t *sorted_list, unsigned long long *sorted_count, int64_t list_cap,
                        int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters,
                        const int64_t *work, const unsigned long long *n_work, int rank_max) {
-    cudaMemsetAsync(sorted_count, 0, 4 * sizeof(unsigned long long), st);
+    cudaMemsetAsync(sorted_count, 0, LEAF_LISTS * sizeof(unsigned long long), st);
     cudaMemsetAsync(exact_count, 0, sizeof(unsigned long long), st);
+    rank_max = rank_max < 1 ? 1 : rank_max > LEAF_FAST_MAX ? LEAF_FAST_MAX : rank_max;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+#if PJG_LEAF_RANK
     // lists longer than rank_max go to the instance with larger buffers (up
     // to LEAF_MID_MAX entries), longer ones to the sorted-axis split
-    rank_max = rank_max < 1 ? 1 : rank_max > LEAF_FAST_MAX ? LEAF_FAST_MAX : rank_max;
     int64_t *mid_list = sorted_list + 3 * list_cap;
     unsigned long long *mid_count = sorted_count + 3;
     k_leaf_order<LEAF_FAST_MAX, LEAF_WARPS><<<blocks, LEAF_WARPS * 32, 0, st>>>(
         cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset, leaf_atom, leaf_xyz, blk_lo, blk_hi,
         sorted_list, sorted_count, list_cap, exact_list, exact_count, counters, rank_max, work, n_work, mid_list,
         mid_count, LEAF_MID_MAX, 1);
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     k_leaf_order<LEAF_MID_MAX, 2><<<sms * 8, 64, 0, st>>>(
         cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset, leaf_atom, leaf_xyz, blk_lo, blk_hi,
         sorted_list, sorted_count, list_cap, exact_list, exact_count, counters, LEAF_MID_MAX, mid_list, mid_count,
         nullptr, nullptr, 0, 0);
+#else
+    (void)blocks;
+    // axis partitions: lists up to rank_max (<= 256 entries) in the first
+    // instance (7 KB a warp, 4 warps a block), which forwards lists up to
+    // 512 and 1024 entries to two instances with larger buffers (14 KB a
+    // warp, 4 a block; 28 KB, 2 a block); one wave of resident blocks each
+    int64_t *list512 = sorted_list + 3 * list_cap, *list1024 = sorted_list + 4 * list_cap;
+    unsigned long long *count512 = sorted_count + 3, *count1024 = sorted_count + 4;
+    auto wave = [&](const void *fn, int threads, int smem) {
+        int per_sm = 0;
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
+        return sms * (per_sm > 0 ? per_sm : 1);
+    };
+    {
+        constexpr int SP = (int)sizeof(PartWarp<256>) * 4;
+        const int g = wave((const void *)k_leaf_part<256, 4>, 128, SP);
+        k_leaf_part<256, 4><<<g, 128, SP, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset,
+                                                leaf_atom, leaf_xyz, blk_lo, blk_hi, sorted_list, sorted_count,
+                                                list_cap, exact_list, exact_count, counters, rank_max, work, n_work,
+                                                list512, count512, 512, list1024, count1024, 1024, 1);
+    }
+    {
+        constexpr int SP = (int)sizeof(PartWarp<512>) * 4;
+        const int g = wave((const void *)k_leaf_part<512, 4>, 128, SP);
+        k_leaf_part<512, 4><<<g, 128, SP, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset,
+                                                leaf_atom, leaf_xyz, blk_lo, blk_hi, sorted_list, sorted_count,
+                                                list_cap, exact_list, exact_count, counters, 512, list512, count512,
+                                                nullptr, nullptr, 0, nullptr, nullptr, 0, 0);
+    }
+    {
+        constexpr int SP = (int)sizeof(PartWarp<1024>) * 2;
+        const int g = wave((const void *)k_leaf_part<1024, 2>, 64, SP);
+        k_leaf_part<1024, 2><<<g, 64, SP, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset,
+                                                leaf_atom, leaf_xyz, blk_lo, blk_hi, sorted_list, sorted_count,
+                                                list_cap, exact_list, exact_count, counters, 1024, list1024,
+                                                count1024, nullptr, nullptr, 0, nullptr, nullptr, 0, 0);
+    }
+#endif
     // sorted-axis split, one worklist per size class: up to 512 entries
     // 13 KB a warp (4 warps a block), up to 1024 25 KB (2 a block), up to
     // LEAF_SORTED_MAX 50 KB (1 a block)

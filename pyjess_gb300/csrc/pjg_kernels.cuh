@@ -36,9 +36,21 @@ constexpr int LARGE_WARPS = 2;
 __host__ __device__ constexpr int large_warp_bytes(int nmax) { return ((52 * nmax) + 15) & ~15; }
 // longest template pjg_templates_create accepts
 constexpr int MAX_TEMPLATE_ATOMS = 1024;
+// kd leaf order of tie-free lists: axis partitions (k_leaf_part), or with
+// -DPJG_LEAF_RANK=1 the rank method (k_leaf_order)
+#ifndef PJG_LEAF_RANK
+#define PJG_LEAF_RANK 0
+#endif
 constexpr int LEAF_WARPS = 4;          // warps per block of k_leaf_order
+#if PJG_LEAF_RANK
 constexpr int LEAF_FAST_MAX = 192;     // capacity of the rank method's buffers
 constexpr int LEAF_RANK_MAX = 192;     // default: longest list ordered by the rank method
+#else
+constexpr int LEAF_FAST_MAX = 256;     // capacity of k_leaf_part's first instance
+constexpr int LEAF_RANK_MAX = 256;     // default: longest list that instance takes
+#endif
+constexpr int LEAF_LISTS = 5;          // leaf-order worklists: three k_leaf_sorted size
+                                       //   classes and two forwarded size classes
 constexpr int LEAF_MID_MAX = 384;      // longest list of the rank method's larger instance
 constexpr int LEAF_SORT_FROM = 64;     // rank method: a level's nodes of this many entries or
                                        //   more are ordered by a bitmap sort

@@ -32,7 +32,7 @@ import time
 
 import numpy as np
 
-DEFAULTS = {"leaf_levels": 4, "block_min": 64, "tile_cap": 4096, "pair_grain": 1, "leaf_rank_max": 192,
+DEFAULTS = {"leaf_levels": 4, "block_min": 64, "tile_cap": 4096, "pair_grain": 1, "leaf_rank_max": 256,
             "leaf_reach": -1}
 # candidate values per knob, searched in this order
 SPACE = {
@@ -41,7 +41,7 @@ SPACE = {
     "block_min": [32, 48, 64, 96, 128, 192],
     "pair_grain": [1, 2, 4, 8],
     "tile_cap": [1024, 2048, 4096, 8192],
-    "leaf_rank_max": [64, 96, 128, 160, 192],
+    "leaf_rank_max": [64, 128, 192, 256],
 }
 CACHE_ENV = "PJG_TUNING_CACHE"
 DEFAULT_CACHE = pathlib.Path(__file__).resolve().with_name("tuning.json")

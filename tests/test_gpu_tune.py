@@ -19,7 +19,7 @@ def test_tuning_abi_defaults_and_range_checks():
     assert _native.get_tuning() == tune.DEFAULTS
     _native.set_tuning({"block_min": 96, "pair_grain": 2})
     assert _native.get_tuning() == dict(tune.DEFAULTS, block_min=96, pair_grain=2)
-    for bad in ({"tile_cap": 16}, {"pair_grain": 65}, {"leaf_levels": -2}, {"leaf_rank_max": 193},
+    for bad in ({"tile_cap": 16}, {"pair_grain": 65}, {"leaf_levels": -2}, {"leaf_rank_max": 257},
                 {"leaf_reach": -2}):
         with pytest.raises(RuntimeError, match="invalid"):
             _native.set_tuning(bad)
