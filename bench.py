@@ -545,8 +545,8 @@ def main():
         "stage_ms": {"candidates": s0["ms_candidates"], "expansion": s0["ms_expansion"],
                      "superposition": s0["ms_superposition"], "total": s0["ms_total"]},
         "counters": {k: s0[k] for k in ("pairs", "candidate_entries", "partials", "complete", "passing", "hits",
-                                        "fp64_rechecks", "leaf_lists", "leaf_entries", "leaf_exact", "suspensions",
-                                        "search_rounds", "chunks", "row_splits")},
+                                        "fp64_rechecks", "leaf_lists", "leaf_entries", "leaf_shared", "leaf_sorted",
+                                        "leaf_exact", "suspensions", "search_rounds", "chunks", "row_splits")},
         "cpu_baseline": cpu,
         "ingestion": ingest,
         "e2e": e2e,

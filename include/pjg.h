@@ -150,6 +150,9 @@ typedef struct {
     int32_t row_splits;              /* chunks redone on fewer structures
                                         because their complete rows did
                                         not fit in memory                  */
+    int64_t leaf_shared;             /* of leaf_lists: lists of the same
+                                        atoms as another list of their
+                                        structure, sharing its leaf order  */
 } pjg_stats;
 
 typedef struct pjg_templates pjg_templates;

@@ -94,6 +94,7 @@ class Stats(C.Structure):
         ("suspensions", C.c_int64),
         ("search_rounds", C.c_int32),
         ("row_splits", C.c_int32),
+        ("leaf_shared", C.c_int64),
     ]
 
     def as_dict(self) -> dict:

@@ -955,6 +955,11 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     DBuf<unsigned char> d_pool_a, d_pool_b;
     DBuf<unsigned long long> d_pool_used;
     int64_t pool_cap = 0;
+    // requested lists sharing one leaf order (table and worklists)
+    DBuf<unsigned long long> d_ls_key, d_ls_n;
+    DBuf<int32_t> d_ls_rep, d_ls_slot;
+    DBuf<int64_t> d_ls_rep_work, d_ls_dup, d_ls_left;
+    DBuf<uint8_t> d_ls_ok;
     DBuf<double> d_c_rmsd;
     DBuf<unsigned long long> d_prof;  // search profile (profile builds)
     // per complete row, in reference order
@@ -1272,6 +1277,10 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 cd.leaf_xyz = d_leaf_xyz.p;
                 return cudaSuccess;
             };
+            // lists of the same atoms share one leaf order (demand mode only:
+            // there the leaf offsets are a separate, writable array)
+            ListShare ls{};
+            bool share_on = false;
             auto order_requested = [&]() -> cudaError_t {
                 if (dm.fill_state) {
                     // the requested lists not filled yet
@@ -1279,11 +1288,32 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                                       dm.work, dm.n_work, dm.fill_state, true);
                     launches++;
                 }
-                launch_leaf_order(st, leaf_blocks, cv, G, cnt_c, d_offset.p, d_boff.p, d_cand_atom.p, leaf_off,
-                                  d_leaf_atom.p, d_leaf_xyz.p, d_blk_lo.p, d_blk_hi.p, d_sorted_list.p,
-                                  d_sorted_count.p, Wc, d_exact_list.p, d_exact_count.p, d_counters.p, dm.work,
-                                  dm.n_work, tune.leaf_rank_max);
-                launches += 7;
+                if (share_on) {
+                    // key every requested list, order one list per key, point
+                    // the others at its leaves, order those whose atoms differ
+                    const cudaError_t e0 = cudaMemsetAsync(ls.n, 0, 3 * sizeof(unsigned long long), st);
+                    if (e0 != cudaSuccess) return e0;
+                    launch_list_keys(st, sm_count() * 16, G, cnt_c, d_offset.p, d_cand_atom.p, dm.work, dm.n_work,
+                                     ls, d_counters.p);
+                    launch_list_reps(st, sm_count() * 16, dm.work, dm.n_work, ls);
+                    launch_leaf_order(st, leaf_blocks, cv, G, cnt_c, d_offset.p, d_boff.p, d_cand_atom.p, leaf_off,
+                                      d_leaf_atom.p, d_leaf_xyz.p, d_blk_lo.p, d_blk_hi.p, d_sorted_list.p,
+                                      d_sorted_count.p, Wc, d_exact_list.p, d_exact_count.p, d_counters.p,
+                                      ls.rep_work, ls.n, tune.leaf_rank_max, ls.part_ok, 0);
+                    launch_list_share(st, sm_count() * 8, cv, G, cnt_c, d_offset.p, d_cand_atom.p, d_leaf_off.p,
+                                      d_boff.p, ls, d_counters.p);
+                    launch_leaf_order(st, leaf_blocks, cv, G, cnt_c, d_offset.p, d_boff.p, d_cand_atom.p, leaf_off,
+                                      d_leaf_atom.p, d_leaf_xyz.p, d_blk_lo.p, d_blk_hi.p, d_sorted_list.p,
+                                      d_sorted_count.p, Wc, d_exact_list.p, d_exact_count.p, d_counters.p,
+                                      ls.left_work, ls.n + 2, tune.leaf_rank_max, ls.part_ok, 0);
+                    launches += 17;
+                } else {
+                    launch_leaf_order(st, leaf_blocks, cv, G, cnt_c, d_offset.p, d_boff.p, d_cand_atom.p, leaf_off,
+                                      d_leaf_atom.p, d_leaf_xyz.p, d_blk_lo.p, d_blk_hi.p, d_sorted_list.p,
+                                      d_sorted_count.p, Wc, d_exact_list.p, d_exact_count.p, d_counters.p, dm.work,
+                                      dm.n_work, tune.leaf_rank_max);
+                    launches += 7;
+                }
                 if (dm.state) {
                     launch_mark_ordered(st, sm_count() * 4, dm);
                     launches++;
@@ -1335,6 +1365,45 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 dm.fill_state = d_fill_state.p;
                 dm.fill_work = d_fill_work.p;
                 dm.n_fill = d_nfill.p;
+                {
+                    // the list-sharing table: twice the chunk's lists, a power
+                    // of two (without the memory, every list is ordered)
+                    int64_t cap = 1;
+                    while (cap < 2 * Wc) cap <<= 1;
+                    cudaError_t e = dalloc(d_ls_key, (size_t)cap, st);
+                    if (e == cudaSuccess) e = dalloc(d_ls_rep, (size_t)cap, st);
+                    if (e == cudaSuccess) e = dalloc(d_ls_slot, (size_t)Wc, st);
+                    if (e == cudaSuccess) e = dalloc(d_ls_rep_work, (size_t)Wc, st);
+                    if (e == cudaSuccess) e = dalloc(d_ls_dup, (size_t)Wc, st);
+                    if (e == cudaSuccess) e = dalloc(d_ls_left, (size_t)Wc, st);
+                    if (e == cudaSuccess) e = dalloc(d_ls_n, 3, st);
+                    if (e == cudaSuccess) e = dalloc(d_ls_ok, (size_t)Wc, st);
+                    if (e == cudaSuccess) e = cudaMemsetAsync(d_ls_key.p, 0, (size_t)cap * sizeof(unsigned long long), st);
+                    if (e == cudaSuccess) e = cudaMemsetAsync(d_ls_rep.p, 0xFF, (size_t)cap * sizeof(int32_t), st);
+                    if (e == cudaSuccess) e = cudaMemsetAsync(d_ls_ok.p, 0, (size_t)Wc, st);
+                    // PJG_LIST_SHARING=0 orders every list itself
+                    const char *v = getenv("PJG_LIST_SHARING");
+                    share_on = e == cudaSuccess && !(v && v[0] == '0');
+                    if (e != cudaSuccess) {
+                        cudaGetLastError();
+                        dfree(d_ls_key, st);
+                        dfree(d_ls_rep, st);
+                        dfree(d_ls_slot, st);
+                        dfree(d_ls_rep_work, st);
+                        dfree(d_ls_dup, st);
+                        dfree(d_ls_left, st);
+                        dfree(d_ls_ok, st);
+                    }
+                    ls.key = d_ls_key.p;
+                    ls.rep = d_ls_rep.p;
+                    ls.mask = cap - 1;
+                    ls.slot = d_ls_slot.p;
+                    ls.rep_work = d_ls_rep_work.p;
+                    ls.dup_work = d_ls_dup.p;
+                    ls.left_work = d_ls_left.p;
+                    ls.n = d_ls_n.p;
+                    ls.part_ok = d_ls_ok.p;
+                }
                 if (n_pairs > INT32_MAX) {
                     status = fail(PJG_ERR_CAPACITY, "too many pairs in one chunk");
                     goto done;
@@ -1526,7 +1595,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                     unsigned long long cur[C_NUM];
                     CUDA_TRY(cudaMemcpyAsync(cur, d_counters.p, sizeof cur, cudaMemcpyDeviceToHost, st));
                     CUDA_TRY(cudaStreamSynchronize(st));
-                    for (int c : {C_LEAF_EXACT, C_LEAF_SORTED, C_LEAF_REPLAY, C_LEAF_LISTS, C_LEAF_ENTRIES, C_ERROR})
+                    for (int c : {C_LEAF_EXACT, C_LEAF_SORTED, C_LEAF_REPLAY, C_LEAF_LISTS, C_LEAF_ENTRIES, C_LEAF_SHARED, C_ERROR})
                         snap[c] = cur[c];
                 }
                 CUDA_TRY(cudaMemcpyAsync(d_counters.p, snap, sizeof snap, cudaMemcpyHostToDevice, st));
@@ -1678,6 +1747,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     res->stats.suspensions = suspensions;
     res->stats.search_rounds = search_rounds;
     res->stats.row_splits = row_splits;
+    res->stats.leaf_shared = (int64_t)counters[C_LEAF_SHARED];
 #if PJG_SEARCH_PROF
     if (d_prof.p) write_search_profile(d_prof.p, st, res->stats);
 #endif
@@ -1698,6 +1768,8 @@ done:
         dfree(d_susp_a, st); dfree(d_susp_b, st); dfree(d_pool_a, st); dfree(d_pool_b, st); dfree(d_pool_used, st);
         dfree(d_prof, st);
         dfree(d_fill_state, st); dfree(d_fill_work, st); dfree(d_nfill, st);
+        dfree(d_ls_key, st); dfree(d_ls_n, st); dfree(d_ls_rep, st); dfree(d_ls_slot, st);
+        dfree(d_ls_rep_work, st); dfree(d_ls_dup, st); dfree(d_ls_left, st); dfree(d_ls_ok, st);
         for (auto &b : scan_tmp) dfree(b, st);
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);

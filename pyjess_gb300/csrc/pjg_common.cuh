@@ -142,6 +142,7 @@ enum Counter : int {
                       // small, 3 time budget exhausted, 4 leaf order: too many
                       // small subtrees, 5 a partition did not converge, 6 an
                       // inconsistent node partition (0 = none)
+    C_LEAF_SHARED,    // requested lists sharing another list's leaf order
     C_NUM
 };
 

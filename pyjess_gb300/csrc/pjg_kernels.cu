@@ -885,7 +885,7 @@ __global__ void __launch_bounds__(WARPS * 32)
                 unsigned long long *exact_count, unsigned long long *counters, int take_max, const int64_t *work,
                 const unsigned long long *n_work, int64_t *fwd_list0, unsigned long long *fwd_count0,
                 int fwd_max0, int64_t *fwd_list1, unsigned long long *fwd_count1, int fwd_max1,
-                int count_lists) {
+                int count_lists, uint8_t *part_ok) {
     extern __shared__ __align__(16) unsigned char part_smem[];
     PartWarp<CAP> &L = reinterpret_cast<PartWarp<CAP> *>(part_smem)[threadIdx.x >> 5];
     const int lane = lane_id();
@@ -1064,6 +1064,7 @@ __global__ void __launch_bounds__(WARPS * 32)
                         blk_hi[bo + r / CULL_BLK] = make_float4(mxx, mxy, mxz, 0.f);
                     }
                 }
+                if (part_ok && lane == 0) part_ok[w] = 1;
                 __syncwarp();
 #if PJG_SEARCH_PROF
                 {
@@ -1102,6 +1103,172 @@ __global__ void __launch_bounds__(WARPS * 32)
     if (lane == 0 && n_sorted) atomicAdd(&counters[C_LEAF_SORTED], n_sorted);
     if (lane == 0 && n_lists) atomicAdd(&counters[C_LEAF_LISTS], n_lists);
     if (lane == 0 && n_entries) atomicAdd(&counters[C_LEAF_ENTRIES], n_entries);
+}
+
+// ---------------------------------------------------------------------------
+// Lists with the same atoms share one kd leaf order.
+//
+// The candidate lists of one structure are built per template-atom
+// signature, and different signatures often select the same atoms (an
+// extra residue name with no atom of the listed name in it, the residue
+// names in another order, ...).  A leaf order without a median tie depends
+// only on the set of atoms (k_leaf_part's splits read nothing else), and
+// any leaf order depends only on the candidate sequence, so each requested
+// list is keyed by (structure, length, a hash of its atom set), the first
+// list to claim a key is ordered, and every other list with that key takes
+// the representative's leaves and blocks -- after checking that its
+// sequence is the representative's, or that its set is and the
+// representative was ordered without a tie.  Lists failing the check are
+// ordered on their own.  Candidate lists never repeat an atom, so equal
+// lengths and inclusion make equal sets.
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    // the splitmix64 output function (Steele, Lea and Flood, 2014)
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+__global__ void k_list_keys(int32_t n_sigs, const int32_t *count, const int64_t *offset, const int32_t *cand_atom,
+                            const int64_t *work, const unsigned long long *n_work, ListShare ls,
+                            unsigned long long *counters) {
+    const int lane = lane_id();
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t total = (int64_t)*n_work;
+    unsigned long long n_lists = 0, n_entries = 0;
+    for (int64_t item = warp; item < total; item += nwarps) {
+        const int64_t w = work[item];
+        const int m = count[w];
+        const int32_t *ca = cand_atom + offset[w];
+        // two order-independent sums of mixed atom indices
+        unsigned long long h1 = 0, h2 = 0;
+        for (int i = lane; i < m; i += 32) {
+            const unsigned long long a = (unsigned long long)(uint32_t)ca[i];
+            h1 += mix64(a + 0x9e3779b97f4a7c15ull);
+            h2 += mix64(a * 0xd6e8feb86659fd93ull + 0x632be59bd9b4e019ull);
+        }
+        for (int o = 16; o; o >>= 1) {
+            h1 += __shfl_xor_sync(FULL_MASK, h1, o);
+            h2 += __shfl_xor_sync(FULL_MASK, h2, o);
+        }
+        const unsigned long long key =
+            mix64(h1 ^ ((h2 << 29) | (h2 >> 35)) ^ ((unsigned long long)(w / n_sigs) << 40) ^ (unsigned long long)m) |
+            1ull;
+        if (lane == 0) {
+            // linear probing, at most one lap (the table holds twice the
+            // chunk's lists, so it never fills)
+            int64_t sl = (int64_t)(key & (unsigned long long)ls.mask), found = -1;
+            for (int64_t it = 0; it <= ls.mask; it++) {
+                const unsigned long long prev = atomicCAS(&ls.key[sl], 0ull, key);
+                if (prev == 0ull || prev == key) {
+                    found = sl;
+                    break;
+                }
+                sl = (sl + 1) & ls.mask;
+            }
+            if (found >= 0) atomicCAS(&ls.rep[found], -1, (int32_t)w);
+            ls.slot[item] = (int32_t)found;
+            n_lists++;
+            n_entries += (unsigned long long)(m > 0 ? m : 0);
+        }
+    }
+    if (lane == 0 && n_lists) atomicAdd(&counters[C_LEAF_LISTS], n_lists);
+    if (lane == 0 && n_entries) atomicAdd(&counters[C_LEAF_ENTRIES], n_entries);
+}
+
+__global__ void k_list_reps(const int64_t *work, const unsigned long long *n_work, ListShare ls) {
+    const int lane = lane_id();
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t total = (int64_t)*n_work;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    // whole warps step through the items (warp-aggregated appends)
+    for (int64_t i0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) & ~31ll; i0 < total; i0 += stride) {
+        const int64_t item = i0 + lane;
+        const bool valid = item < total;
+        int64_t w = 0;
+        int32_t r = -1;
+        if (valid) {
+            w = work[item];
+            const int32_t sl = ls.slot[item];
+            r = sl >= 0 ? ls.rep[sl] : -1;
+        }
+        const bool own = valid && (r < 0 || (int64_t)r == w);
+        const bool dup = valid && !own;
+        const unsigned mo = __ballot_sync(FULL_MASK, own), md = __ballot_sync(FULL_MASK, dup);
+        unsigned long long bo = 0, bd = 0;
+        if (lane == 0) {
+            if (mo) bo = atomicAdd(&ls.n[0], (unsigned long long)__popc(mo));
+            if (md) bd = atomicAdd(&ls.n[1], (unsigned long long)__popc(md));
+        }
+        bo = __shfl_sync(FULL_MASK, bo, 0);
+        bd = __shfl_sync(FULL_MASK, bd, 0);
+        if (own) ls.rep_work[bo + __popc(mo & lt)] = w;
+        if (dup) ls.dup_work[bd + __popc(md & lt)] = (w << 32) | (int64_t)(uint32_t)r;
+    }
+}
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+    k_list_share(ChunkView cv, int32_t n_sigs, const int32_t *count, const int64_t *offset,
+                 const int32_t *cand_atom, int64_t *leaf_offset, int64_t *blk_offset, ListShare ls,
+                 unsigned long long *counters) {
+    __shared__ uint32_t bits[WARPS][LEAF_SORT_WORDS];
+    constexpr int WB = 32 * LEAF_SORT_WORDS;
+    const int lane = lane_id();
+    uint32_t *B = bits[threadIdx.x >> 5];
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t total = (int64_t)ls.n[1];
+    unsigned long long n_shared = 0;
+    for (int64_t i = warp; i < total; i += nwarps) {
+        const int64_t v = ls.dup_work[i];
+        const int64_t w = v >> 32, r = (int64_t)(uint32_t)(v & 0xFFFFFFFFll);
+        const int m = count[w];
+        const int s = (int)(w / n_sigs);
+        bool same = count[r] == m && (int)(r / n_sigs) == s;
+        const int32_t *cw = cand_atom + offset[w], *cr = cand_atom + offset[r];
+        bool seq = same;
+        if (same) {
+            bool eq = true;
+            for (int k = lane; k < m; k += 32) eq &= cw[k] == cr[k];
+            seq = __all_sync(FULL_MASK, eq);
+        }
+        if (same && !seq) {
+            // the same set: every atom of w marked by r, one window of the
+            // structure's atom indices at a time
+            same = ls.part_ok[r] != 0;
+            const int natoms = cv.atom_count[s];
+            for (int wb = 0; wb < natoms && same; wb += WB) {
+                const int nwords = min(LEAF_SORT_WORDS, (natoms - wb + 31) >> 5);
+                for (int q = lane; q < nwords; q += 32) B[q] = 0u;
+                __syncwarp();
+                for (int k = lane; k < m; k += 32) {
+                    const uint32_t u = (uint32_t)cr[k] - (uint32_t)wb;
+                    if (u < (uint32_t)WB) atomicOr(&B[u >> 5], 1u << (u & 31));
+                }
+                __syncwarp();
+                bool in = true;
+                for (int k = lane; k < m; k += 32) {
+                    const uint32_t u = (uint32_t)cw[k] - (uint32_t)wb;
+                    if (u < (uint32_t)WB) in &= ((B[u >> 5] >> (u & 31)) & 1u) != 0u;
+                }
+                same = __all_sync(FULL_MASK, in);
+                __syncwarp();
+            }
+        }
+        if (lane == 0) {
+            if (same) {
+                leaf_offset[w] = leaf_offset[r];
+                blk_offset[w] = blk_offset[r];
+                n_shared++;
+            } else {
+                ls.left_work[atomicAdd(&ls.n[2], 1ull)] = w;
+            }
+        }
+        __syncwarp();
+    }
+    if (lane == 0 && n_shared) atomicAdd(&counters[C_LEAF_SHARED], n_shared);
 }
 
 // Exact replay for the lists k_leaf_order could not order by ranks (a tie
@@ -3745,7 +3912,8 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
                        const int64_t *leaf_offset, int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
                        int64_t *sorted_list, unsigned long long *sorted_count, int64_t list_cap,
                        int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters,
-                       const int64_t *work, const unsigned long long *n_work, int rank_max) {
+                       const int64_t *work, const unsigned long long *n_work, int rank_max, uint8_t *part_ok,
+                       int count_lists) {
     cudaMemsetAsync(sorted_count, 0, LEAF_LISTS * sizeof(unsigned long long), st);
     cudaMemsetAsync(exact_count, 0, sizeof(unsigned long long), st);
     rank_max = rank_max < 1 ? 1 : rank_max > LEAF_FAST_MAX ? LEAF_FAST_MAX : rank_max;
@@ -3760,7 +3928,8 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
     k_leaf_order<LEAF_FAST_MAX, LEAF_WARPS><<<blocks, LEAF_WARPS * 32, 0, st>>>(
         cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset, leaf_atom, leaf_xyz, blk_lo, blk_hi,
         sorted_list, sorted_count, list_cap, exact_list, exact_count, counters, rank_max, work, n_work, mid_list,
-        mid_count, LEAF_MID_MAX, 1);
+        mid_count, LEAF_MID_MAX, count_lists);
+    (void)part_ok;
     k_leaf_order<LEAF_MID_MAX, 2><<<sms * 8, 64, 0, st>>>(
         cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset, leaf_atom, leaf_xyz, blk_lo, blk_hi,
         sorted_list, sorted_count, list_cap, exact_list, exact_count, counters, LEAF_MID_MAX, mid_list, mid_count,
@@ -3785,7 +3954,8 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
         k_leaf_part<256, 4><<<g, 128, SP, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset,
                                                 leaf_atom, leaf_xyz, blk_lo, blk_hi, sorted_list, sorted_count,
                                                 list_cap, exact_list, exact_count, counters, rank_max, work, n_work,
-                                                list512, count512, 512, list1024, count1024, 1024, 1);
+                                                list512, count512, 512, list1024, count1024, 1024, count_lists,
+                                                part_ok);
     }
     {
         constexpr int SP = (int)sizeof(PartWarp<512>) * 4;
@@ -3793,7 +3963,7 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
         k_leaf_part<512, 4><<<g, 128, SP, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset,
                                                 leaf_atom, leaf_xyz, blk_lo, blk_hi, sorted_list, sorted_count,
                                                 list_cap, exact_list, exact_count, counters, 512, list512, count512,
-                                                nullptr, nullptr, 0, nullptr, nullptr, 0, 0);
+                                                nullptr, nullptr, 0, nullptr, nullptr, 0, 0, part_ok);
     }
     {
         constexpr int SP = (int)sizeof(PartWarp<1024>) * 2;
@@ -3801,7 +3971,7 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
         k_leaf_part<1024, 2><<<g, 64, SP, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset,
                                                 leaf_atom, leaf_xyz, blk_lo, blk_hi, sorted_list, sorted_count,
                                                 list_cap, exact_list, exact_count, counters, 1024, list1024,
-                                                count1024, nullptr, nullptr, 0, nullptr, nullptr, 0, 0);
+                                                count1024, nullptr, nullptr, 0, nullptr, nullptr, 0, 0, part_ok);
     }
 #endif
     // sorted-axis split, one worklist per size class: up to 512 entries
@@ -3851,6 +4021,24 @@ void launch_demand_levels(cudaStream_t st, int blocks, const TemplateView &tv, c
     // (also with max_level 0: the pairs of templates over 32 atoms request
     // every list here)
     if (n_pairs > 0) k_demand_levels<<<blocks, 256, 0, st>>>(tv, cd, n_pairs, max_level, reorder, dm);
+}
+
+void launch_list_keys(cudaStream_t st, int blocks, int32_t n_sigs, const int32_t *count, const int64_t *offset,
+                      const int32_t *cand_atom, const int64_t *work, const unsigned long long *n_work,
+                      const ListShare &ls, unsigned long long *counters) {
+    k_list_keys<<<blocks, 256, 0, st>>>(n_sigs, count, offset, cand_atom, work, n_work, ls, counters);
+}
+
+void launch_list_reps(cudaStream_t st, int blocks, const int64_t *work, const unsigned long long *n_work,
+                      const ListShare &ls) {
+    k_list_reps<<<blocks, 256, 0, st>>>(work, n_work, ls);
+}
+
+void launch_list_share(cudaStream_t st, int blocks, const ChunkView &cv, int32_t n_sigs, const int32_t *count,
+                       const int64_t *offset, const int32_t *cand_atom, int64_t *leaf_offset, int64_t *blk_offset,
+                       const ListShare &ls, unsigned long long *counters) {
+    k_list_share<8><<<blocks, 256, 0, st>>>(cv, n_sigs, count, offset, cand_atom, leaf_offset, blk_offset, ls,
+                                            counters);
 }
 
 void launch_mark_ordered(cudaStream_t st, int blocks, const LeafDemand &dm) {

@@ -197,6 +197,25 @@ struct LeafDemand {
     unsigned long long *n_fill;
 };
 
+// Requested lists whose candidate atoms are the same share one kd leaf
+// order: a table of list keys (structure, length, hash of the atom set) for
+// the chunk, and the worklists of one ordering round.
+struct ListShare {
+    unsigned long long *key;       // [mask + 1] table keys (0: empty slot)
+    int32_t *rep;                  // [mask + 1] the list ordered for the key
+                                   //   (-1: none yet; the first to claim it)
+    int64_t mask;                  // table size - 1 (a power of two)
+    int32_t *slot;                 // [requested lists] table slot of each (-1:
+                                   //   table full, ordered on its own)
+    int64_t *rep_work;             // lists ordered in this round
+    int64_t *dup_work;             // lists sharing another's order: list << 32 | rep
+    int64_t *left_work;            // shared lists whose atoms turned out to
+                                   //   differ: ordered on their own
+    unsigned long long *n;         // [3] lengths of the three worklists
+    uint8_t *part_ok;              // [lists] ordered by k_leaf_part (no median
+                                   //   tie: the order depends on the set only)
+};
+
 // Complete assignments written by k_search.
 struct CompleteRows {
     unsigned long long *count;
@@ -272,7 +291,22 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
                        const int64_t *leaf_offset, int32_t *leaf_atom, float4 *leaf_xyz, float4 *blk_lo, float4 *blk_hi,
                        int64_t *sorted_list, unsigned long long *sorted_count, int64_t list_cap,
                        int64_t *exact_list, unsigned long long *exact_count, unsigned long long *counters,
-                       const int64_t *work, const unsigned long long *n_work, int rank_max);
+                       const int64_t *work, const unsigned long long *n_work, int rank_max,
+                       uint8_t *part_ok = nullptr, int count_lists = 1);
+
+// list sharing, around the leaf-order launches of a round: keys of the
+// requested lists into the table (and the lists / entries counters), the
+// split into lists to order and lists sharing another's order, and after
+// the ordering the shared lists pointed at their representatives' leaves and
+// blocks once their atoms are checked equal (else queued in left_work)
+void launch_list_keys(cudaStream_t st, int blocks, int32_t n_sigs, const int32_t *count, const int64_t *offset,
+                      const int32_t *cand_atom, const int64_t *work, const unsigned long long *n_work,
+                      const ListShare &ls, unsigned long long *counters);
+void launch_list_reps(cudaStream_t st, int blocks, const int64_t *work, const unsigned long long *n_work,
+                      const ListShare &ls);
+void launch_list_share(cudaStream_t st, int blocks, const ChunkView &cv, int32_t n_sigs, const int32_t *count,
+                       const int64_t *offset, const int32_t *cand_atom, int64_t *leaf_offset, int64_t *blk_offset,
+                       const ListShare &ls, unsigned long long *counters);
 
 // requests (LeafDemand) the lists of levels 1 .. max_level of every pair
 // of the chunk that has no empty candidate list

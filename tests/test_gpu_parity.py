@@ -334,6 +334,33 @@ def test_leaf_order_on_demand_config3(monkeypatch, levels, pool):
 
 
 @pytest.mark.parametrize("pool", POOLS)
+@pytest.mark.parametrize("levels", [4, 1])
+def test_list_sharing(monkeypatch, levels, pool):
+    """Requested lists of one structure with the same atoms share one leaf
+    order (the default; PJG_LIST_SHARING=0 orders every list itself).  The
+    workload's templates list extra residue names in random order, so lists
+    share by equal sequences and by equal sets in another order; both runs
+    give the oracle's hits, bit for bit the same arrays."""
+    from pyjess_gb300 import workloads as W
+
+    monkeypatch.setenv("PJG_LEAF_LEVELS", str(levels))
+    set_pool(monkeypatch, pool)
+    wl = W.config(3, n_structures=30, n_templates=300)
+    res, _ = compare(wl.templates, wl.structures, mode="fp32", **wl.params)
+    st = res.stats()
+    assert 0 < st["leaf_shared"] < st["leaf_lists"]
+    monkeypatch.setenv("PJG_LIST_SHARING", "0")
+    res0, _ = compare(wl.templates, wl.structures, mode="fp32", **wl.params)
+    st0 = res0.stats()
+    assert st0["leaf_shared"] == 0 and st0["leaf_lists"] == st["leaf_lists"]
+    a, b = res.arrays(), res0.arrays()
+    assert a["count"] == b["count"]
+    for k in a:
+        if k != "count":
+            assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("pool", POOLS)
 @pytest.mark.parametrize("levels", [0, 1])
 @pytest.mark.parametrize("best", [False, True])
 def test_leaf_order_on_demand_cut(monkeypatch, levels, best, pool):
