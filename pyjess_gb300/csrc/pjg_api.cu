@@ -185,6 +185,10 @@ struct pjg_structures {
     int32_t *d_nh_begin = nullptr, *d_nh_count = nullptr;  // name histogram per bucket
     uint32_t *d_nh_name = nullptr;
     uint8_t *d_name_id = nullptr;                      // name index within the bucket
+    // per distinct name of a bucket: where its atoms start (structure-local)
+    // in nh_pos, which holds every structure's atoms grouped by (bucket,
+    // name), each group in ResIndex order
+    int32_t *d_nh_off = nullptr, *d_nh_pos = nullptr;
     int device = 0;
 };
 
@@ -549,6 +553,7 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
     HostArray<uint32_t> name((size_t)N), resname((size_t)N);
     HostArray<int32_t> sorted((size_t)N);
     HostArray<uint8_t> name_id((size_t)N);
+    HostArray<int32_t> nh_pos((size_t)N);
     std::vector<int32_t> bucket_begin{0}, bucket_lo, bucket_hi;
     std::vector<uint32_t> bucket_name;
     for (int s = 0; s < S; s++) {
@@ -573,6 +578,7 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
         std::vector<int32_t> lo, hi;
         std::vector<uint32_t> hname;  // distinct atom names of each bucket, sorted
         std::vector<int32_t> hcount, hbegin{0};
+        std::vector<int32_t> hoff;    // start of each distinct name's atoms in nh_pos (structure-local)
         double radius = 0.0;
         int64_t bad = -1;  // first atom with a non-finite coordinate
     };
@@ -663,11 +669,20 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
                 B.hcount.back()++;
             }
             B.hbegin.push_back((int32_t)B.hname.size());
+            // the bucket's atoms grouped by name (groups in name order, each
+            // in ResIndex order), from the bucket's first position
+            std::vector<int32_t> fill(B.hname.size() - h0);
+            for (size_t j = 0, acc = (size_t)B.lo[k]; j < fill.size(); j++) {
+                fill[j] = (int32_t)acc;
+                B.hoff.push_back((int32_t)acc);
+                acc += (size_t)B.hcount[h0 + j];
+            }
             for (int i = B.lo[k]; i < B.hi[k]; i++) {
                 const int a = idx[i];
                 const size_t id = std::lower_bound(B.hname.begin() + h0, B.hname.end(), name[b0 + a]) -
                                   (B.hname.begin() + h0);
                 name_id[b0 + a] = (uint8_t)std::min<size_t>(id, 255);
+                nh_pos[b0 + fill[id]++] = a;
             }
         }
     };
@@ -687,13 +702,14 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
             delete h;
             return fail(PJG_ERR_INVALID, "structure %d atom %lld: non-finite coordinate", s, (long long)bk[s].bad);
         }
-    std::vector<int32_t> nh_begin{0}, nh_count;
+    std::vector<int32_t> nh_begin{0}, nh_count, nh_off;
     std::vector<uint32_t> nh_name;
     for (int s = 0; s < S; s++) {
         const Buckets &B = bk[s];
         for (size_t k = 0; k + 1 < B.hbegin.size(); k++) nh_begin.push_back((int32_t)nh_name.size() + B.hbegin[k + 1]);
         nh_name.insert(nh_name.end(), B.hname.begin(), B.hname.end());
         nh_count.insert(nh_count.end(), B.hcount.begin(), B.hcount.end());
+        nh_off.insert(nh_off.end(), B.hoff.begin(), B.hoff.end());
     }
     for (int s = 0; s < S; s++) {
         const Buckets &B = bk[s];
@@ -721,6 +737,8 @@ pjg_status pjg_structures_create(const pjg_structure_set *set, pjg_structures **
     if (e == cudaSuccess) e = upload(&h->d_nh_name, nh_name);
     if (e == cudaSuccess) e = upload(&h->d_nh_count, nh_count);
     if (e == cudaSuccess) e = upload(&h->d_name_id, name_id.p.get(), (size_t)N);
+    if (e == cudaSuccess) e = upload(&h->d_nh_off, nh_off);
+    if (e == cudaSuccess) e = upload(&h->d_nh_pos, nh_pos.p.get(), (size_t)N);
     if (e == cudaSuccess) {
         // axis ranks of every atom (the leaf-order sorted-axis path)
         const size_t n3 = 3 * (size_t)std::max<int64_t>(N, 1);
@@ -753,7 +771,8 @@ void pjg_structures_destroy(pjg_structures *h) {
     if (!h) return;
     void *ptrs[] = {h->d_atom_base, h->d_atom_count, h->d_xyz64, h->d_xyz32, h->d_name, h->d_resname,
                     h->d_sorted, h->d_bucket_begin, h->d_bucket_name, h->d_bucket_lo, h->d_bucket_hi,
-                    h->d_lrank, h->d_urank, h->d_nh_begin, h->d_nh_name, h->d_nh_count, h->d_name_id};
+                    h->d_lrank, h->d_urank, h->d_nh_begin, h->d_nh_name, h->d_nh_count, h->d_name_id,
+                    h->d_nh_off, h->d_nh_pos};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete h;
@@ -1060,7 +1079,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
         ChunkView cv{S, sp->d_atom_base, sp->d_atom_count, sp->d_xyz64, sp->d_xyz32, sp->d_name, sp->d_resname,
                      sp->d_sorted, sp->d_bucket_begin, sp->d_bucket_name, sp->d_bucket_lo, sp->d_bucket_hi,
                      sp->N, sp->d_lrank, sp->d_urank, sp->d_nh_begin, sp->d_nh_name, sp->d_nh_count,
-                     sp->d_name_id};
+                     sp->d_name_id, sp->d_nh_off, sp->d_nh_pos};
         SigView sv{G, tp->d_code, tp->d_rule, tp->d_mainchain, tp->d_name_begin, tp->d_names, tp->d_res_begin,
                    tp->d_resnames, tp->d_partner_begin, tp->d_partner_res, tp->d_partner_name};
         int blocks = (int)std::min<int64_t>((W + 7) / 8, (int64_t)sm_count() * 32);
@@ -1180,7 +1199,7 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
             ChunkView cv{Sc, sp->d_atom_base + s0, sp->d_atom_count + s0, sp->d_xyz64, sp->d_xyz32, sp->d_name,
                          sp->d_resname, sp->d_sorted, sp->d_bucket_begin + s0, sp->d_bucket_name, sp->d_bucket_lo,
                          sp->d_bucket_hi, sp->N, sp->d_lrank, sp->d_urank, sp->d_nh_begin, sp->d_nh_name,
-                         sp->d_nh_count, sp->d_name_id};
+                         sp->d_nh_count, sp->d_name_id, sp->d_nh_off, sp->d_nh_pos};
             SigView sv{G, tp->d_code, tp->d_rule, tp->d_mainchain, tp->d_name_begin, tp->d_names, tp->d_res_begin,
                        tp->d_resnames, tp->d_partner_begin, tp->d_partner_res, tp->d_partner_name};
             int32_t *cnt_c = d_count.p + (int64_t)s0 * G;

@@ -78,6 +78,11 @@ struct ChunkView {
     const int32_t *nh_count;
     const uint8_t *name_id;       // per atom: index of its name among its
                                   // bucket's distinct names (255 past 254)
+    // per distinct name of a bucket (same indexing as nh_name): start of its
+    // atoms in nh_pos, structure-local; nh_pos holds each structure's atoms
+    // grouped by (bucket, name), each group in ResIndex order
+    const int32_t *nh_off;
+    const int32_t *nh_pos;
 };
 
 struct SigView {

@@ -261,6 +261,16 @@ __global__ void k_candidates(ChunkView cv, SigView sv, const int64_t *offset, in
                     (uint64_t)__ballot_sync(FULL_MASK, m0) | ((uint64_t)__ballot_sync(FULL_MASK, m1) << 32);
                 const int p_lo = cv.bucket_lo[found], p_hi = cv.bucket_hi[found];
                 if (!mask) continue;
+                if (__popcll((long long)mask) == 1) {
+                    // one passing name: its atoms, already grouped in
+                    // ResIndex order, copied as they are
+                    const int q = nb + __ffsll((long long)mask) - 1;
+                    const int cq = cv.nh_count[q];
+                    const int32_t *src = cv.nh_pos + abase + cv.nh_off[q];
+                    for (int i = lane; i < cq; i += 32) cand_atom[out0 + cnt + i] = src[i];
+                    cnt += cq;
+                    continue;
+                }
                 for (int p0 = p_lo; p0 < p_hi; p0 += 32) {
                     const int p = p0 + lane;
                     int atom = 0;
@@ -285,14 +295,14 @@ __global__ void k_candidates(ChunkView cv, SigView sv, const int64_t *offset, in
 // depends only on its (residue name, atom name) and the signature, so a
 // list's length is the sum, over the distinct atom names of each residue
 // bucket it walks, of the counts of the names that pass the rule (the
-// molecule-order codes walk every bucket of the structure).  Warp per
-// (structure, signature), lanes over a bucket's distinct names.
+// molecule-order codes walk every bucket of the structure).  Thread per
+// (structure, signature): consecutive threads take consecutive signatures of
+// one structure, so the structure's bucket tables are read by the whole warp
+// at once.
 __global__ void k_candidate_counts(ChunkView cv, SigView sv, int32_t *count, int32_t *scanned) {
-    const int lane = lane_id();
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int64_t total = (int64_t)cv.n_structures * sv.n_sigs;
-    for (int64_t w = warp; w < total; w += nwarps) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < total; w += stride) {
         const int s = (int)(w / sv.n_sigs);
         const int g = (int)(w % sv.n_sigs);
         const int code = sv.code[g];
@@ -300,34 +310,25 @@ __global__ void k_candidate_counts(ChunkView cv, SigView sv, int32_t *count, int
         const int b0 = cv.bucket_begin[s], b1 = cv.bucket_begin[s + 1];
         int cnt = 0, sc = 0;
         auto bucket_sum = [&](int b, uint32_t rn) {
-            for (int q = cv.nh_begin[b] + lane; q < cv.nh_begin[b + 1]; q += 32)
+            const int q1 = cv.nh_begin[b + 1];
+            for (int q = cv.nh_begin[b]; q < q1; q++)
                 if (sig_match_regs(sv, sr, cv.nh_name[q], rn)) cnt += cv.nh_count[q];
         };
         if (code >= -1 && code <= 8) {
             for (int ri = sv.res_begin[g]; ri < sv.res_begin[g + 1]; ri++) {
                 const uint32_t rn = sv.resnames[ri];
-                int found = -1;
-                for (int bb = b0; bb < b1; bb += 32) {
-                    const int b = bb + lane;
-                    const unsigned m = __ballot_sync(FULL_MASK, b < b1 && cv.bucket_name[b] == rn);
-                    if (m) {
-                        found = bb + __ffs(m) - 1;
-                        break;
-                    }
-                }
-                if (found < 0) continue;
-                bucket_sum(found, rn);
-                sc += cv.bucket_hi[found] - cv.bucket_lo[found];
+                int b = b0;
+                while (b < b1 && cv.bucket_name[b] != rn) b++;
+                if (b == b1) continue;
+                bucket_sum(b, rn);
+                sc += cv.bucket_hi[b] - cv.bucket_lo[b];
             }
         } else {
             for (int b = b0; b < b1; b++) bucket_sum(b, cv.bucket_name[b]);
             sc = cv.atom_count[s];
         }
-        for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(FULL_MASK, cnt, o);
-        if (lane == 0) {
-            count[w] = cnt;
-            scanned[w] = sc;
-        }
+        count[w] = cnt;
+        scanned[w] = sc;
     }
 }
 
@@ -3878,7 +3879,16 @@ void launch_candidates(cudaStream_t st, int blocks, bool fill, const ChunkView &
                        const int64_t *work, const unsigned long long *n_work, int32_t *fill_state, bool claim) {
     if (fill)
         k_candidates<<<blocks, 256, 0, st>>>(cv, sv, offset, cand_atom, work, n_work, fill_state, claim ? 1 : 0);
-    else k_candidate_counts<<<blocks, 256, 0, st>>>(cv, sv, count, scanned);
+    else {
+        // thread per list
+        const int64_t n = (int64_t)cv.n_structures * sv.n_sigs;
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int cb = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sms * 8));
+        (void)blocks;
+        k_candidate_counts<<<cb, 256, 0, st>>>(cv, sv, count, scanned);
+    }
 }
 
 void launch_scan_tiles_i32(cudaStream_t st, const int32_t *in, int64_t n, int64_t *out, int64_t *tile_sums) {
