@@ -3101,9 +3101,7 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                         const unsigned m = __ballot_sync(FULL_MASK, pass);
                         SPROF_ADD(SP_CHILD_BLOCK, __popc(m));
                         if (last) {
-                            int32_t pos[32];
-                            for (int j = 0; j <= lev; j++) pos[j] = st.cpos[j];
-                            emit(pass, pos, cr);
+                            emit(pass, st.cpos, cr);
                         } else if (pass) {
                             E e;
                             e.pos = (PosT)cr;
@@ -3275,18 +3273,18 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                     }
 #endif
                     if (valid) {
-                        int idx = p;
-                        for (int j = lev; j >= 0; j--) {
-                            E e = tiles[st.tile[j] + idx];
-                            chainpos[j] = (int)e.pos;
-                            idx = e.parent;
-                        }
-                        float4 xc = cd.leaf_xyz[coff + cr];
-                        int32_t kn = __float_as_int(xc.w);
+                        // the parent chain walked up from the parent, each
+                        // level tested as it is reached (the first failing
+                        // test ends the walk)
+                        const float4 xc = cd.leaf_xyz[coff + cr];
+                        const int32_t kn = __float_as_int(xc.w);
                         pass = true;
                         unsigned exact = 0;
-                        for (int j = 0; j <= lev; j++) {
-                            float4 xj = level_xyz(j, chainpos[j]);
+                        int idx = p;
+                        for (int j = lev; j >= 0; j--) {
+                            const E e = tiles[st.tile[j] + idx];
+                            idx = e.parent;
+                            const float4 xj = level_xyz(j, (int)e.pos);
                             if (!check_pair(__float_as_int(xj.w), kn, st.tkey[j], tn, sa.ignore_chain)) {
                                 pass = false;
                                 break;
@@ -3302,6 +3300,16 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
                                 if (!(d2 >= th.y && d2 <= th.z)) exact |= 1u << j;
                             } else {
                                 exact |= 1u << j;
+                            }
+                        }
+                        if (pass && (last || exact)) {
+                            // positions of the chain (passing lanes): the
+                            // row's atoms, the FP64 recheck
+                            int ix = p;
+                            for (int j = lev; j >= 0; j--) {
+                                const E e = tiles[st.tile[j] + ix];
+                                chainpos[j] = (int)e.pos;
+                                ix = e.parent;
                             }
                         }
                         if (pass && exact) {
