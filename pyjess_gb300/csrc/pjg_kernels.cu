@@ -1138,25 +1138,35 @@ __global__ void k_list_keys(int32_t n_sigs, const int32_t *count, const int64_t 
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int64_t total = (int64_t)*n_work;
     unsigned long long n_lists = 0, n_entries = 0;
-    for (int64_t item = warp; item < total; item += nwarps) {
-        const int64_t w = work[item];
-        const int m = count[w];
-        const int32_t *ca = cand_atom + offset[w];
-        // two order-independent sums of mixed atom indices
-        unsigned long long h1 = 0, h2 = 0;
-        for (int i = lane; i < m; i += 32) {
-            const unsigned long long a = (unsigned long long)(uint32_t)ca[i];
-            h1 += mix64(a + 0x9e3779b97f4a7c15ull);
-            h2 += mix64(a * 0xd6e8feb86659fd93ull + 0x632be59bd9b4e019ull);
+    // 32 consecutive items a warp: the lists hashed one after the other by
+    // the whole warp, then every lane inserts its own list's key
+    for (int64_t base = warp * 32; base < total; base += nwarps * 32) {
+        const int64_t item = base + lane;
+        const bool valid = item < total;
+        const int64_t w = valid ? work[item] : 0;
+        const int m = valid ? count[w] : 0;
+        const int64_t off = valid ? offset[w] : 0;
+        unsigned long long key = 0;
+        const int nt = total - base < 32 ? (int)(total - base) : 32;
+        for (int t = 0; t < nt; t++) {
+            const int mt = __shfl_sync(FULL_MASK, m, t);
+            const int64_t ot = __shfl_sync(FULL_MASK, off, t);
+            const int32_t *ca = cand_atom + ot;
+            // two order-independent sums of mixed atom indices
+            unsigned long long h1 = 0, h2 = 0;
+            for (int i = lane; i < mt; i += 32) {
+                const unsigned long long a = (unsigned long long)(uint32_t)ca[i];
+                h1 += mix64(a + 0x9e3779b97f4a7c15ull);
+                h2 += mix64(a * 0xd6e8feb86659fd93ull + 0x632be59bd9b4e019ull);
+            }
+            for (int o = 16; o; o >>= 1) {
+                h1 += __shfl_xor_sync(FULL_MASK, h1, o);
+                h2 += __shfl_xor_sync(FULL_MASK, h2, o);
+            }
+            if (lane == t) key = h1 ^ ((h2 << 29) | (h2 >> 35));
         }
-        for (int o = 16; o; o >>= 1) {
-            h1 += __shfl_xor_sync(FULL_MASK, h1, o);
-            h2 += __shfl_xor_sync(FULL_MASK, h2, o);
-        }
-        const unsigned long long key =
-            mix64(h1 ^ ((h2 << 29) | (h2 >> 35)) ^ ((unsigned long long)(w / n_sigs) << 40) ^ (unsigned long long)m) |
-            1ull;
-        if (lane == 0) {
+        if (valid) {
+            key = mix64(key ^ ((unsigned long long)(w / n_sigs) << 40) ^ (unsigned long long)m) | 1ull;
             // linear probing, at most one lap (the table holds twice the
             // chunk's lists, so it never fills)
             int64_t sl = (int64_t)(key & (unsigned long long)ls.mask), found = -1;
@@ -1173,6 +1183,10 @@ __global__ void k_list_keys(int32_t n_sigs, const int32_t *count, const int64_t 
             n_lists++;
             n_entries += (unsigned long long)(m > 0 ? m : 0);
         }
+    }
+    for (int o = 16; o; o >>= 1) {
+        n_lists += __shfl_xor_sync(FULL_MASK, n_lists, o);
+        n_entries += __shfl_xor_sync(FULL_MASK, n_entries, o);
     }
     if (lane == 0 && n_lists) atomicAdd(&counters[C_LEAF_LISTS], n_lists);
     if (lane == 0 && n_entries) atomicAdd(&counters[C_LEAF_ENTRIES], n_entries);
@@ -2032,74 +2046,148 @@ __device__ __forceinline__ void request_list(const LeafDemand &dm, int64_t w, in
     }
 }
 
+// Warp-wide forms of request_fill / request_list, called by every lane of
+// the warp: the lists a lane wins (state 0 -> 1) get their leaf-array ranges
+// and worklist places from one atomic add per warp.
+__device__ __forceinline__ void request_fill_warp(const LeafDemand &dm, bool want, int64_t w) {
+    const int lane = lane_id();
+    const bool win =
+        want && dm.fill_state && dm.fill_state[w] == 0 && atomicCAS(&dm.fill_state[w], 0, 1) == 0;
+    const unsigned wm = __ballot_sync(FULL_MASK, win);
+    if (!wm) return;
+    unsigned long long b = 0;
+    if (lane == 0) b = atomicAdd(dm.n_fill, (unsigned long long)__popc(wm));
+    b = __shfl_sync(FULL_MASK, b, 0);
+    if (win) dm.fill_work[b + __popc(wm & ((1u << lane) - 1u))] = w;
+}
+
+__device__ __forceinline__ void request_list_warp(const LeafDemand &dm, bool want, int64_t w, int m) {
+    const int lane = lane_id();
+    const bool win = want && dm.state[w] == 0 && atomicCAS(&dm.state[w], 0, 1) == 0;
+    const unsigned wm = __ballot_sync(FULL_MASK, win);
+    if (!wm) return;
+    const unsigned long long mm = win ? (unsigned long long)m : 0ull;
+    unsigned long long incl = mm;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(FULL_MASK, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const unsigned long long tot = __shfl_sync(FULL_MASK, incl, 31);
+    unsigned long long bo = 0, bw = 0;
+    if (lane == 0) {
+        bo = atomicAdd(dm.leaf_used, tot);
+        bw = atomicAdd(dm.n_work, (unsigned long long)__popc(wm));
+    }
+    bo = __shfl_sync(FULL_MASK, bo, 0);
+    bw = __shfl_sync(FULL_MASK, bw, 0);
+    if (win) {
+        dm.leaf_offset[w] = (int64_t)(bo + incl - mm);
+        dm.work[bw + __popc(wm & ((1u << lane) - 1u))] = w;
+    }
+}
+
 // Lists needed before the search starts: a pair with no empty candidate
 // list reads the lists of levels 1, 2, ... in kd leaf order as its frontier
 // reaches them; the lists of the first `max_level` levels are requested
-// here (warp per pair, the level order of k_search), deeper ones by the
-// search itself when a pair first reaches them.
+// here (thread per pair, the level order of k_search), deeper ones by the
+// search itself when a pair first reaches them.  Consecutive threads take
+// consecutive templates of one structure.
 __global__ void k_demand_levels(TemplateView tv, CandView cd, int32_t n_pairs, int32_t max_level, int32_t reorder,
                                 LeafDemand dm) {
+    constexpr int TOP = 8;  // levels requested through the warp-wide path
     const int lane = lane_id();
     const int T = tv.n_templates, G = cd.n_sigs;
-    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t pair = warp; pair < n_pairs; pair += nwarps) {
-        const int s = (int)(pair / T), t = (int)(pair % T);
-        const int ab = tv.atom_begin[t];
-        const int n = tv.atom_begin[t + 1] - ab;
-        if (n < 1) continue;
-        if (n == 1) {
-            // a one-atom template reads its only list, in candidate order
-            const int64_t w = (int64_t)s * G + tv.sig[ab];
-            if (lane == 0 && cd.count[w] > 0) request_fill(dm, w);
-            continue;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) & ~31ll; base < n_pairs; base += stride) {
+        const int64_t pair = base + lane;
+        int n = 0, ab = 0;
+        int64_t wb = 0;
+        if (pair < n_pairs) {
+            const int s = (int)(pair / T), t = (int)(pair % T);
+            ab = tv.atom_begin[t];
+            n = tv.atom_begin[t + 1] - ab;
+            wb = (int64_t)s * G;
         }
-        if (n > 32) {
-            // k_search_large: every list but the level-0 one, before the
-            // search (those pairs never suspend)
+        // this pair's plan: levels 0..levels (-1: none) of atoms k_i
+        int levels = -1;
+        bool per_thread = false;
+        unsigned long long top[TOP];
+#pragma unroll
+        for (int i = 0; i < TOP; i++) top[i] = ~0ull;
+        if (n == 1) {
+            if (cd.count[wb + tv.sig[ab]] > 0) levels = 0;  // its only list, in candidate order
+            top[0] = 0;
+        } else if (n > 32) {
+            per_thread = true;  // k_search_large: every list, below
+        } else if (n >= 2) {
+            // the (max_level + 1) smallest (length, index) keys, sorted in
+            // registers
             bool empty = false;
-            int best = INT_MAX, best_k = 0;  // the level-0 atom: smallest (length, index)
-            for (int k = lane; k < n; k += 32) {
-                const int c = cd.count[(int64_t)s * G + tv.sig[ab + k]];
+            for (int k = 0; k < n; k++) {
+                const int c = cd.count[wb + tv.sig[ab + k]];
+                empty |= c == 0;
+                unsigned long long key = ((unsigned long long)(uint32_t)c << 5) | (unsigned long long)k;
+#pragma unroll
+                for (int i = 0; i < TOP; i++) {
+                    const unsigned long long lo = key < top[i] ? key : top[i];
+                    key = key < top[i] ? top[i] : key;
+                    top[i] = lo;
+                }
+            }
+            if (!empty) {
+                levels = min(n - 1, max_level);
+                if (levels >= TOP) per_thread = true;
+            }
+        }
+        // levels 0..TOP-1, warp-wide (every lane takes every step)
+#pragma unroll
+        for (int i = 0; i < TOP; i++) {
+            const bool want = !per_thread && i <= levels;
+            const int k = !want ? 0 : (reorder ? (int)(top[i] & 31ull) : i);
+            const int64_t w = want ? wb + tv.sig[ab + k] : 0;
+            if (i == 0) request_fill_warp(dm, want, w);
+            else request_list_warp(dm, want, w, !want ? 0 : reorder ? (int)(top[i] >> 5) : cd.count[w]);
+        }
+        if (!per_thread) continue;
+        if (n > 32) {
+            // every list but the level-0 one, before the search (those pairs
+            // never suspend); the level-0 atom has the smallest (length,
+            // index)
+            bool empty = false;
+            int best = INT_MAX, best_k = 0;
+            for (int k = 0; k < n; k++) {
+                const int c = cd.count[wb + tv.sig[ab + k]];
                 if (c == 0) empty = true;
                 if (c < best) {
                     best = c;
                     best_k = k;
                 }
             }
-            if (__any_sync(FULL_MASK, empty)) continue;
-            for (int o = 16; o; o >>= 1) {
-                const int ob = __shfl_xor_sync(FULL_MASK, best, o), ok = __shfl_xor_sync(FULL_MASK, best_k, o);
-                if (ob < best || (ob == best && ok < best_k)) {
-                    best = ob;
-                    best_k = ok;
-                }
-            }
+            if (empty) continue;
             const int k0 = reorder ? best_k : 0;
-            for (int k = lane; k < n; k += 32) {
-                const int64_t w = (int64_t)s * G + tv.sig[ab + k];
+            for (int k = 0; k < n; k++) {
+                const int64_t w = wb + tv.sig[ab + k];
                 if (k != k0) request_list(dm, w, cd.count[w]);
                 else request_fill(dm, w);
             }
-            continue;
-        }
-        int c = INT_MAX;
-        int64_t w = 0;
-        if (lane < n) {
-            w = (int64_t)s * G + tv.sig[ab + lane];
-            c = cd.count[w];
-        }
-        if (__ballot_sync(FULL_MASK, lane < n && c == 0)) continue;
-        int rank = lane;
-        if (reorder) {
-            rank = 0;
-            for (int j = 0; j < n; j++) {
-                int cj = __shfl_sync(FULL_MASK, c, j);
-                if (cj < c || (cj == c && j < lane)) rank++;
+        } else {
+            // more levels than the register list holds: each atom's rank
+            // from the keys below its own
+            for (int k = 0; k < n; k++) {
+                const int64_t w = wb + tv.sig[ab + k];
+                const int c = cd.count[w];
+                int rank = k;
+                if (reorder) {
+                    rank = 0;
+                    for (int j = 0; j < n; j++) {
+                        const int cj = cd.count[wb + tv.sig[ab + j]];
+                        rank += (cj < c || (cj == c && j < k)) ? 1 : 0;
+                    }
+                }
+                if (rank == 0) request_fill(dm, w);
+                else if (rank <= max_level) request_list(dm, w, c);
             }
         }
-        if (lane < n && rank >= 1 && rank <= max_level) request_list(dm, w, c);
-        if (lane < n && rank == 0) request_fill(dm, w);
     }
 }
 
@@ -4038,7 +4126,13 @@ void launch_demand_levels(cudaStream_t st, int blocks, const TemplateView &tv, c
                           int32_t max_level, int32_t reorder, const LeafDemand &dm) {
     // (also with max_level 0: the pairs of templates over 32 atoms request
     // every list here)
-    if (n_pairs > 0) k_demand_levels<<<blocks, 256, 0, st>>>(tv, cd, n_pairs, max_level, reorder, dm);
+    // thread per pair
+    (void)blocks;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)n_pairs + 255) / 256, (int64_t)sms * 8));
+    if (n_pairs > 0) k_demand_levels<<<g, 256, 0, st>>>(tv, cd, n_pairs, max_level, reorder, dm);
 }
 
 void launch_list_keys(cudaStream_t st, int blocks, int32_t n_sigs, const int32_t *count, const int64_t *offset,
