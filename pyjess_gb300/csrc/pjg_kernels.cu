@@ -1236,53 +1236,75 @@ __global__ void __launch_bounds__(WARPS * 32)
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int64_t total = (int64_t)ls.n[1];
     unsigned long long n_shared = 0;
-    for (int64_t i = warp; i < total; i += nwarps) {
-        const int64_t v = ls.dup_work[i];
-        const int64_t w = v >> 32, r = (int64_t)(uint32_t)(v & 0xFFFFFFFFll);
-        const int m = count[w];
-        const int s = (int)(w / n_sigs);
-        bool same = count[r] == m && (int)(r / n_sigs) == s;
-        const int32_t *cw = cand_atom + offset[w], *cr = cand_atom + offset[r];
-        bool seq = same;
-        if (same) {
+    // 32 consecutive duplicates a warp: each lane loads one's lengths and
+    // offsets, then the warp checks them one after the other
+    for (int64_t base = warp * 32; base < total; base += nwarps * 32) {
+        const int64_t item = base + lane;
+        int64_t w = 0, r = 0, ow = 0, orr = 0;
+        int m = 0;
+        bool same = false;
+        if (item < total) {
+            const int64_t v = ls.dup_work[item];
+            w = v >> 32;
+            r = (int64_t)(uint32_t)(v & 0xFFFFFFFFll);
+            m = count[w];
+            same = count[r] == m && (r / n_sigs) == (w / n_sigs);
+            ow = offset[w];
+            orr = offset[r];
+        }
+        const int nt = total - base < 32 ? (int)(total - base) : 32;
+        bool verdict = false;
+        for (int t = 0; t < nt; t++) {
+            const int mt = __shfl_sync(FULL_MASK, m, t);
+            bool st = __shfl_sync(FULL_MASK, same, t);
+            if (!st) continue;
+            const int64_t rt = __shfl_sync(FULL_MASK, r, t), wt = __shfl_sync(FULL_MASK, w, t);
+            const int32_t *cw = cand_atom + __shfl_sync(FULL_MASK, ow, t);
+            const int32_t *cr = cand_atom + __shfl_sync(FULL_MASK, orr, t);
             bool eq = true;
-            for (int k = lane; k < m; k += 32) eq &= cw[k] == cr[k];
-            seq = __all_sync(FULL_MASK, eq);
-        }
-        if (same && !seq) {
-            // the same set: every atom of w marked by r, one window of the
-            // structure's atom indices at a time
-            same = ls.part_ok[r] != 0;
-            const int natoms = cv.atom_count[s];
-            for (int wb = 0; wb < natoms && same; wb += WB) {
-                const int nwords = min(LEAF_SORT_WORDS, (natoms - wb + 31) >> 5);
-                for (int q = lane; q < nwords; q += 32) B[q] = 0u;
-                __syncwarp();
-                for (int k = lane; k < m; k += 32) {
-                    const uint32_t u = (uint32_t)cr[k] - (uint32_t)wb;
-                    if (u < (uint32_t)WB) atomicOr(&B[u >> 5], 1u << (u & 31));
+            for (int k = lane; k < mt; k += 32) eq &= cw[k] == cr[k];
+            if (!__all_sync(FULL_MASK, eq)) {
+                // the same set: every atom of w marked by r, one window of
+                // the structure's atom indices at a time
+                st = ls.part_ok[rt] != 0;
+                const int natoms = cv.atom_count[(int)(wt / n_sigs)];
+                for (int wb = 0; wb < natoms && st; wb += WB) {
+                    const int nwords = min(LEAF_SORT_WORDS, (natoms - wb + 31) >> 5);
+                    for (int q = lane; q < nwords; q += 32) B[q] = 0u;
+                    __syncwarp();
+                    for (int k = lane; k < mt; k += 32) {
+                        const uint32_t u = (uint32_t)cr[k] - (uint32_t)wb;
+                        if (u < (uint32_t)WB) atomicOr(&B[u >> 5], 1u << (u & 31));
+                    }
+                    __syncwarp();
+                    bool in = true;
+                    for (int k = lane; k < mt; k += 32) {
+                        const uint32_t u = (uint32_t)cw[k] - (uint32_t)wb;
+                        if (u < (uint32_t)WB) in &= ((B[u >> 5] >> (u & 31)) & 1u) != 0u;
+                    }
+                    st = __all_sync(FULL_MASK, in);
+                    __syncwarp();
                 }
-                __syncwarp();
-                bool in = true;
-                for (int k = lane; k < m; k += 32) {
-                    const uint32_t u = (uint32_t)cw[k] - (uint32_t)wb;
-                    if (u < (uint32_t)WB) in &= ((B[u >> 5] >> (u & 31)) & 1u) != 0u;
-                }
-                same = __all_sync(FULL_MASK, in);
-                __syncwarp();
             }
+            if (lane == t) verdict = st;
         }
-        if (lane == 0) {
-            if (same) {
+        if (item < total) {
+            if (verdict) {
                 leaf_offset[w] = leaf_offset[r];
                 blk_offset[w] = blk_offset[r];
                 n_shared++;
-            } else {
-                ls.left_work[atomicAdd(&ls.n[2], 1ull)] = w;
             }
         }
-        __syncwarp();
+        const bool left = item < total && !verdict;
+        const unsigned lm = __ballot_sync(FULL_MASK, left);
+        if (lm) {
+            unsigned long long b = 0;
+            if (lane == 0) b = atomicAdd(&ls.n[2], (unsigned long long)__popc(lm));
+            b = __shfl_sync(FULL_MASK, b, 0);
+            if (left) ls.left_work[b + __popc(lm & ((1u << lane) - 1u))] = w;
+        }
     }
+    for (int o = 16; o; o >>= 1) n_shared += __shfl_xor_sync(FULL_MASK, n_shared, o);
     if (lane == 0 && n_shared) atomicAdd(&counters[C_LEAF_SHARED], n_shared);
 }
 
