@@ -423,11 +423,17 @@ def main():
     exp_bytes = sum(s["bytes_expansion"] for s in stats)
     achieved = exp_bytes / (exp_ms / 1e3) / 1e9 if exp_ms > 0 else 0.0
     peak = float(peaks["hbm_gbs"])
-    traffic = None
+    traffic, issue = None, None
     tpath = os.path.join(ROOT, "profiles", "k_search_traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
             tr = json.load(f)
+        # the resource that binds k_search: issue slots (ncu, same capture)
+        if tr.get("issue_active_frac") is not None:
+            issue = {"frac": tr["issue_active_frac"], "frac_first_round": tr.get("issue_active_frac_first_round"),
+                     "warp_inst_per_partial": tr.get("warp_inst_per_partial"),
+                     "source": "ncu smsp__issue_active.avg.pct_of_peak_sustained_active and sm__inst_executed.sum "
+                               "of the k_search launches of a 20 x 5,000 query (profiles/k_search_traffic.json)"}
         # DRAM bytes per algorithmic expansion byte, measured by ncu over the
         # k_search launches of one query of a smaller case, times the
         # expansion bytes of an average launch of this workload
@@ -539,7 +545,7 @@ def main():
         "batched_over_plain": value / plain["value"] if plain else None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
-                     "kernel": "k_search", "peak_kind": peak_kind,
+                     "kernel": "k_search", "peak_kind": peak_kind, "issue_slots": issue,
                      "bytes_expansion_per_step": exp_bytes / args.steps,
                      "ms_expansion_per_step": exp_ms / args.steps},
         "stage_ms": {"candidates": s0["ms_candidates"], "expansion": s0["ms_expansion"],
