@@ -33,10 +33,13 @@ SOURCES = ["pjg_kernels.cu", "pjg_api.cu", "pjg_io.cpp"]
 # file named by PJG_PROF_OUT) and is never the timed build; "blk8"/"blk16"
 # cull by blocks of 8/16 leaves instead of 32, "w10" runs the search with
 # 10 warps a block, "rank" orders tie-free lists by the rank method instead
-# of axis partitions (measured against each other)
+# of axis partitions, "part256"/"part512" order tie-free lists longer than
+# 256/512 entries by sorted axes instead of axis partitions (measured against
+# each other)
 VARIANTS = {"": [], "prof": ["-DPJG_SEARCH_PROF=1"], "blk8": ["-DPJG_CULL_BLK=8"], "blk16": ["-DPJG_CULL_BLK=16"],
             "blk8prof": ["-DPJG_CULL_BLK=8", "-DPJG_SEARCH_PROF=1"], "w10": ["-DPJG_SEARCH_WARPS=10"],
-            "rank": ["-DPJG_LEAF_RANK=1"], "rankprof": ["-DPJG_LEAF_RANK=1", "-DPJG_SEARCH_PROF=1"]}
+            "rank": ["-DPJG_LEAF_RANK=1"], "rankprof": ["-DPJG_LEAF_RANK=1", "-DPJG_SEARCH_PROF=1"],
+            "part256": ["-DPJG_PART_MAX=256"], "part512": ["-DPJG_PART_MAX=512"]}
 
 
 def lib_path(variant: str = "") -> pathlib.Path:

@@ -1325,13 +1325,13 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                                       d_leaf_atom.p, d_leaf_xyz.p, d_blk_lo.p, d_blk_hi.p, d_sorted_list.p,
                                       d_sorted_count.p, Wc, d_exact_list.p, d_exact_count.p, d_counters.p,
                                       ls.left_work, ls.n + 2, tune.leaf_rank_max, ls.part_ok, 0);
-                    launches += 17;
+                    launches += 2 * LEAF_ORDER_LAUNCHES + 3;
                 } else {
                     launch_leaf_order(st, leaf_blocks, cv, G, cnt_c, d_offset.p, d_boff.p, d_cand_atom.p, leaf_off,
                                       d_leaf_atom.p, d_leaf_xyz.p, d_blk_lo.p, d_blk_hi.p, d_sorted_list.p,
                                       d_sorted_count.p, Wc, d_exact_list.p, d_exact_count.p, d_counters.p, dm.work,
                                       dm.n_work, tune.leaf_rank_max);
-                    launches += 7;
+                    launches += LEAF_ORDER_LAUNCHES;
                 }
                 if (dm.state) {
                     launch_mark_ordered(st, sm_count() * 4, dm);

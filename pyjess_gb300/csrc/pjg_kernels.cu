@@ -4082,10 +4082,11 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
         k_leaf_part<256, 4><<<g, 128, SP, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset,
                                                 leaf_atom, leaf_xyz, blk_lo, blk_hi, sorted_list, sorted_count,
                                                 list_cap, exact_list, exact_count, counters, rank_max, work, n_work,
-                                                list512, count512, 512, list1024, count1024, 1024, count_lists,
+                                                PART_MAX >= 512 ? list512 : nullptr, count512, 512,
+                                                PART_MAX >= 1024 ? list1024 : nullptr, count1024, 1024, count_lists,
                                                 part_ok);
     }
-    {
+    if (PART_MAX >= 512) {
         constexpr int SP = (int)sizeof(PartWarp<512>) * 4;
         const int g = wave((const void *)k_leaf_part<512, 4>, 128, SP);
         k_leaf_part<512, 4><<<g, 128, SP, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset,
@@ -4093,7 +4094,7 @@ void launch_leaf_order(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
                                                 list_cap, exact_list, exact_count, counters, 512, list512, count512,
                                                 nullptr, nullptr, 0, nullptr, nullptr, 0, 0, part_ok);
     }
-    {
+    if (PART_MAX >= 1024) {
         constexpr int SP = (int)sizeof(PartWarp<1024>) * 2;
         const int g = wave((const void *)k_leaf_part<1024, 2>, 64, SP);
         k_leaf_part<1024, 2><<<g, 64, SP, st>>>(cv, n_sigs, count, offset, blk_offset, cand_atom, leaf_offset,

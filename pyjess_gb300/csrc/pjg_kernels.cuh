@@ -49,6 +49,15 @@ constexpr int LEAF_RANK_MAX = 192;     // default: longest list ordered by the r
 constexpr int LEAF_FAST_MAX = 256;     // capacity of k_leaf_part's first instance
 constexpr int LEAF_RANK_MAX = 256;     // default: longest list that instance takes
 #endif
+// longest tie-free list ordered by axis partitions (256, 512 or 1024; the
+// longer ones by sorted axes)
+#ifndef PJG_PART_MAX
+#define PJG_PART_MAX 1024
+#endif
+constexpr int PART_MAX = PJG_PART_MAX;
+static_assert(PART_MAX == 256 || PART_MAX == 512 || PART_MAX == 1024, "axis partitions up to 256, 512 or 1024");
+// kernels one launch_leaf_order call launches
+constexpr int LEAF_ORDER_LAUNCHES = PJG_LEAF_RANK ? 7 : (PART_MAX >= 1024 ? 8 : PART_MAX >= 512 ? 7 : 6);
 constexpr int LEAF_LISTS = 5;          // leaf-order worklists: three k_leaf_sorted size
                                        //   classes and two forwarded size classes
 constexpr int LEAF_MID_MAX = 384;      // longest list of the rank method's larger instance
