@@ -12,13 +12,19 @@
 //   k_axis_ranks        per-structure axis ranks (once, at upload)
 //   k_demand_levels     requests the kd leaf order of the lists a pair
 //                       reaches first
-//   k_leaf_order        kd leaf order of short tie-free lists by ranks (tied
-//                       or longer lists are passed on)
+//   k_list_keys, k_list_reps, k_list_share
+//                       requested lists with the same atoms share one
+//                       leaf order
+//   k_leaf_part<M>      kd leaf order of tie-free lists by axis partitions
+//                       of presorted orders (tied or longer lists are
+//                       passed on; k_leaf_order, the rank method, in the
+//                       PJG_LEAF_RANK build)
 //   k_leaf_sorted<M>    kd leaf order by sorted-axis splits, with a qselect
 //                       replay of tied nodes
 //   k_leaf_exact<M>     the literal qselect sequence, for the rest
 //   k_search            persistent warp per pair, order-preserving
 //                       depth-first-over-tiles frontier expansion
+//                       (k_search_large: templates over 32 atoms)
 //   k_superpose         thread per complete row, FP64 covariance and
 //                       quaternion eigen-solve
 //   k_order_counts, k_automaton, k_gather_hits
