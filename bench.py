@@ -341,6 +341,10 @@ def search_profile(args):
         "children_per_product_test": prof["child_prod"] / max(1, prof["prod_lanes"]),
         "lanes_per_product_batch": prof["prod_lanes"] / max(1, prof["prod_batches"]),
         "block_visits_per_partial": prof["block_visits"] / max(1, st["partials"]),
+        # the launches' tails (queue empty to last warp out) against the
+        # expansion time, and the longest single pair (at 2.07 GHz)
+        "tail_share_of_expansion": prof.get("tail_ns", 0) / max(1.0, st["ms_expansion"] * 1e6),
+        "longest_pair_us": prof.get("pair_max_cyc", 0) / 2070.0,
     }
     lo = prof.get("leaf_order")
     if lo:

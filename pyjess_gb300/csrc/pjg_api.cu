@@ -839,7 +839,8 @@ void write_search_profile(const unsigned long long *d_prof, cudaStream_t st, con
         "pairs", "empty", "cyc_pair", "cyc_setup", "cyc_seed", "cyc_block", "cyc_prod", "cyc_emit",
         "loop_iters", "block_visits", "block_visits_l0", "chain_full", "chain_sibling", "g0_iters",
         "blocks_tested", "blocks_hit", "leaves_inbox", "batches", "batch_lanes", "child_block",
-        "prod_batches", "prod_batches_l0", "prod_lanes", "child_prod", "fp64", "rows", "cyc_chain", "cyc_batch", "cyc_ctrl", "cyc_susp"};
+        "prod_batches", "prod_batches_l0", "prod_lanes", "child_prod", "fp64", "rows", "cyc_chain", "cyc_batch", "cyc_ctrl", "cyc_susp",
+        "tail_ns", "pair_max_cyc"};
     unsigned long long h[SP_NUM] = {};
     if (cudaMemcpyAsync(h, d_prof, sizeof h, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)

@@ -2635,6 +2635,8 @@ __device__ __noinline__ bool decide_fp64(unsigned exact_mask, int lev, const int
     } while (0)
 #define SPROF_T(name) const long long name = clock64()
 #define SPROF_CYC(i, t0) SPROF_ADD(i, clock64() - (t0))
+// queue-empty and exit times of the warps of one k_search launch (ns)
+__device__ unsigned long long g_search_tail[2];
 #else
 #define SPROF_ADD(i, v) \
     do {                \
@@ -3509,6 +3511,12 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
         }
         __syncwarp();
         SPROF_CYC(SP_CYC_PAIR, t_pair);
+#if PJG_SEARCH_PROF
+        if (lane == 0) {
+            const unsigned long long c = (unsigned long long)(clock64() - t_pair);
+            if (c > sprof[wib][SP_PAIR_MAX_CYC]) sprof[wib][SP_PAIR_MAX_CYC] = c;
+        }
+#endif
         if (suspended) continue;
         if (lane == 0 && emitted > 0) out.pair_rows[pair] = (int32_t)emitted;
         // ---- statistics of the pair
@@ -3525,13 +3533,20 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
         }
         __syncwarp();
     }
+#if PJG_SEARCH_PROF
+    if (lane == 0) atomicMin(&g_search_tail[0], (unsigned long long)global_ns());
+#endif
     __syncwarp();
     if (lane <= C_BYTES_EXP && st.acc[lane]) atomicAdd(&counters[lane], st.acc[lane]);
 #if PJG_SEARCH_PROF
     for (int o = 16; o; o >>= 1) sp_fp64 += __shfl_xor_sync(FULL_MASK, sp_fp64, o);
     SPROF_ADD(SP_FP64, sp_fp64);
     __syncwarp();
-    if (sa.prof && lane < SP_NUM) atomicAdd(&sa.prof[lane], sprof[wib][lane]);
+    if (sa.prof && lane < SP_NUM) {
+        if (lane == SP_PAIR_MAX_CYC) atomicMax(&sa.prof[lane], sprof[wib][lane]);
+        else if (lane != SP_TAIL_NS) atomicAdd(&sa.prof[lane], sprof[wib][lane]);
+    }
+    if (lane == 0) atomicMax(&g_search_tail[1], (unsigned long long)global_ns());
 #endif
 }
 
@@ -4219,15 +4234,31 @@ static cudaError_t search_cut(cudaStream_t st, int grid, const ChunkView &cv, co
                : search_variant<RowT, FP32, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm);
 }
 
+#if PJG_SEARCH_PROF
+__global__ void k_prof_tail(unsigned long long *prof) {
+    if (g_search_tail[1] > g_search_tail[0]) prof[SP_TAIL_NS] += g_search_tail[1] - g_search_tail[0];
+}
+#endif
+
 cudaError_t launch_search(cudaStream_t st, int grid, bool wide, bool fp32, const ChunkView &cv,
                           const TemplateView &tv, const CandView &cd, const SearchArgs &sa, int32_t *pair_counter,
                           const int32_t *scanned, const CompleteRows &out, unsigned long long *counters,
                           const LeafDemand &dm) {
+#if PJG_SEARCH_PROF
+    const unsigned long long t0[2] = {~0ull, 0ull};
+    cudaMemcpyToSymbolAsync(g_search_tail, t0, sizeof t0, 0, cudaMemcpyHostToDevice, st);
+#endif
+    cudaError_t e;
     if (wide)
-        return fp32 ? search_cut<uint32_t, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm)
-                    : search_cut<uint32_t, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm);
-    return fp32 ? search_cut<uint16_t, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm)
-                : search_cut<uint16_t, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm);
+        e = fp32 ? search_cut<uint32_t, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm)
+                 : search_cut<uint32_t, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm);
+    else
+        e = fp32 ? search_cut<uint16_t, true>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm)
+                 : search_cut<uint16_t, false>(st, grid, cv, tv, cd, sa, pair_counter, scanned, out, counters, dm);
+#if PJG_SEARCH_PROF
+    if (e == cudaSuccess && sa.prof) k_prof_tail<<<1, 1, 0, st>>>(sa.prof);
+#endif
+    return e;
 }
 
 cudaError_t launch_search_large(cudaStream_t st, const ChunkView &cv, const TemplateView &tv, const CandView &cd,

@@ -107,6 +107,9 @@ enum SearchProf : int {
     SP_CYC_CTRL,         // cycles of the loop's level bookkeeping (moving up
                          // or down a level, choosing the expansion mode)
     SP_CYC_SUSP,         // cycles suspending pairs (state saved, lists requested)
+    SP_TAIL_NS,          // per launch, summed: ns from the first warp finding the
+                         // work queue empty to the last warp's exit
+    SP_PAIR_MAX_CYC,     // most cycles one pair took (a maximum, not a sum)
     SP_NUM
 };
 
