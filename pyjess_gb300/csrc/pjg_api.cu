@@ -973,6 +973,10 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
     DBuf<unsigned long long> d_nfill;
     DBuf<Suspended> d_susp_a, d_susp_b;
     DBuf<unsigned char> d_pool_a, d_pool_b;
+    // costliest pairs first: cost buckets, heavy flags and list, histogram
+    DBuf<uint8_t> d_pcost, d_hflag;
+    DBuf<int32_t> d_heavy;
+    DBuf<unsigned long long> d_hbins;
     DBuf<unsigned long long> d_pool_used;
     int64_t pool_cap = 0;
     // requested lists sharing one leaf order (table and worklists)
@@ -1428,7 +1432,33 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                     status = fail(PJG_ERR_CAPACITY, "too many pairs in one chunk");
                     goto done;
                 }
+                // the costliest pairs are searched first (a pair can take
+                // milliseconds; started last, it alone would run on while the
+                // other warps idle): the level demand estimates each pair's
+                // cost, and the pairs of the top cost buckets, at most two per
+                // resident search warp, are taken before the others
+                const int64_t heavy_target = 4LL * sm_count() * SEARCH_WARPS;
+                const char *hf = getenv("PJG_HEAVY_FIRST");
+                const bool heavy_on = (int64_t)n_pairs >= 8 * heavy_target && !(hf && atoi(hf) == 0);
+                dm.pair_cost = nullptr;
+                dm.heavy = nullptr;
+                if (heavy_on) {
+                    CUDA_TRY(dalloc(d_pcost, (size_t)n_pairs, st));
+                    CUDA_TRY(dalloc(d_hflag, (size_t)n_pairs, st));
+                    CUDA_TRY(dalloc(d_heavy, (size_t)heavy_target, st));
+                    CUDA_TRY(dalloc(d_hbins, 66, st));
+                    CUDA_TRY(cudaMemsetAsync(d_hbins.p, 0, 66 * sizeof(unsigned long long), st));
+                    dm.pair_cost = d_pcost.p;
+                }
                 launch_demand_levels(st, sm_count() * 16, tv, cd, (int32_t)n_pairs, demand_levels, P->reorder, dm);
+                if (heavy_on) {
+                    launch_heavy_pairs(st, (int32_t)n_pairs, d_pcost.p, d_hbins.p, heavy_target, d_hflag.p,
+                                       d_heavy.p);
+                    dm.heavy = d_heavy.p;
+                    dm.n_heavy = d_hbins.p + 64;
+                    dm.heavy_flag = d_hflag.p;
+                    launches += 2;
+                }
                 // the level-0 lists the pairs read in candidate order
                 launch_candidates(st, fill_blocks, true, cv, sv, nullptr, nullptr, d_offset.p, d_cand_atom.p,
                                   dm.fill_work, dm.n_fill, nullptr, false);
@@ -1785,6 +1815,7 @@ done:
         dfree(d_r_rmsd, st); dfree(d_r_rot, st); dfree(d_r_cen, st); dfree(d_r_nan, st); dfree(d_r_hit, st);
         dfree(d_r_warn, st); dfree(d_r_hatoms, st); dfree(d_r_src, st); dfree(d_r_hidx, st); dfree(d_r_widx, st);
         dfree(d_r_aidx, st); dfree(d_lstate, st); dfree(d_work, st); dfree(d_nwork, st); dfree(d_nsusp, st);
+        dfree(d_pcost, st); dfree(d_hflag, st); dfree(d_heavy, st); dfree(d_hbins, st);
         dfree(d_susp_a, st); dfree(d_susp_b, st); dfree(d_pool_a, st); dfree(d_pool_b, st); dfree(d_pool_used, st);
         dfree(d_prof, st);
         dfree(d_fill_state, st); dfree(d_fill_work, st); dfree(d_nfill, st);

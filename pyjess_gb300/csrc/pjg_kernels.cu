@@ -2167,6 +2167,15 @@ __global__ void k_demand_levels(TemplateView tv, CandView cd, int32_t n_pairs, i
                 if (levels >= TOP) per_thread = true;
             }
         }
+        if (dm.pair_cost && pair < n_pairs) {
+            // estimated cost: the product of the two shortest list lengths
+            // (a one-atom template: its list's length), as a power-of-two
+            // bucket; 0 for a pair with nothing to search here
+            unsigned long long cost = 0;
+            if (n == 1 && levels == 0) cost = (unsigned long long)cd.count[wb + tv.sig[ab]];
+            else if (n >= 2 && n <= 32 && levels >= 0) cost = (top[0] >> 5) * (top[1] >> 5);
+            dm.pair_cost[pair] = (uint8_t)(cost ? min(63, 64 - __clzll((long long)cost)) : 0);
+        }
         // levels 0..TOP-1, warp-wide (every lane takes every step)
 #pragma unroll
         for (int i = 0; i < TOP; i++) {
@@ -2215,6 +2224,50 @@ __global__ void k_demand_levels(TemplateView tv, CandView cd, int32_t n_pairs, i
                 if (rank == 0) request_fill(dm, w);
                 else if (rank <= max_level) request_list(dm, w, c);
             }
+        }
+    }
+}
+
+// Costliest pairs first.  Pass 1: a histogram of the pairs' cost buckets.
+__global__ void k_cost_hist(int32_t n_pairs, const uint8_t *cost, unsigned long long *bins) {
+    __shared__ unsigned int h[64];
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_pairs; p += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&h[cost[p]], 1u);
+    __syncthreads();
+    for (int i = threadIdx.x; i < 64; i += blockDim.x)
+        if (h[i]) atomicAdd(&bins[i], (unsigned long long)h[i]);
+}
+
+// Pass 2: the threshold (the highest bucket at which the pairs of that
+// bucket and above pass `target`; the pairs above it are heavy), then each
+// heavy pair flagged and listed (bins[64]: their count).
+__global__ void k_heavy_list(int32_t n_pairs, const uint8_t *cost, unsigned long long *bins, int64_t target,
+                             uint8_t *heavy_flag, int32_t *heavy) {
+    __shared__ int thr;
+    if (threadIdx.x == 0) {
+        unsigned long long acc = 0;
+        int b = 63;
+        for (; b > 0; b--) {
+            acc += bins[b];
+            if (acc > (unsigned long long)target) break;
+        }
+        thr = b;  // b == 0: every pair with a cost fits under the target
+    }
+    __syncthreads();
+    const int lane = lane_id();
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t p0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) & ~31ll; p0 < n_pairs; p0 += stride) {
+        const int64_t p = p0 + lane;
+        const bool hv = p < n_pairs && cost[p] > thr;
+        if (p < n_pairs) heavy_flag[p] = hv ? 1 : 0;
+        const unsigned m = __ballot_sync(FULL_MASK, hv);
+        if (m) {
+            unsigned long long b = 0;
+            if (lane == 0) b = atomicAdd(&bins[64], (unsigned long long)__popc(m));
+            b = __shfl_sync(FULL_MASK, b, 0);
+            if (hv) heavy[b + __popc(m & ((1u << lane) - 1u))] = (int32_t)p;
         }
     }
 }
@@ -2694,7 +2747,10 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
     // pairs of this round: every pair of the chunk, or the pairs that an
     // earlier round suspended (each with the rows it has already emitted)
     const bool fresh = dm.resume == nullptr;
-    const int n_items = fresh ? sa.n_pairs : dm.n_resume;
+    // a fresh round takes the heavy pairs first, then every pair in order
+    // (skipping the heavy ones)
+    const int n_heavy = fresh && dm.heavy ? (int)*dm.n_heavy : 0;
+    const int n_items = fresh ? sa.n_pairs + n_heavy : dm.n_resume;
     // work queue: a warp takes sa.pair_grain consecutive items at a time
     int g_next = 0, g_end = 0;
     for (;;) {
@@ -2706,9 +2762,17 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32, PJG_SEARCH_MIN_BLOCKS)
         }
         const int item = g_next++;
         if (item >= n_items || timed_out) break;
+        int pair;
+        if (!fresh) {
+            pair = dm.resume[item].pair;
+        } else if (item < n_heavy) {
+            pair = dm.heavy[item];
+        } else {
+            pair = item - n_heavy;
+            if (n_heavy && dm.heavy_flag[pair]) continue;
+        }
         SPROF_T(t_pair);
         SPROF_ADD(SP_PAIRS, 1);
-        const int pair = fresh ? item : dm.resume[item].pair;
         const int64_t skip = fresh ? 0 : dm.resume[item].skip;
         const int64_t saved = fresh ? -1 : dm.resume[item].state;
         const int s = pair / T;
@@ -4195,6 +4259,17 @@ void launch_list_share(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
                        const ListShare &ls, unsigned long long *counters) {
     k_list_share<8><<<blocks, 256, 0, st>>>(cv, n_sigs, count, offset, cand_atom, leaf_offset, blk_offset, ls,
                                             counters);
+}
+
+void launch_heavy_pairs(cudaStream_t st, int32_t n_pairs, const uint8_t *pair_cost, unsigned long long *bins,
+                        int64_t target, uint8_t *heavy_flag, int32_t *heavy) {
+    if (n_pairs <= 0) return;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)n_pairs + 255) / 256, (int64_t)sms * 4));
+    k_cost_hist<<<g, 256, 0, st>>>(n_pairs, pair_cost, bins);
+    k_heavy_list<<<g, 256, 0, st>>>(n_pairs, pair_cost, bins, target, heavy_flag, heavy);
 }
 
 void launch_mark_ordered(cudaStream_t st, int blocks, const LeafDemand &dm) {

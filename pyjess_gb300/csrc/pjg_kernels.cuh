@@ -207,6 +207,14 @@ struct LeafDemand {
     int32_t *fill_state;
     int64_t *fill_work;                // level-0 lists queued for the fill
     unsigned long long *n_fill;
+    // the costliest pairs first (the round that runs every pair): the
+    // level demand writes each pair's estimated cost as a power-of-two
+    // bucket (0: nothing to search), the pairs above a threshold are listed
+    // in `heavy` and taken before the others, which keep their order
+    uint8_t *pair_cost;                // [n_pairs] (nullptr: not estimated)
+    const int32_t *heavy;              // pairs taken first (nullptr: none)
+    const unsigned long long *n_heavy; //   how many
+    const uint8_t *heavy_flag;         // [n_pairs] 1: the pair is in `heavy`
 };
 
 // Requested lists whose candidate atoms are the same share one kd leaf
@@ -324,6 +332,11 @@ void launch_list_share(cudaStream_t st, int blocks, const ChunkView &cv, int32_t
 // of the chunk that has no empty candidate list
 void launch_demand_levels(cudaStream_t st, int blocks, const TemplateView &tv, const CandView &cd, int32_t n_pairs,
                           int32_t max_level, int32_t reorder, const LeafDemand &dm);
+// the pairs whose cost bucket is above the level that leaves at most
+// `target` pairs above it: flags and list (n_heavy), from the buckets the
+// level demand wrote (bins: 66 counters, zeroed by the caller)
+void launch_heavy_pairs(cudaStream_t st, int32_t n_pairs, const uint8_t *pair_cost, unsigned long long *bins,
+                        int64_t target, uint8_t *heavy_flag, int32_t *heavy);
 
 // state[work[i]] = 2 for the n_work requested lists
 void launch_mark_ordered(cudaStream_t st, int blocks, const LeafDemand &dm);

@@ -318,7 +318,7 @@ def set_pool(monkeypatch, pool):
 
 
 @pytest.mark.parametrize("pool", POOLS)
-@pytest.mark.parametrize("levels", [-1, 0, 1, 2])
+@pytest.mark.parametrize("levels", [-1, 0, 1, 2, 9, 12])
 def test_leaf_order_on_demand_config3(monkeypatch, levels, pool):
     from pyjess_gb300 import workloads as W
 
@@ -331,6 +331,18 @@ def test_leaf_order_on_demand_config3(monkeypatch, levels, pool):
         assert st["suspensions"] > 0 and st["search_rounds"] > 1
     if levels == -1:
         assert st["suspensions"] == 0 and st["search_rounds"] == st["chunks"]
+
+
+@pytest.mark.parametrize("levels", [3, 10])
+def test_leaf_order_up_front_levels_without_reorder(monkeypatch, levels):
+    """Template atoms taken in their own order (reorder=False) with 3 and
+    10 levels put in leaf order before the search (the second deeper than
+    the level demand keeps in registers): the oracle's hits."""
+    from pyjess_gb300 import workloads as W
+
+    monkeypatch.setenv("PJG_LEAF_LEVELS", str(levels))
+    wl = W.config(3, n_structures=20, n_templates=200)
+    compare(wl.templates, wl.structures, mode="fp32", reorder=False, **wl.params)
 
 
 @pytest.mark.parametrize("pool", POOLS)
