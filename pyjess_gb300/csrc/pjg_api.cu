@@ -1435,9 +1435,12 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 // the costliest pairs are searched first (a pair can take
                 // milliseconds; started last, it alone would run on while the
                 // other warps idle): the level demand estimates each pair's
-                // cost, and the pairs of the top cost buckets, at most two per
-                // resident search warp, are taken before the others
-                const int64_t heavy_target = 4LL * sm_count() * SEARCH_WARPS;
+                // cost, and the pairs of the top cost buckets, at most two
+                // (PJG_HEAVY_PER_WARP) per resident search warp, are taken
+                // before the others
+                const char *hw = getenv("PJG_HEAVY_PER_WARP");
+                const int64_t per_warp = hw && atoi(hw) > 0 ? atoi(hw) : 2;
+                const int64_t heavy_target = per_warp * 2 * sm_count() * SEARCH_WARPS;
                 const char *hf = getenv("PJG_HEAVY_FIRST");
                 const bool heavy_on = (int64_t)n_pairs >= 8 * heavy_target && !(hf && atoi(hf) == 0);
                 dm.pair_cost = nullptr;
