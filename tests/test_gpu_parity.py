@@ -333,6 +333,20 @@ def test_leaf_order_on_demand_config3(monkeypatch, levels, pool):
         assert st["suspensions"] == 0 and st["search_rounds"] == st["chunks"]
 
 
+@pytest.mark.parametrize("heavy", ["1", "0"])
+def test_heavy_pairs_first(monkeypatch, heavy):
+    """The costliest pairs taken first (done for chunks of at least eight
+    times the heavy-pair target; PJG_HEAVY_PER_WARP=1 brings the target
+    within reach of a 70 x 300 workload) or not: the oracle's hits and
+    search counters either way."""
+    from pyjess_gb300 import workloads as W
+
+    monkeypatch.setenv("PJG_HEAVY_PER_WARP", "1")
+    monkeypatch.setenv("PJG_HEAVY_FIRST", heavy)
+    wl = W.config(3, n_structures=70, n_templates=300)
+    compare(wl.templates, wl.structures, mode="fp32", **wl.params)
+
+
 @pytest.mark.parametrize("levels", [3, 10])
 def test_leaf_order_up_front_levels_without_reorder(monkeypatch, levels):
     """Template atoms taken in their own order (reorder=False) with 3 and
