@@ -64,3 +64,17 @@ def test_single_rank_is_config3():
     b = W.config(3, n_structures=3, n_templates=4)
     assert (a.structures.xyz == b.structures.xyz).all()
     assert bench.max_over_ranks(5.0, None) == 5.0
+
+
+def test_search_profile_fields_the_bench_line_reads():
+    """The committed k_search capture holds what the bench line's roofline
+    reports: DRAM bytes per expansion byte and the issue-slot fraction."""
+    import json
+    import pathlib
+
+    tr = json.loads((pathlib.Path(__file__).resolve().parents[1] / "profiles" / "k_search_traffic.json").read_text())
+    assert 1.0 < tr["dram_per_expansion_byte"] < 10.0
+    assert 0.0 < tr["issue_active_frac"] <= tr["issue_active_frac_first_round"] <= 1.0
+    assert tr["warp_inst_per_partial"] == round(tr["inst_executed"] / tr["partials"], 1)
+    timed = [l for l in tr["launches"] if l["query"] == "timed"]
+    assert sum(l["dram_bytes_read"] + l["dram_bytes_write"] for l in timed) == tr["dram_bytes"]
