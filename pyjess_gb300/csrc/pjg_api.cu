@@ -1442,7 +1442,9 @@ extern "C" pjg_status pjg_query(const pjg_templates *tp, const pjg_structures *s
                 const int64_t per_warp = hw && atoi(hw) > 0 ? atoi(hw) : 2;
                 const int64_t heavy_target = per_warp * 2 * sm_count() * SEARCH_WARPS;
                 const char *hf = getenv("PJG_HEAVY_FIRST");
-                const bool heavy_on = (int64_t)n_pairs >= 8 * heavy_target && !(hf && atoi(hf) == 0);
+                const bool heavy_on = (int64_t)n_pairs >= 8 * heavy_target &&
+                                      (int64_t)n_pairs <= (int64_t)INT32_MAX - heavy_target &&
+                                      !(hf && atoi(hf) == 0);
                 dm.pair_cost = nullptr;
                 dm.heavy = nullptr;
                 if (heavy_on) {
