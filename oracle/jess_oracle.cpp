@@ -30,6 +30,7 @@
 #include <cstring>
 #include <mutex>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 namespace {
@@ -297,6 +298,44 @@ inline void count_boundary(const Annulus &A, const double *x, BoundaryCount *bc)
 
 struct Box { double min[3], max[3]; };
 
+// Instrumentation for comparing culling schemes (not part of the
+// reference's algorithm; off unless oracle_set_cull_stats(1)): for every kd
+// range query on a list of at least CULL_MIN_LIST points, how many of the
+// list's points a search would load under each scheme -- the blocks of 32
+// consecutive kd leaves whose bounding box meets the join box (the GPU
+// search's block culling), and uniform grids of cell size CULL_GRID[g] over
+// the list (every point of every cell the join box meets) -- against the
+// points inside the join box and the query's actual results.
+constexpr int CULL_MIN_LIST = 64;
+constexpr int CULL_NGRID = 4;
+constexpr double CULL_GRID[CULL_NGRID] = {2.0, 3.0, 4.0, 6.0};
+int g_cull_stats = 0;
+
+struct CullCount {
+    int64_t queries = 0;        // range queries on lists of >= CULL_MIN_LIST points
+    int64_t points = 0;         //   the lists' points
+    int64_t in_box = 0;         //   points inside the join box
+    int64_t children = 0;       //   points inside every annulus (the results)
+    int64_t kd_nodes = 0;       //   kd nodes the reference's traversal visits
+    int64_t blocks_hit = 0;     //   32-leaf blocks meeting the join box
+    int64_t block_loaded = 0;   //   points of those blocks
+    int64_t grid_cells[CULL_NGRID] = {};   // grid cells the join box meets
+    int64_t grid_loaded[CULL_NGRID] = {};  //   points in them
+    void add(const CullCount &o) {
+        queries += o.queries;
+        points += o.points;
+        in_box += o.in_box;
+        children += o.children;
+        kd_nodes += o.kd_nodes;
+        blocks_hit += o.blocks_hit;
+        block_loaded += o.block_loaded;
+        for (int g = 0; g < CULL_NGRID; g++) {
+            grid_cells[g] += o.grid_cells[g];
+            grid_loaded[g] += o.grid_loaded[g];
+        }
+    }
+};
+
 void join_box(const Annulus *R, int count, Box &B) {
     if (count == 0) {
         for (int i = 0; i < 3; i++) B.min[i] = B.max[i] = 0.0;
@@ -415,12 +454,104 @@ struct KdTree {
     }
 
     std::vector<int> tmp;
+    // cull instrumentation (g_cull_stats): the points in kd leaf order, the
+    // boxes of each 32 consecutive leaves, per grid size the list's origin
+    // and its points per cell
+    const std::vector<const double *> *pts = nullptr;
+    std::vector<int> leaf_order;
+    std::vector<Box> blocks;
+    double origin[3] = {0, 0, 0};
+    std::unordered_map<int64_t, int> cells[CULL_NGRID];
+
+    static int64_t cell_key(int64_t i, int64_t j, int64_t k) { return (i << 42) ^ (j << 21) ^ k; }
 
     void build(const std::vector<const double *> &u) {
         nodes.clear();
         tmp.resize(u.size());
         for (size_t i = 0; i < u.size(); i++) tmp[i] = (int)i;
         root = create(tmp.data(), (int)u.size(), 0, u);
+        leaf_order.clear();
+        blocks.clear();
+        pts = &u;
+        if (!g_cull_stats || (int)u.size() < CULL_MIN_LIST) return;
+        // the order a query that prunes nothing returns the points in
+        std::vector<int> st{root};
+        while (!st.empty()) {
+            const KdNode &N = nodes[st.back()];
+            st.pop_back();
+            if (N.type < 0) {
+                leaf_order.push_back(N.index);
+                continue;
+            }
+            if (g_kd_right_first) {
+                st.push_back(N.left);
+                st.push_back(N.right);
+            } else {
+                st.push_back(N.right);
+                st.push_back(N.left);
+            }
+        }
+        for (size_t b = 0; b < leaf_order.size(); b += 32) {
+            Box B;
+            for (int i = 0; i < 3; i++) {
+                B.min[i] = INFINITY;
+                B.max[i] = -INFINITY;
+            }
+            for (size_t r = b; r < leaf_order.size() && r < b + 32; r++)
+                for (int i = 0; i < 3; i++) {
+                    const double x = u[leaf_order[r]][i];
+                    B.min[i] = std::min(B.min[i], x);
+                    B.max[i] = std::max(B.max[i], x);
+                }
+            blocks.push_back(B);
+        }
+        for (int i = 0; i < 3; i++) {
+            origin[i] = INFINITY;
+            for (const double *x : u) origin[i] = std::min(origin[i], x[i]);
+        }
+        for (int g = 0; g < CULL_NGRID; g++) {
+            cells[g].clear();
+            for (const double *x : u) {
+                int64_t c[3];
+                for (int i = 0; i < 3; i++) c[i] = (int64_t)std::floor((x[i] - origin[i]) / CULL_GRID[g]);
+                cells[g][cell_key(c[0], c[1], c[2])]++;
+            }
+        }
+    }
+
+    // the counts of one query with join box B and regions R
+    void cull_count(const Box &B, const Annulus *R, int count, CullCount *cc) const {
+        if (!cc || leaf_order.empty()) return;
+        const std::vector<const double *> &u = *pts;
+        cc->queries++;
+        cc->points += (int64_t)u.size();
+        for (const double *x : u) {
+            bool in = true;
+            for (int i = 0; i < 3; i++) in = in && x[i] >= B.min[i] && x[i] <= B.max[i];
+            cc->in_box += in;
+            bool all = true;
+            for (int j = 0; j < count && all; j++) all = annulus_includes(R[j], x);
+            cc->children += all;
+        }
+        for (size_t b = 0; b < blocks.size(); b++)
+            if (box_overlaps(B, blocks[b].min, blocks[b].max)) {
+                cc->blocks_hit++;
+                cc->block_loaded += (int64_t)std::min<size_t>(32, leaf_order.size() - 32 * b);
+            }
+        for (int g = 0; g < CULL_NGRID; g++) {
+            int64_t lo[3], hi[3];
+            for (int i = 0; i < 3; i++) {
+                lo[i] = (int64_t)std::floor((B.min[i] - origin[i]) / CULL_GRID[g]);
+                hi[i] = (int64_t)std::floor((B.max[i] - origin[i]) / CULL_GRID[g]);
+            }
+            for (int64_t a = lo[0]; a <= hi[0]; a++)
+                for (int64_t b = lo[1]; b <= hi[1]; b++)
+                    for (int64_t c = lo[2]; c <= hi[2]; c++) {
+                        cc->grid_cells[g]++;
+                        const auto it = cells[g].find(cell_key(a, b, c));
+                        if (it != cells[g].end()) cc->grid_loaded[g] += it->second;
+                    }
+        }
     }
 };
 
@@ -431,21 +562,26 @@ struct KdQuery {
     Box box;
     std::vector<int> stack;
     BoundaryCount *bc = nullptr;
+    CullCount *cc = nullptr;
 
-    void reset(const KdTree *t, const Annulus *regions, int nregions, BoundaryCount *counts) {
+    void reset(const KdTree *t, const Annulus *regions, int nregions, BoundaryCount *counts,
+               CullCount *culls = nullptr) {
         tree = t;
         R = regions;
         count = nregions;
         bc = counts;
+        cc = culls && !t->leaf_order.empty() ? culls : nullptr;
         join_box(regions, nregions, box);
         stack.clear();
         stack.push_back(t->root);
+        if (cc) t->cull_count(box, regions, nregions, cc);
     }
 
     int next() {
         while (!stack.empty()) {
             const KdNode &N = tree->nodes[stack.back()];
             stack.pop_back();
+            if (cc) cc->kd_nodes++;
             if (N.type < 0) {
                 bool in = true;
                 for (int j = 0; j < count && in; j++) {
@@ -476,6 +612,7 @@ struct PairStats {
     int64_t cand = 0;        // sum |C_k|
     std::vector<int64_t> frontier;  // |F_l| per level
     BoundaryCount boundary;  // candidate-pair distance tests
+    CullCount cull;          // culling-scheme counts (g_cull_stats)
 };
 
 // ---------------------------------------------------------------------------
@@ -627,7 +764,8 @@ struct Scanner {
                 annulus_set(regions[k][j], atom[oj]->x, mn, mx);
             }
             active[ok] = 1;
-            query[ok].reset(&tree[ok], regions[k].data(), k, stats ? &stats->boundary : nullptr);
+            query[ok].reset(&tree[ok], regions[k].data(), k, stats ? &stats->boundary : nullptr,
+                            stats ? &stats->cull : nullptr);
         }
         return k >= 0;
     }
@@ -776,6 +914,7 @@ struct StructureResult {
     std::vector<Warning> warnings;
     pjg_stats stats{};
     BoundaryCount boundary;
+    CullCount cull;
 };
 
 // ---------------------------------------------------------------------------
@@ -794,6 +933,7 @@ struct JessQuery {
     PairStats pst;
     pjg_stats *stats;
     BoundaryCount *boundary;
+    CullCount *cull;
     int n_templates() const { return (int)templates->size(); }
     const Template *tpl() const { return node < n_templates() ? &(*templates)[n_templates() - 1 - node] : nullptr; }
 
@@ -803,6 +943,7 @@ struct JessQuery {
         stats->pairs++;
         boundary->tests += pst.boundary.tests;
         boundary->near += pst.boundary.near;
+        cull->add(pst.cull);
         stats->candidate_entries += pst.cand;
         stats->bytes_candidates += 8 * pst.scanned + 16 * pst.cand;
         int n = T->count();
@@ -854,6 +995,7 @@ void run_structure(const std::vector<Template> &templates, const Molecule &M, in
     Q.reorder = P.reorder != 0;
     Q.stats = &out.stats;
     Q.boundary = &out.boundary;
+    Q.cull = &out.cull;
 
     bool partial = false;
     int candidates_seen = 0;
@@ -942,11 +1084,29 @@ struct oracle_result {
     std::vector<Warning> warnings;
     pjg_stats stats{};
     BoundaryCount boundary;
+    CullCount cull;
 };
 
 extern "C" {
 
 void oracle_set_kd_right_first(int v) { g_kd_right_first = v; }
+
+// culling-scheme counts on (1) or off (0, the default), for the queries that
+// follow
+void oracle_set_cull_stats(int v) { g_cull_stats = v; }
+
+// queries, points, in_box, children, kd_nodes, blocks_hit, block_loaded, then
+// per grid size (CULL_GRID) its cells and loaded points: 7 + 2 * CULL_NGRID
+// values
+void oracle_cull_stats(const oracle_result *r, int64_t *out) {
+    const CullCount &c = r->cull;
+    const int64_t v[7] = {c.queries, c.points, c.in_box, c.children, c.kd_nodes, c.blocks_hit, c.block_loaded};
+    for (int i = 0; i < 7; i++) out[i] = v[i];
+    for (int g = 0; g < CULL_NGRID; g++) {
+        out[7 + 2 * g] = c.grid_cells[g];
+        out[8 + 2 * g] = c.grid_loaded[g];
+    }
+}
 
 oracle_result *oracle_query(const pjg_template_set *ts, const pjg_structure_set *ss,
                             const pjg_query_params *P, int n_threads, int record_stream) {
@@ -1039,6 +1199,7 @@ oracle_result *oracle_query(const pjg_template_set *ts, const pjg_structure_set 
         a.bytes_superposition += b.bytes_superposition;
         r->boundary.tests += per[s].boundary.tests;
         r->boundary.near += per[s].boundary.near;
+        r->cull.add(per[s].cull);
     }
     {
         int64_t H = (int64_t)r->hits.size();

@@ -31,6 +31,10 @@ def build() -> pathlib.Path:
     return LIB_PATH
 
 
+# cell sizes (A) of the uniform grids the culling counts model
+CULL_GRID = (2.0, 3.0, 4.0, 6.0)
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -51,17 +55,22 @@ def lib():
         L.oracle_boundary_stats.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_set_kd_right_first.argtypes = [C.c_int]
         L.oracle_set_kd_right_first(KD_RIGHT_FIRST)
+        L.oracle_set_cull_stats.argtypes = [C.c_int]
+        L.oracle_cull_stats.argtypes = [C.c_void_p, C.c_void_p]
         _lib = L
     return _lib
 
 
 def query(ptemplates, pstructures, *, rmsd_threshold, distance_cutoff, max_dynamic_distance,
           max_candidates=-1, ignore_chain=0, best_match=False, reorder=True, threads=1,
-          stream=False, kd_right_first=None):
-    """Run the oracle; returns a dict of NumPy arrays (hits, stream, warnings, stats)."""
+          stream=False, kd_right_first=None, cull_stats=False):
+    """Run the oracle; returns a dict of NumPy arrays (hits, stream, warnings, stats).
+    cull_stats: also count, for every kd range query on a list of 64 or more
+    points, the points each culling scheme would load (``out["cull"]``)."""
     L = lib()
     if kd_right_first is not None:
         L.oracle_set_kd_right_first(int(kd_right_first))
+    L.oracle_set_cull_stats(1 if cull_stats else 0)
     P = QueryParams(rmsd_threshold=rmsd_threshold, distance_cutoff=distance_cutoff,
                     max_dynamic_distance=max_dynamic_distance,
                     max_candidates=-1 if max_candidates is None else int(max_candidates),
@@ -117,6 +126,14 @@ def query(ptemplates, pstructures, *, rmsd_threshold, distance_cutoff, max_dynam
         tests, near = C.c_int64(), C.c_int64()
         L.oracle_boundary_stats(h, C.byref(tests), C.byref(near))
         out["boundary"] = {"tests": tests.value, "near": near.value}
+        if cull_stats:
+            v = np.zeros(7 + 2 * len(CULL_GRID), np.int64)
+            L.oracle_cull_stats(h, v.ctypes.data)
+            out["cull"] = {
+                **dict(zip(("queries", "points", "in_box", "children", "kd_nodes", "blocks_hit", "block_loaded"),
+                           (int(x) for x in v[:7]))),
+                "grid": {g: {"cells": int(v[7 + 2 * i]), "loaded": int(v[8 + 2 * i])}
+                         for i, g in enumerate(CULL_GRID)}}
         return out
     finally:
         L.oracle_free(h)
