@@ -305,7 +305,9 @@ struct Box { double min[3], max[3]; };
 // consecutive kd leaves whose bounding box meets the join box (the GPU
 // search's block culling), and uniform grids of cell size CULL_GRID[g] over
 // the list (every point of every cell the join box meets) -- against the
-// points inside the join box and the query's actual results.
+// points inside the join box and the query's actual results; and, within
+// the blocks that meet the box, the 8-leaf sub-blocks that do (a second
+// culling level).
 constexpr int CULL_MIN_LIST = 64;
 constexpr int CULL_NGRID = 4;
 constexpr double CULL_GRID[CULL_NGRID] = {2.0, 3.0, 4.0, 6.0};
@@ -319,6 +321,8 @@ struct CullCount {
     int64_t kd_nodes = 0;       //   kd nodes the reference's traversal visits
     int64_t blocks_hit = 0;     //   32-leaf blocks meeting the join box
     int64_t block_loaded = 0;   //   points of those blocks
+    int64_t sub_hit = 0;        //   8-leaf sub-blocks of those blocks meeting it
+    int64_t sub_loaded = 0;     //   points of those sub-blocks
     int64_t grid_cells[CULL_NGRID] = {};   // grid cells the join box meets
     int64_t grid_loaded[CULL_NGRID] = {};  //   points in them
     void add(const CullCount &o) {
@@ -329,6 +333,8 @@ struct CullCount {
         kd_nodes += o.kd_nodes;
         blocks_hit += o.blocks_hit;
         block_loaded += o.block_loaded;
+        sub_hit += o.sub_hit;
+        sub_loaded += o.sub_loaded;
         for (int g = 0; g < CULL_NGRID; g++) {
             grid_cells[g] += o.grid_cells[g];
             grid_loaded[g] += o.grid_loaded[g];
@@ -459,7 +465,7 @@ struct KdTree {
     // and its points per cell
     const std::vector<const double *> *pts = nullptr;
     std::vector<int> leaf_order;
-    std::vector<Box> blocks;
+    std::vector<Box> blocks, subs;  // boxes of 32 and of 8 consecutive leaves
     double origin[3] = {0, 0, 0};
     std::unordered_map<int64_t, int> cells[CULL_NGRID];
 
@@ -472,6 +478,7 @@ struct KdTree {
         root = create(tmp.data(), (int)u.size(), 0, u);
         leaf_order.clear();
         blocks.clear();
+        subs.clear();
         pts = &u;
         if (!g_cull_stats || (int)u.size() < CULL_MIN_LIST) return;
         // the order a query that prunes nothing returns the points in
@@ -491,19 +498,22 @@ struct KdTree {
                 st.push_back(N.left);
             }
         }
-        for (size_t b = 0; b < leaf_order.size(); b += 32) {
-            Box B;
-            for (int i = 0; i < 3; i++) {
-                B.min[i] = INFINITY;
-                B.max[i] = -INFINITY;
-            }
-            for (size_t r = b; r < leaf_order.size() && r < b + 32; r++)
+        for (int size : {32, 8}) {
+            std::vector<Box> &out = size == 32 ? blocks : subs;
+            for (size_t b = 0; b < leaf_order.size(); b += size) {
+                Box B;
                 for (int i = 0; i < 3; i++) {
-                    const double x = u[leaf_order[r]][i];
-                    B.min[i] = std::min(B.min[i], x);
-                    B.max[i] = std::max(B.max[i], x);
+                    B.min[i] = INFINITY;
+                    B.max[i] = -INFINITY;
                 }
-            blocks.push_back(B);
+                for (size_t r = b; r < leaf_order.size() && r < b + size; r++)
+                    for (int i = 0; i < 3; i++) {
+                        const double x = u[leaf_order[r]][i];
+                        B.min[i] = std::min(B.min[i], x);
+                        B.max[i] = std::max(B.max[i], x);
+                    }
+                out.push_back(B);
+            }
         }
         for (int i = 0; i < 3; i++) {
             origin[i] = INFINITY;
@@ -537,6 +547,11 @@ struct KdTree {
             if (box_overlaps(B, blocks[b].min, blocks[b].max)) {
                 cc->blocks_hit++;
                 cc->block_loaded += (int64_t)std::min<size_t>(32, leaf_order.size() - 32 * b);
+                for (size_t q = 4 * b; q < subs.size() && q < 4 * b + 4; q++)
+                    if (box_overlaps(B, subs[q].min, subs[q].max)) {
+                        cc->sub_hit++;
+                        cc->sub_loaded += (int64_t)std::min<size_t>(8, leaf_order.size() - 8 * q);
+                    }
             }
         for (int g = 0; g < CULL_NGRID; g++) {
             int64_t lo[3], hi[3];
@@ -1095,16 +1110,17 @@ void oracle_set_kd_right_first(int v) { g_kd_right_first = v; }
 // follow
 void oracle_set_cull_stats(int v) { g_cull_stats = v; }
 
-// queries, points, in_box, children, kd_nodes, blocks_hit, block_loaded, then
-// per grid size (CULL_GRID) its cells and loaded points: 7 + 2 * CULL_NGRID
-// values
+// queries, points, in_box, children, kd_nodes, blocks_hit, block_loaded,
+// sub_hit, sub_loaded, then per grid size (CULL_GRID) its cells and loaded
+// points: 9 + 2 * CULL_NGRID values
 void oracle_cull_stats(const oracle_result *r, int64_t *out) {
     const CullCount &c = r->cull;
-    const int64_t v[7] = {c.queries, c.points, c.in_box, c.children, c.kd_nodes, c.blocks_hit, c.block_loaded};
-    for (int i = 0; i < 7; i++) out[i] = v[i];
+    const int64_t v[9] = {c.queries,    c.points,       c.in_box,  c.children,  c.kd_nodes,
+                          c.blocks_hit, c.block_loaded, c.sub_hit, c.sub_loaded};
+    for (int i = 0; i < 9; i++) out[i] = v[i];
     for (int g = 0; g < CULL_NGRID; g++) {
-        out[7 + 2 * g] = c.grid_cells[g];
-        out[8 + 2 * g] = c.grid_loaded[g];
+        out[9 + 2 * g] = c.grid_cells[g];
+        out[10 + 2 * g] = c.grid_loaded[g];
     }
 }
 

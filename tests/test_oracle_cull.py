@@ -25,6 +25,8 @@ def test_cull_counts():
     # blocks the box meets, so at least those inside it, and at most all
     assert 0 < c["children"] <= c["in_box"] <= c["block_loaded"] <= c["points"]
     assert c["blocks_hit"] * 32 >= c["block_loaded"] >= c["blocks_hit"]
+    # the 8-leaf sub-blocks that meet the box lie in the blocks that do
+    assert c["in_box"] <= c["sub_loaded"] <= c["block_loaded"] and c["sub_hit"] <= 4 * c["blocks_hit"]
     cells = [c["grid"][g]["cells"] for g in oracle.CULL_GRID]
     for g in oracle.CULL_GRID:
         assert c["in_box"] <= c["grid"][g]["loaded"] <= c["points"]
