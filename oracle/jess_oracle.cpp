@@ -309,6 +309,7 @@ struct Box { double min[3], max[3]; };
 // the blocks that meet the box, the 8-leaf sub-blocks that do (a second
 // culling level).
 constexpr int CULL_MIN_LIST = 64;
+constexpr int CULL_GROUP = 4;
 constexpr int CULL_NGRID = 4;
 constexpr double CULL_GRID[CULL_NGRID] = {2.0, 3.0, 4.0, 6.0};
 int g_cull_stats = 0;
@@ -323,6 +324,10 @@ struct CullCount {
     int64_t block_loaded = 0;   //   points of those blocks
     int64_t sub_hit = 0;        //   8-leaf sub-blocks of those blocks meeting it
     int64_t sub_loaded = 0;     //   points of those sub-blocks
+    // consecutive sibling parents (same atoms below the parent's level), in
+    // groups of up to CULL_GROUP, culled once with the union of their join
+    // boxes
+    int64_t groups = 0, group_members = 0, group_blocks_hit = 0, group_loaded = 0;
     int64_t grid_cells[CULL_NGRID] = {};   // grid cells the join box meets
     int64_t grid_loaded[CULL_NGRID] = {};  //   points in them
     void add(const CullCount &o) {
@@ -335,6 +340,10 @@ struct CullCount {
         block_loaded += o.block_loaded;
         sub_hit += o.sub_hit;
         sub_loaded += o.sub_loaded;
+        groups += o.groups;
+        group_members += o.group_members;
+        group_blocks_hit += o.group_blocks_hit;
+        group_loaded += o.group_loaded;
         for (int g = 0; g < CULL_NGRID; g++) {
             grid_cells[g] += o.grid_cells[g];
             grid_loaded[g] += o.grid_loaded[g];
@@ -529,6 +538,15 @@ struct KdTree {
         }
     }
 
+    // blocks of 32 leaves a box meets, and their points
+    void blocks_met(const Box &B, int64_t *hit, int64_t *loaded) const {
+        for (size_t b = 0; b < blocks.size(); b++)
+            if (box_overlaps(B, blocks[b].min, blocks[b].max)) {
+                (*hit)++;
+                *loaded += (int64_t)std::min<size_t>(32, leaf_order.size() - 32 * b);
+            }
+    }
+
     // the counts of one query with join box B and regions R
     void cull_count(const Box &B, const Annulus *R, int count, CullCount *cc) const {
         if (!cc || leaf_order.empty()) return;
@@ -650,9 +668,28 @@ struct Scanner {
     std::vector<double> weights;
     std::vector<int> order;
     PairStats *stats = nullptr;
+    // sibling groups of the cull instrumentation, per level: the atoms below
+    // the parent's level, the union of the members' join boxes, the members
+    std::vector<uint64_t> sib_sig;
+    std::vector<Box> sib_box;
+    std::vector<int> sib_n;
+
+    void flush_group(int k) {
+        if (k >= (int)sib_n.size() || sib_n[k] == 0) return;
+        CullCount &c = stats->cull;
+        c.groups++;
+        c.group_members += sib_n[k];
+        tree[order[k]].blocks_met(sib_box[k], &c.group_blocks_hit, &c.group_loaded);
+        sib_n[k] = 0;
+    }
+    void flush_groups() {
+        if (!stats) return;
+        for (int k = 0; k < (int)sib_n.size(); k++) flush_group(k);
+    }
 
     bool reuse(const Molecule &mol, const Template &tpl, double r, double s, bool reorder,
                PairStats *st) {
+        flush_groups();
         T = &tpl;
         M = &mol;
         n = tpl.count();
@@ -781,6 +818,29 @@ struct Scanner {
             active[ok] = 1;
             query[ok].reset(&tree[ok], regions[k].data(), k, stats ? &stats->boundary : nullptr,
                             stats ? &stats->cull : nullptr);
+            if (stats && !tree[ok].leaf_order.empty()) {
+                if ((int)sib_n.size() < n) {
+                    sib_n.resize(n, 0);
+                    sib_sig.resize(n, 0);
+                    sib_box.resize(n);
+                }
+                uint64_t sig = 0x9e3779b97f4a7c15ull;
+                for (int j = 0; j + 1 < k; j++)
+                    sig = (sig ^ (uint64_t)(uintptr_t)atom[order[j]]) * 0x100000001b3ull;
+                if (sib_n[k] > 0 && sig == sib_sig[k] && sib_n[k] < CULL_GROUP) {
+                    Box &U = sib_box[k];
+                    for (int i = 0; i < 3; i++) {
+                        U.min[i] = std::min(U.min[i], query[ok].box.min[i]);
+                        U.max[i] = std::max(U.max[i], query[ok].box.max[i]);
+                    }
+                    sib_n[k]++;
+                } else {
+                    flush_group(k);
+                    sib_sig[k] = sig;
+                    sib_box[k] = query[ok].box;
+                    sib_n[k] = 1;
+                }
+            }
         }
         return k >= 0;
     }
@@ -955,6 +1015,7 @@ struct JessQuery {
     void account_pair() {
         const Template *T = tpl();
         if (!T) return;
+        S.flush_groups();
         stats->pairs++;
         boundary->tests += pst.boundary.tests;
         boundary->near += pst.boundary.near;
@@ -1111,16 +1172,18 @@ void oracle_set_kd_right_first(int v) { g_kd_right_first = v; }
 void oracle_set_cull_stats(int v) { g_cull_stats = v; }
 
 // queries, points, in_box, children, kd_nodes, blocks_hit, block_loaded,
-// sub_hit, sub_loaded, then per grid size (CULL_GRID) its cells and loaded
-// points: 9 + 2 * CULL_NGRID values
+// sub_hit, sub_loaded, groups, group_members, group_blocks_hit, group_loaded,
+// then per grid size (CULL_GRID) its cells and loaded points: 13 + 2 *
+// CULL_NGRID values
 void oracle_cull_stats(const oracle_result *r, int64_t *out) {
     const CullCount &c = r->cull;
-    const int64_t v[9] = {c.queries,    c.points,       c.in_box,  c.children,  c.kd_nodes,
-                          c.blocks_hit, c.block_loaded, c.sub_hit, c.sub_loaded};
-    for (int i = 0; i < 9; i++) out[i] = v[i];
+    const int64_t v[13] = {c.queries,    c.points,       c.in_box,  c.children,   c.kd_nodes,
+                           c.blocks_hit, c.block_loaded, c.sub_hit, c.sub_loaded, c.groups,
+                           c.group_members, c.group_blocks_hit, c.group_loaded};
+    for (int i = 0; i < 13; i++) out[i] = v[i];
     for (int g = 0; g < CULL_NGRID; g++) {
-        out[9 + 2 * g] = c.grid_cells[g];
-        out[10 + 2 * g] = c.grid_loaded[g];
+        out[13 + 2 * g] = c.grid_cells[g];
+        out[14 + 2 * g] = c.grid_loaded[g];
     }
 }
 

@@ -127,12 +127,13 @@ def query(ptemplates, pstructures, *, rmsd_threshold, distance_cutoff, max_dynam
         L.oracle_boundary_stats(h, C.byref(tests), C.byref(near))
         out["boundary"] = {"tests": tests.value, "near": near.value}
         if cull_stats:
-            v = np.zeros(9 + 2 * len(CULL_GRID), np.int64)
+            v = np.zeros(13 + 2 * len(CULL_GRID), np.int64)
             L.oracle_cull_stats(h, v.ctypes.data)
             out["cull"] = {
                 **dict(zip(("queries", "points", "in_box", "children", "kd_nodes", "blocks_hit", "block_loaded",
-                            "sub_hit", "sub_loaded"), (int(x) for x in v[:9]))),
-                "grid": {g: {"cells": int(v[9 + 2 * i]), "loaded": int(v[10 + 2 * i])}
+                            "sub_hit", "sub_loaded", "groups", "group_members", "group_blocks_hit",
+                            "group_loaded"), (int(x) for x in v[:13]))),
+                "grid": {g: {"cells": int(v[13 + 2 * i]), "loaded": int(v[14 + 2 * i])}
                          for i, g in enumerate(CULL_GRID)}}
         return out
     finally:

@@ -27,6 +27,10 @@ def test_cull_counts():
     assert c["blocks_hit"] * 32 >= c["block_loaded"] >= c["blocks_hit"]
     # the 8-leaf sub-blocks that meet the box lie in the blocks that do
     assert c["in_box"] <= c["sub_loaded"] <= c["block_loaded"] and c["sub_hit"] <= 4 * c["blocks_hit"]
+    # sibling groups: every query belongs to exactly one, and a group's
+    # union box meets at least one block (each member's results lie in it)
+    assert c["group_members"] == c["queries"] and 0 < c["groups"] <= c["queries"]
+    assert c["groups"] <= c["group_blocks_hit"] <= 32 * c["group_loaded"]
     cells = [c["grid"][g]["cells"] for g in oracle.CULL_GRID]
     for g in oracle.CULL_GRID:
         assert c["in_box"] <= c["grid"][g]["loaded"] <= c["points"]
